@@ -1,0 +1,144 @@
+/*
+ * mhdgb — C ABI of the GB300-native 3D incompressible MHD right-hand side and RK4 / LSRK4 step.
+ *
+ * This is the drop-in boundary for MHDFlows.jl's MHD hot path.  Each entry point replaces one
+ * piece of the reference's interface (paths are inside the MHDFlows.jl project):
+ *
+ *   mhd_create / mhd_destroy   Problem(dev; nx, Lx, nu, eta, nnu, B_field=true, stepper, T=Float32, dt)
+ *                              src/pgen.jl:64-127, src/Problems.jl:118-140 (grid, vars, params,
+ *                              equation with L = 0, time stepper, sol = zeros(nkr, n, n, 6))
+ *   mhd_set_physical           SetUpProblemIC!(prob; ux, uy, uz, bx, by, bz)  src/utils/IC.jl:41-109
+ *                              (host physical field -> device -> forward r2c into sol)
+ *   mhd_set_state / get_state  prob.sol (nkr, n, n, 6) ComplexF32, column-major  src/Problems.jl:130
+ *   mhd_step                   stepforward!(prob.sol, clock, ts, eqn, vars, params, grid)
+ *                              src/timestepper/timestepper.jl:4-6 (FourierFlows RK4 / LSRK4 calling
+ *                              MHDcalcN! src/pgen.jl:153-162 -> MHDcalcN_advection!
+ *                              src/Solver/MHDSolver.jl:330-351), clock.t += dt, clock.step += 1
+ *   mhd_compute_rhs            eqn.calcN!(N, sol, t, clock, vars, params, grid)  src/pgen.jl:153-162
+ *   mhd_get_physical           updatevars!(prob): vars.ux..bz <- irfft(sol)  (exported but never
+ *                              defined in the reference, src/Solver/MHDSolver.jl:10; refreshed there
+ *                              only as a side effect of calcN!, src/Solver/MHDSolver.jl:333-338)
+ *   mhd_diagnostics            ProbDiagnostic src/utils/UserInterface.jl:29,65-86 (KE, ME = sum|.|^2 dV),
+ *                              Div src/utils/VectorCalculus.jl:72-94 (div B), cross-helicity (new)
+ *   mhd_get_clock / set_clock  prob.clock (t, step, dt)  src/Problems.jl:123
+ *   mhd_last_error             the message of Julia's error(...) at the failing call
+ *
+ * Conventions: every function returns MHD_OK (0) or an MHD_ERR_* code and sets a thread-local
+ * message readable with mhd_last_error().  Host arrays are plain pointers in the reference's
+ * column-major layout; complex values are interleaved float pairs.  A handle owns all of its
+ * device memory and one CUDA stream; calls on one handle are not thread-safe, calls on different
+ * handles are.  Nothing here calls back into the host language.
+ */
+#ifndef MHDGB_H
+#define MHDGB_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MHD_OK 0
+#define MHD_ERR_INVALID 1     /* bad argument (size, field index, null pointer, unsupported n) */
+#define MHD_ERR_CUDA 2        /* CUDA runtime error (launch failure, device fault) */
+#define MHD_ERR_OOM 3         /* device or pinned-host allocation failed */
+#define MHD_ERR_NONFINITE 4   /* diagnostics found NaN/Inf in the state */
+#define MHD_ERR_STATE 5       /* call not valid in the handle's current state */
+
+#define MHD_RK4 0
+#define MHD_LSRK4 1
+
+#define MHD_PREC_FP32 0
+
+typedef struct mhd_params {
+  int n;          /* grid points per axis (nx = ny = nz); supported: 16,32,48,64,96,128,256,512 */
+  double L;       /* box side (Lx = Ly = Lz), default 2*pi */
+  double nu;      /* viscosity */
+  double eta;     /* resistivity */
+  int nnu;        /* hyper-viscosity order; values > 1 are rejected (the MHD path uses nnu <= 1) */
+  int neta;       /* hyper-resistivity order; values > 1 are rejected */
+  double dt;      /* fixed time step */
+  int scheme;     /* MHD_RK4 or MHD_LSRK4 */
+  int precision;  /* MHD_PREC_FP32 */
+  int device;     /* CUDA device ordinal */
+} mhd_params;
+
+typedef struct mhd_problem* mhd_handle;
+
+/* Problem construction (Problem(GPU(); ...), src/pgen.jl:64-127). */
+int mhd_create(const mhd_params* params, mhd_handle* out);
+int mhd_destroy(mhd_handle h);
+
+/* Supported grid sizes; returns 1 if n is supported. */
+int mhd_supported_n(int n);
+
+/* Kept (de-aliased) mode counts for size n: kx modes on the rfft axis, kp non-negative and kn
+ * negative modes on each full axis (FourierFlows getaliasedwavenumbers with aliased_fraction 1/3). */
+int mhd_kept_modes(int n, int* kx, int* kp, int* kn);
+
+/* prob.sol <-> host: complex64 interleaved, column-major (nkr, n, n, 6), nkr = n/2+1.
+ * set_state keeps only the retained (de-aliased) band; get_state writes zeros in the alias band. */
+int mhd_set_state(mhd_handle h, const float* sol);
+int mhd_get_state(mhd_handle h, float* sol);
+
+/* SetUpProblemIC!: physical field (n, n, n) float32 column-major -> forward r2c into sol[:,:,:,field]. */
+int mhd_set_physical(mhd_handle h, int field, const float* phys);
+/* updatevars!: vars.<field> <- normalised c2r of sol[:,:,:,field]. field 0..5 = ux uy uz bx by bz. */
+int mhd_get_physical(mhd_handle h, int field, float* phys);
+
+/* stepforward! x nsteps (clock.t += dt, clock.step += 1 per step). Asynchronous on the handle's
+ * stream; errors of the launches are reported, device faults surface at the next synchronising call. */
+int mhd_step(mhd_handle h, int nsteps);
+
+/* calcN!(N, sol, ...): one right-hand-side evaluation of the current state, written to rhs_out
+ * in the prob.sol layout (alias band zero). */
+int mhd_compute_rhs(mhd_handle h, float* rhs_out);
+
+/* Clock access. */
+int mhd_get_clock(mhd_handle h, double* t, long long* step, double* dt);
+int mhd_set_clock(mhd_handle h, double t, long long step, double dt);
+
+/* Diagnostics of the current state (FP64 accumulation on the device):
+ * out[0] E_u = sum |u|^2 dV      out[1] E_B = sum |B|^2 dV       (the reference's KE, ME; no 1/2)
+ * out[2] H_c = sum u.B dV        out[3] max|k.u_hat|             out[4] max|k.B_hat|
+ * out[5] max|div B| (physical)   out[6] non-finite value count   out[7] t
+ * nout >= 8. Returns MHD_ERR_NONFINITE (after filling out) if the state holds NaN/Inf. */
+int mhd_diagnostics(mhd_handle h, double* out, int nout);
+
+/* Wait for all work of the handle. */
+int mhd_synchronize(mhd_handle h);
+
+/* Use an external CUDA stream (cudaStream_t) for this handle's work; NULL restores its own. */
+int mhd_set_stream(mhd_handle h, void* stream);
+void* mhd_get_stream(mhd_handle h);
+
+/* Device bytes held by the handle (state, stage arrays, pass buffers, staging). */
+int mhd_memory_bytes(mhd_handle h, long long* bytes);
+/* Device bytes a handle of these parameters would hold, without allocating. */
+int mhd_footprint_bytes(const mhd_params* params, long long* bytes);
+
+/* Pinned host memory for fast transfers. */
+int mhd_host_alloc(size_t bytes, void** ptr);
+int mhd_host_free(void* ptr);
+
+/* Per-kernel timing with CUDA events on the handle's stream.  While enabled, mhd_step brackets
+ * every launch with events; mhd_profile_read returns, per kernel class, the launch count and the
+ * summed device milliseconds since the last enable.  Classes are named by mhd_kernel_class_name. */
+int mhd_profile_enable(mhd_handle h, int enable);
+int mhd_profile_read(mhd_handle h, long long* launches, double* ms, int nclass);
+const char* mhd_kernel_class_name(int cls);
+int mhd_kernel_class_count(void);
+/* Algorithmic HBM bytes one launch of a kernel class moves for this handle's size. */
+int mhd_kernel_class_bytes(mhd_handle h, int cls, double* bytes);
+
+/* Timing helper: elapsed device milliseconds of nsteps steps measured with events on the stream. */
+int mhd_time_steps(mhd_handle h, int nsteps, double* ms);
+
+/* Last error message of the calling thread ("" if none). */
+const char* mhd_last_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* MHDGB_H */

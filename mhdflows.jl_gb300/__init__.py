@@ -1,0 +1,358 @@
+"""GB300-native drop-in for MHDFlows.jl's 3D incompressible MHD RHS + RK4/LSRK4 step.
+
+Host-side mirror of the reference's interface for this path, over the C ABI in
+``include/mhdgb.h`` (libmhdgb.so, hand-written sm_103a CUDA):
+
+    prob = Problem(GPU(); nx=256, Lx=2pi, nu=1e-3, eta=1e-3, B_field=True, stepper="RK4",
+                   T=np.float32, dt=5e-4)                 # src/pgen.jl:64-127
+    SetUpProblemIC(prob, ux=..., uy=..., uz=..., bx=..., by=..., bz=...)   # src/utils/IC.jl:41-109
+    stepforward(prob)                                      # stepforward!(prob.sol, prob.clock, ...)
+    updatevars(prob)                                       # vars <- irfft(sol)
+    KE, ME = ProbDiagnostic(prob)                          # src/utils/UserInterface.jl:65-86
+    TimeIntegrator(prob, t0, N0, usr_dt=...)               # src/integrator.jl:31-156 (stepping part)
+
+Arrays use the reference's index order: ``prob.sol[i, j, k, f]`` is a complex64 array of shape
+(nkr, ny, nz, 6) and ``prob.vars.ux[i, j, k]`` a float32 array of shape (nx, ny, nz), both
+Fortran-ordered (the memory of a Julia Array).  There is no CPU fallback: ``Problem(CPU())``
+raises, and a missing CUDA library raises at import of the first problem.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+
+import numpy as np
+
+from . import _lib
+from ._lib import MHDError, MHD_LSRK4, MHD_RK4
+
+__all__ = [
+    "GPU", "CPU", "Problem", "SetUpProblemIC", "stepforward", "updatevars", "ProbDiagnostic",
+    "Diagnostics", "TimeIntegrator", "MHDError", "kept_modes", "supported_sizes", "footprint_bytes",
+]
+
+FIELDS = ("ux", "uy", "uz", "bx", "by", "bz")
+
+
+class GPU:
+    """Device tag (FourierFlows ``GPU()``)."""
+
+    def __init__(self, device: int = 0):
+        self.device = device
+
+    def __repr__(self):
+        return f"GPU({self.device})"
+
+
+class CPU:
+    """Device tag (FourierFlows ``CPU()``); this library has no CPU path."""
+
+
+def supported_sizes():
+    lib = _lib.load()
+    return [n for n in (16, 32, 48, 64, 96, 128, 256, 512) if lib.mhd_supported_n(n)]
+
+
+def kept_modes(n: int):
+    """(kx, kp, kn) kept modes of the 2/3 rule (FourierFlows getaliasedwavenumbers, 1/3)."""
+    lib = _lib.load()
+    a, b, c = C.c_int(), C.c_int(), C.c_int()
+    _lib.check(lib.mhd_kept_modes(n, C.byref(a), C.byref(b), C.byref(c)))
+    return a.value, b.value, c.value
+
+
+def _params(n, L, nu, eta, nnu, neta, dt, scheme, device):
+    return _lib.MhdParams(n, L, nu, eta, nnu, neta, dt, scheme, _lib.MHD_PREC_FP32, device)
+
+
+def footprint_bytes(n: int, L: float = 2 * math.pi, stepper: str = "RK4") -> int:
+    """Device bytes one problem of size n holds (admission control of the serving loop)."""
+    lib = _lib.load()
+    p = _params(n, L, 0.0, 0.0, 0, 0, 0.0, MHD_RK4 if stepper.upper() == "RK4" else MHD_LSRK4, 0)
+    out = C.c_longlong()
+    _lib.check(lib.mhd_footprint_bytes(C.byref(p), C.byref(out)))
+    return out.value
+
+
+class Clock:
+    """FourierFlows Clock: t, step, dt (kept by the library, mirrored here)."""
+
+    def __init__(self, prob):
+        self._p = prob
+
+    def _read(self):
+        t, s, dt = C.c_double(), C.c_longlong(), C.c_double()
+        _lib.check(self._p._lib.mhd_get_clock(self._p._h, C.byref(t), C.byref(s), C.byref(dt)))
+        return t.value, s.value, dt.value
+
+    @property
+    def t(self):
+        return self._read()[0]
+
+    @t.setter
+    def t(self, v):
+        _, s, dt = self._read()
+        _lib.check(self._p._lib.mhd_set_clock(self._p._h, float(v), s, dt))
+
+    @property
+    def step(self):
+        return self._read()[1]
+
+    @step.setter
+    def step(self, v):
+        t, _, dt = self._read()
+        _lib.check(self._p._lib.mhd_set_clock(self._p._h, t, int(v), dt))
+
+    @property
+    def dt(self):
+        return self._read()[2]
+
+    @dt.setter
+    def dt(self, v):
+        t, s, _ = self._read()
+        _lib.check(self._p._lib.mhd_set_clock(self._p._h, t, s, float(v)))
+
+
+class Vars:
+    """Physical fields ux..bz (MVars, src/Structure/MHDVars.jl:1-24), filled by updatevars."""
+
+    def __init__(self, n):
+        for f in FIELDS:
+            setattr(self, f, np.zeros((n, n, n), dtype=np.float32, order="F"))
+
+
+class Params:
+    def __init__(self, nu, eta, nnu, neta):
+        self.nu, self.eta, self.nnu, self.neta = nu, eta, nnu, neta
+        self.ν, self.η, self.nν, self.nη = nu, eta, nnu, neta
+        self.ux_ind, self.uy_ind, self.uz_ind, self.bx_ind, self.by_ind, self.bz_ind = 1, 2, 3, 4, 5, 6
+
+
+class Grid:
+    """Grid quantities the host needs (ThreeDGrid conventions: centred x, kr, l, m)."""
+
+    def __init__(self, n, L):
+        self.nx = self.ny = self.nz = n
+        self.Lx = self.Ly = self.Lz = L
+        self.nkr = n // 2 + 1
+        self.dx = self.dy = self.dz = L / n
+        self.x = (-L / 2 + self.dx * np.arange(n)).astype(np.float32)
+        self.y = self.x.copy()
+        self.z = self.x.copy()
+        self.kr = (2 * math.pi / L) * np.arange(self.nkr, dtype=np.float32)
+        self.l = ((2 * math.pi / L) * np.fft.fftfreq(n, 1.0 / n)).astype(np.float32)
+        self.m = self.l.copy()
+
+
+class Problem:
+    """``Problem(GPU(); nx, Lx, ν/nu, η/eta, nν, nη, B_field=True, stepper, T=Float32, dt)``.
+
+    Only the MHD branch of src/pgen.jl:64-127 lives on this path: ``B_field`` must be true and
+    EMHD, compressibility, shear, VP, dye and forcing must be off.
+    """
+
+    def __init__(self, dev=None, *, nx=64, ny=None, nz=None, Lx=2 * math.pi, Ly=None, Lz=None,
+                 dt=0.0, nu=None, eta=None, nnu=0, neta=0, B_field=True, EMHD=False,
+                 Compressibility=False, Shear=False, VP_method=False, Dye_Module=False,
+                 stepper="RK4", calcF=None, T=np.float32, aliased_fraction=1 / 3, **kw):
+        nu = kw.pop("ν", nu)
+        eta = kw.pop("η", eta)
+        nnu = kw.pop("nν", nnu)
+        neta = kw.pop("nη", neta)
+        if kw:
+            raise TypeError(f"unexpected keyword arguments: {sorted(kw)}")
+        if dev is None:
+            dev = GPU()
+        if isinstance(dev, CPU) or dev is CPU:
+            raise MHDError(_lib.MHD_ERR_INVALID, "this library runs on the GPU only: use Problem(GPU(); ...)")
+        if not B_field:
+            raise MHDError(_lib.MHD_ERR_INVALID, "only the MHD path (B_field=true) is provided")
+        if EMHD or Compressibility or Shear or VP_method or Dye_Module or calcF is not None:
+            raise MHDError(_lib.MHD_ERR_INVALID, "EMHD, compressibility, shear, VP, dye and forcing are not on this path")
+        if (ny not in (None, nx)) or (nz not in (None, nx)) or (Ly not in (None, Lx)) or (Lz not in (None, Lx)):
+            raise MHDError(_lib.MHD_ERR_INVALID, "only cubic boxes (nx = ny = nz, Lx = Ly = Lz) are provided")
+        if np.dtype(T) != np.float32:
+            raise MHDError(_lib.MHD_ERR_INVALID, "the plain form computes in Float32 (T=Float32)")
+        if abs(aliased_fraction - 1 / 3) > 1e-12:
+            raise MHDError(_lib.MHD_ERR_INVALID, "aliased_fraction is fixed at 1/3 (the reference does not forward it)")
+        scheme = {"RK4": MHD_RK4, "LSRK4": MHD_LSRK4}.get(str(stepper).upper())
+        if scheme is None:
+            raise MHDError(_lib.MHD_ERR_INVALID, f"unknown stepper {stepper!r} (RK4 or LSRK4)")
+        self._lib = _lib.load()
+        self.n = int(nx)
+        self.L = float(Lx)
+        self.stepper = str(stepper).upper()
+        p = _params(self.n, self.L, float(nu or 0.0), float(eta or 0.0), int(nnu), int(neta), float(dt),
+                    scheme, dev.device)
+        h = C.c_void_p()
+        _lib.check(self._lib.mhd_create(C.byref(p), C.byref(h)))
+        self._h = h
+        self.grid = Grid(self.n, self.L)
+        self.params = Params(float(nu or 0.0), float(eta or 0.0), int(nnu), int(neta))
+        self.vars = Vars(self.n)
+        self.clock = Clock(self)
+        self.device = dev
+
+    # -- lifecycle
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.mhd_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    @property
+    def handle(self):
+        return self._h
+
+    # -- state
+    @property
+    def sol(self):
+        """Copy of prob.sol, complex64 (nkr, n, n, 6) Fortran order; alias band is zero."""
+        out = np.empty((6, self.n, self.n, self.grid.nkr), dtype=np.complex64)
+        _lib.check(self._lib.mhd_get_state(self._h, out.ctypes.data))
+        return out.T
+
+    @sol.setter
+    def sol(self, value):
+        self.set_sol(value)
+
+    def set_sol(self, value):
+        a = np.asarray(value)
+        if a.shape == (self.grid.nkr, self.n, self.n, 6):
+            a = a.T
+        if a.shape != (6, self.n, self.n, self.grid.nkr):
+            raise MHDError(_lib.MHD_ERR_INVALID, f"sol must have shape (nkr, n, n, 6) = {(self.grid.nkr, self.n, self.n, 6)}")
+        a = np.ascontiguousarray(a, dtype=np.complex64)
+        _lib.check(self._lib.mhd_set_state(self._h, a.ctypes.data))
+
+    def sol_c(self):
+        """prob.sol as a C-ordered (6, nz, ny, nkr) array (same memory order as the Julia array)."""
+        out = np.empty((6, self.n, self.n, self.grid.nkr), dtype=np.complex64)
+        _lib.check(self._lib.mhd_get_state(self._h, out.ctypes.data))
+        return out
+
+    def rhs_c(self):
+        """calcN!(N, sol, ...) of the current state, C-ordered (6, nz, ny, nkr)."""
+        out = np.empty((6, self.n, self.n, self.grid.nkr), dtype=np.complex64)
+        _lib.check(self._lib.mhd_compute_rhs(self._h, out.ctypes.data))
+        return out
+
+    def physical_c(self, field: int):
+        out = np.empty((self.n, self.n, self.n), dtype=np.float32)
+        _lib.check(self._lib.mhd_get_physical(self._h, int(field), out.ctypes.data))
+        return out
+
+    def set_physical_c(self, field: int, arr):
+        a = np.ascontiguousarray(arr, dtype=np.float32)
+        if a.shape != (self.n, self.n, self.n):
+            raise MHDError(_lib.MHD_ERR_INVALID, "physical fields are (n, n, n)")
+        _lib.check(self._lib.mhd_set_physical(self._h, int(field), a.ctypes.data))
+
+    def synchronize(self):
+        _lib.check(self._lib.mhd_synchronize(self._h))
+
+    def memory_bytes(self):
+        b = C.c_longlong()
+        _lib.check(self._lib.mhd_memory_bytes(self._h, C.byref(b)))
+        return b.value
+
+    def diagnostics(self):
+        out = (C.c_double * 8)()
+        rc = self._lib.mhd_diagnostics(self._h, out, 8)
+        d = Diagnostics(*list(out))
+        if rc == _lib.MHD_ERR_NONFINITE:
+            raise MHDError(rc, self._lib.mhd_last_error().decode())
+        _lib.check(rc)
+        return d
+
+    def __repr__(self):
+        return (f"MHDFlows Problem (GB300)\n  grid: {self.n}^3, L = {self.L:.6g}\n  stepper: {self.stepper}\n"
+                f"  nu = {self.params.nu}, eta = {self.params.eta}, dt = {self.clock.dt}")
+
+
+class Diagnostics:
+    """Result of mhd_diagnostics (FP64 accumulation on the device)."""
+
+    __slots__ = ("E_u", "E_B", "H_c", "max_kdotu", "max_kdotb", "max_divb", "nonfinite", "t")
+
+    def __init__(self, E_u, E_B, H_c, max_kdotu, max_kdotb, max_divb, nonfinite, t):
+        self.E_u, self.E_B, self.H_c = E_u, E_B, H_c
+        self.max_kdotu, self.max_kdotb, self.max_divb = max_kdotu, max_kdotb, max_divb
+        self.nonfinite, self.t = nonfinite, t
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k in self.__slots__}
+
+
+def _to_c_phys(a, n):
+    a = np.asarray(a)
+    if a.shape != (n, n, n):
+        raise MHDError(_lib.MHD_ERR_INVALID, f"initial fields must be (nx, ny, nz) = {(n, n, n)}")
+    # Julia (nx, ny, nz) column-major == C-ordered (nz, ny, nx): transpose the index order
+    return np.ascontiguousarray(np.asarray(a, dtype=np.float32).T)
+
+
+def SetUpProblemIC(prob: Problem, *, ux=None, uy=None, uz=None, bx=None, by=None, bz=None):
+    """SetUpProblemIC!(prob; ux, ..., bz) (src/utils/IC.jl:41-109): host field -> device -> r2c."""
+    for f, arr in enumerate((ux, uy, uz, bx, by, bz)):
+        if arr is None:
+            continue
+        c = _to_c_phys(arr, prob.n)
+        prob.set_physical_c(f, c)
+        getattr(prob.vars, FIELDS[f])[...] = c.T
+    return None
+
+
+def stepforward(prob: Problem, nsteps: int = 1):
+    """stepforward!(prob.sol, prob.clock, prob.timestepper, ...): advance nsteps (default 1)."""
+    _lib.check(prob._lib.mhd_step(prob._h, int(nsteps)))
+    return None
+
+
+def updatevars(prob: Problem):
+    """updatevars!(prob): vars.ux..bz <- normalised c2r of the current sol."""
+    for f, name in enumerate(FIELDS):
+        getattr(prob.vars, name)[...] = prob.physical_c(f).T
+    return None
+
+
+def ProbDiagnostic(prob: Problem):
+    """(KE, ME) = (sum |u|^2 dV, sum |B|^2 dV) of the current state, rounded to 3 significant
+    digits like src/utils/UserInterface.jl:65-86; NaN raises."""
+    d = prob.diagnostics()
+
+    def r3(x):
+        return float(f"{x:.3g}")
+
+    return r3(d.E_u), r3(d.E_B)
+
+
+def TimeIntegrator(prob: Problem, t0: float, N0: int, *, usr_dt: float = 0.0, diags=(), loop_number=100):
+    """Stepping part of TimeIntegrator! (src/integrator.jl:104-113): runs while N0 >= step and
+    t0 >= t, i.e. N0+1 steps from step 0, like the reference.  A fixed ``usr_dt`` is required
+    (the CFL path is not part of this drop-in).  Returns zone updates per second."""
+    import time
+
+    if usr_dt <= 0:
+        raise MHDError(_lib.MHD_ERR_INVALID, "TimeIntegrator on this path needs a fixed usr_dt > 0")
+    prob.clock.dt = usr_dt
+    prob.clock.step = 0
+    start = time.perf_counter()
+    while N0 >= prob.clock.step and t0 >= prob.clock.t:
+        stepforward(prob)
+        for d in diags:
+            d(prob)
+    prob.synchronize()
+    el = time.perf_counter() - start
+    return prob.clock.step * prob.n ** 3 / el if el > 0 else float("inf")

@@ -1,0 +1,321 @@
+// Register-resident mixed-radix FFT building blocks for the MHD pass kernels (sm_103a).
+//
+// A length-N transform is spread over G cooperating threads that each hold V = N/G complex
+// values in registers.  N = R0*R1*R2 (R2 may be 1) and every radix divides V, so each stage is
+// V/R_s small DFTs per thread, done fully unrolled in registers (Cooley-Tukey codelets built from
+// radix-2/3/4 butterflies).  Between stages the values are exchanged through shared memory; the
+// stage twiddles W_N^j come from a per-size table computed in double precision on the host.
+//
+// Index conventions (DIR = -1 forward, +1 inverse, X[k] = sum_n x[n] exp(DIR*2*pi*i*n*k/N)):
+//   input  n = n0*(R1*R2) + n1*R2 + n2        (stage-1 label l1 = n1*R2 + n2 = n mod R1*R2)
+//   output k = k0 + k1*R0 + k2*R0*R1          (last-stage label lF = k mod (N/RF))
+// A thread with lane g owns labels l = g + G*d, d = 0..V/R-1, for every stage, so a transform
+// with radices (R0,R1,R2) leaves its outputs exactly where a transform with the reversed radices
+// (R2,R1,R0) expects its inputs: the physical-space product step between an inverse and a
+// forward row transform needs no data movement at all.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace mhdgb {
+
+// ------------------------------------------------------------------------------------------
+// Compile-time trigonometry (Taylor series in double, argument reduced to [-pi, pi]) used only
+// to build the constant twiddles inside the small register codelets.
+// ------------------------------------------------------------------------------------------
+__host__ __device__ constexpr double k_pi() { return 3.141592653589793238462643383279502884; }
+
+__host__ __device__ constexpr double taylor_sin(double x) {
+  double term = x, sum = x;
+  for (int i = 1; i < 28; ++i) {
+    term *= -x * x / ((2.0 * i) * (2.0 * i + 1.0));
+    sum += term;
+  }
+  return sum;
+}
+__host__ __device__ constexpr double taylor_cos(double x) {
+  double term = 1.0, sum = 1.0;
+  for (int i = 1; i < 28; ++i) {
+    term *= -x * x / ((2.0 * i - 1.0) * (2.0 * i));
+    sum += term;
+  }
+  return sum;
+}
+// cos / sin of 2*pi*j/R with exact values on the axes.
+__host__ __device__ constexpr double unit_cos(int j, int R) {
+  j %= R; if (j < 0) j += R;
+  if (4 * j == 0) return 1.0;
+  if (4 * j == R || 4 * j == 3 * R) return 0.0;
+  if (2 * j == R) return -1.0;
+  int jj = (2 * j > R) ? j - R : j;
+  return taylor_cos(2.0 * k_pi() * jj / R);
+}
+__host__ __device__ constexpr double unit_sin(int j, int R) {
+  j %= R; if (j < 0) j += R;
+  if (j == 0 || 2 * j == R) return 0.0;
+  if (4 * j == R) return 1.0;
+  if (4 * j == 3 * R) return -1.0;
+  int jj = (2 * j > R) ? j - R : j;
+  return taylor_sin(2.0 * k_pi() * jj / R);
+}
+
+template <int R>
+struct TwTab {
+  float c[R];
+  float s[R];
+  __host__ __device__ constexpr TwTab() : c(), s() {
+    for (int j = 0; j < R; ++j) {
+      c[j] = (float)unit_cos(j, R);
+      s[j] = (float)unit_sin(j, R);
+    }
+  }
+};
+
+// ------------------------------------------------------------------------------------------
+// Complex helpers
+// ------------------------------------------------------------------------------------------
+__device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+__device__ __forceinline__ float2 cscale(float2 a, float s) { return make_float2(a.x * s, a.y * s); }
+__device__ __forceinline__ float2 cconj(float2 a) { return make_float2(a.x, -a.y); }
+// a * (c + i*DIR*s)
+template <int DIR>
+__device__ __forceinline__ float2 cmul_cs(float2 a, float c, float s) {
+  const float ds = DIR * s;
+  return make_float2(fmaf(a.x, c, -a.y * ds), fmaf(a.x, ds, a.y * c));
+}
+// a * (DIR * i)
+template <int DIR>
+__device__ __forceinline__ float2 cmul_diri(float2 a) {
+  return DIR > 0 ? make_float2(-a.y, a.x) : make_float2(a.y, -a.x);
+}
+
+// ------------------------------------------------------------------------------------------
+// Small in-register DFT codelets: x[0..R) in place, natural-order output.
+// ------------------------------------------------------------------------------------------
+template <int R>
+struct FirstFactor {
+  static constexpr int value = (R % 4 == 0 && R != 4) ? 4 : (R % 2 == 0 && R != 2) ? 2 : (R % 3 == 0 && R != 3) ? 3 : R;
+};
+
+template <int R, int DIR>
+struct Dft;
+
+template <int DIR>
+struct Dft<1, DIR> {
+  template <int S, int O, int A>
+  __device__ __forceinline__ static void run(float2 (&)[A]) {}
+};
+
+template <int DIR>
+struct Dft<2, DIR> {
+  // operates on x[O], x[O+S]
+  template <int S, int O, int A>
+  __device__ __forceinline__ static void run(float2 (&x)[A]) {
+    float2 a = x[O], b = x[O + S];
+    x[O] = cadd(a, b);
+    x[O + S] = csub(a, b);
+  }
+};
+
+template <int DIR>
+struct Dft<3, DIR> {
+  template <int S, int O, int A>
+  __device__ __forceinline__ static void run(float2 (&x)[A]) {
+    const float h = 0.86602540378443864676f;  // sqrt(3)/2
+    float2 x0 = x[O], x1 = x[O + S], x2 = x[O + 2 * S];
+    float2 t1 = cadd(x1, x2);
+    float2 t2 = make_float2(fmaf(-0.5f, t1.x, x0.x), fmaf(-0.5f, t1.y, x0.y));
+    float2 d = csub(x1, x2);
+    float2 t3 = cmul_diri<DIR>(cscale(d, h));
+    x[O] = cadd(x0, t1);
+    x[O + S] = cadd(t2, t3);
+    x[O + 2 * S] = csub(t2, t3);
+  }
+};
+
+template <int DIR>
+struct Dft<4, DIR> {
+  template <int S, int O, int A>
+  __device__ __forceinline__ static void run(float2 (&x)[A]) {
+    float2 x0 = x[O], x1 = x[O + S], x2 = x[O + 2 * S], x3 = x[O + 3 * S];
+    float2 a = cadd(x0, x2), b = csub(x0, x2);
+    float2 c = cadd(x1, x3), d = cmul_diri<DIR>(csub(x1, x3));
+    x[O] = cadd(a, c);
+    x[O + 2 * S] = csub(a, c);
+    x[O + S] = cadd(b, d);
+    x[O + 3 * S] = csub(b, d);
+  }
+};
+
+// Composite R = P*Q (P = FirstFactor): x[n], n = Q*a + b;  X[k], k = ka + P*kb.
+// The element set is x[O + S*i], i = 0..R-1 (strided view inside a register array).
+template <int R, int DIR>
+struct Dft {
+  static constexpr int P = FirstFactor<R>::value;
+  static constexpr int Q = R / P;
+  static_assert(P * Q == R && P > 1 && Q > 1, "unsupported radix");
+
+  template <int S, int O, int A>
+  __device__ __forceinline__ static void run(float2 (&x)[A]) {
+    constexpr TwTab<R> tw{};
+    // step 1: Q DFTs of size P over a (elements O + S*(Q*a + b))
+#pragma unroll
+    for (int b = 0; b < Q; ++b) {
+      float2 t[P];
+#pragma unroll
+      for (int a = 0; a < P; ++a) t[a] = x[O + S * (Q * a + b)];
+      Dft<P, DIR>::template run<1, 0>(t);
+      // twiddle W_R^{b*ka}
+#pragma unroll
+      for (int ka = 0; ka < P; ++ka) {
+        const int e = (b * ka) % R;
+        if (e != 0) t[ka] = cmul_cs<DIR>(t[ka], tw.c[e], tw.s[e]);
+        x[O + S * (Q * ka + b)] = t[ka];
+      }
+    }
+    // step 2: P DFTs of size Q over b (elements O + S*(Q*ka + b)), output k = ka + P*kb
+    float2 out[R];
+#pragma unroll
+    for (int ka = 0; ka < P; ++ka) {
+      float2 t[Q];
+#pragma unroll
+      for (int b = 0; b < Q; ++b) t[b] = x[O + S * (Q * ka + b)];
+      Dft<Q, DIR>::template run<1, 0>(t);
+#pragma unroll
+      for (int kb = 0; kb < Q; ++kb) out[ka + P * kb] = t[kb];
+    }
+#pragma unroll
+    for (int k = 0; k < R; ++k) x[O + S * k] = out[k];
+  }
+};
+
+// Run DFT-R on each of the D = A/R contiguous groups of a register array.
+template <int R, int DIR, int A>
+__device__ __forceinline__ void dft_groups(float2 (&x)[A]) {
+  static_assert(A % R == 0, "radix must divide the per-thread count");
+#pragma unroll
+  for (int d = 0; d < A / R; ++d) {
+    float2 t[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) t[r] = x[d * R + r];
+    Dft<R, DIR>::template run<1, 0>(t);
+#pragma unroll
+    for (int r = 0; r < R; ++r) x[d * R + r] = t[r];
+  }
+}
+
+// ------------------------------------------------------------------------------------------
+// Multi-stage thread-distributed plan.
+// ------------------------------------------------------------------------------------------
+template <int N_, int G_, int R0_, int R1_, int R2_ = 1>
+struct Plan {
+  static constexpr int N = N_, G = G_, V = N_ / G_;
+  static constexpr int R0 = R0_, R1 = R1_, R2 = R2_;
+  static_assert(R0 * R1 * R2 == N, "radices must multiply to N");
+  static_assert(V * G == N, "G must divide N");
+  static_assert(V % R0 == 0 && V % R1 == 0 && V % R2 == 0, "radices must divide V");
+  static constexpr int STAGES = (R2 == 1) ? 2 : 3;
+  static constexpr int RF = (R2 == 1) ? R1 : R2;      // last radix
+  static constexpr int LI = N / R0;                    // input label count
+  static constexpr int LF = N / RF;                    // output label count
+  static constexpr int DI = V / R0;                    // input slots per thread
+  static constexpr int DF = V / RF;                    // output slots per thread
+  // shared-memory exchange strides (padding spreads 8-byte words over banks for row layouts)
+  static constexpr int P1 = 1;
+  static constexpr int E1S = R1 * R2 + P1;
+  static constexpr int P2 = (R0 * R1) % 16 == 0 ? (R0 % 16) : 0;
+  static constexpr int E2S = R0 * R1 + P2;
+  static constexpr int SMEM1 = R0 * E1S;              // words used by exchange 1
+  static constexpr int SMEM2 = R2 * E2S;              // words used by exchange 2
+  static constexpr int SMEM = (STAGES == 3 && SMEM2 > SMEM1) ? SMEM2 : SMEM1;
+};
+
+// Reversed-radix plan: its input layout equals the output layout of P.
+template <class P>
+struct Reverse;
+template <int N, int G, int R0, int R1>
+struct Reverse<Plan<N, G, R0, R1, 1>> { using type = Plan<N, G, R1, R0, 1>; };
+template <int N, int G, int R0, int R1, int R2>
+struct Reverse<Plan<N, G, R0, R1, R2>> { using type = Plan<N, G, R2, R1, R0>; };
+
+__device__ __forceinline__ float2 ldtw(const float2* __restrict__ tw, int j) { return __ldg(tw + j); }
+
+// Executes stages of plan P on NT independent transforms held as v[t][V] by this thread.
+// Shared memory word address of logical element a for transform t is  buf[t*TS + a*STR + OFF].
+// SYNC() must be a barrier over every thread that shares buf.
+// Input: v[t][d*R0 + n0] = x[l1 + LI*n0] with l1 = g + G*d.
+// Output: v[t][d*RF + e] = X[lF + LF*e] with lF = g + G*d.
+template <class P, int DIR, int NT, int TS, int STR, class SyncF>
+__device__ __forceinline__ void fft_run(float2 (&v)[NT][P::V], float2* buf, int off, int g,
+                                        const float2* __restrict__ tw, SyncF SYNC) {
+  constexpr int V = P::V, G = P::G, R0 = P::R0, R1 = P::R1, R2 = P::R2, N = P::N;
+  // ---- stage 1: DFT-R0 over n0
+#pragma unroll
+  for (int t = 0; t < NT; ++t) dft_groups<R0, DIR>(v[t]);
+  // ---- exchange 1: write Y1[k0; l1] at k0*E1S + l1
+#pragma unroll
+  for (int t = 0; t < NT; ++t)
+#pragma unroll
+    for (int d = 0; d < V / R0; ++d) {
+      const int l1 = g + G * d;
+#pragma unroll
+      for (int k0 = 0; k0 < R0; ++k0) buf[t * TS + (k0 * P::E1S + l1) * STR + off] = v[t][d * R0 + k0];
+    }
+  SYNC();
+  // ---- read for stage 2: label l2 = k0 + R0*n2, elements n1
+#pragma unroll
+  for (int t = 0; t < NT; ++t)
+#pragma unroll
+    for (int d = 0; d < V / R1; ++d) {
+      const int l2 = g + G * d;
+      const int k0 = l2 % R0, n2 = l2 / R0;
+#pragma unroll
+      for (int n1 = 0; n1 < R1; ++n1) {
+        float2 a = buf[t * TS + (k0 * P::E1S + n1 * R2 + n2) * STR + off];
+        const int e = ((n1 * k0) % (R0 * R1)) * R2;  // W_{R0R1}^{n1 k0} = W_N^{n1 k0 R2}
+        if (n1 != 0 && k0 != 0) {
+          float2 w = ldtw(tw, e);
+          a = cmul_cs<DIR>(a, w.x, w.y);
+        }
+        v[t][d * R1 + n1] = a;
+      }
+    }
+  // ---- stage 2: DFT-R1 over n1
+#pragma unroll
+  for (int t = 0; t < NT; ++t) dft_groups<R1, DIR>(v[t]);
+  if constexpr (P::STAGES == 3) {
+    SYNC();  // every thread finished reading exchange 1
+    // twiddle W_N^{n2 (k0 + R0 k1)} and exchange 2: write at n2*E2S + l3, l3 = k0 + R0*k1
+#pragma unroll
+    for (int t = 0; t < NT; ++t)
+#pragma unroll
+      for (int d = 0; d < V / R1; ++d) {
+        const int l2 = g + G * d;
+        const int k0 = l2 % R0, n2 = l2 / R0;
+#pragma unroll
+        for (int k1 = 0; k1 < R1; ++k1) {
+          float2 a = v[t][d * R1 + k1];
+          const int l3 = k0 + R0 * k1;
+          if (n2 != 0 && l3 != 0) {
+            float2 w = ldtw(tw, (n2 * l3) % N);
+            a = cmul_cs<DIR>(a, w.x, w.y);
+          }
+          buf[t * TS + (n2 * P::E2S + l3) * STR + off] = a;
+        }
+      }
+    SYNC();
+#pragma unroll
+    for (int t = 0; t < NT; ++t)
+#pragma unroll
+      for (int d = 0; d < V / R2; ++d) {
+        const int l3 = g + G * d;
+#pragma unroll
+        for (int n2 = 0; n2 < R2; ++n2) v[t][d * R2 + n2] = buf[t * TS + (n2 * P::E2S + l3) * STR + off];
+      }
+#pragma unroll
+    for (int t = 0; t < NT; ++t) dft_groups<R2, DIR>(v[t]);
+  }
+}
+
+}  // namespace mhdgb

@@ -1,0 +1,537 @@
+// Pass kernels of the pruned pseudospectral MHD right-hand side (sm_103a).
+//
+// Data layouts in HBM (complex = float2, kx fastest everywhere, rows padded to kxp):
+//   state   S[f][kz'][ky'][kx]          retained band only (kx < Kx, ky', kz' kept indices)
+//   colbuf  A[z][ky'][slot][kx]         after the z pass (inverse) / before it (forward)
+//   rowbuf  B[z][y][slot][kx]           after the y pass (inverse) / before it (forward)
+// 8 slots per (z, ky') and (z, y): fields 0..5 on the way in, products 0..7 on the way out.
+// A kept index j maps to frequency index j (j < Kp) or j + n - K2 (negative wavenumbers).
+#pragma once
+#include "fft_core.cuh"
+
+namespace mhdgb {
+
+struct Geom {
+  int n;      // points per axis
+  int kx;     // kept rfft-axis modes
+  int kxp;    // padded row length
+  int kp;     // kept non-negative full-axis modes
+  int kn;     // kept negative full-axis modes
+  int k2;     // kp + kn
+  float kscale;  // 2*pi/L
+};
+
+__host__ __device__ __forceinline__ int kept_of_freq(const Geom& g, int f) {
+  return f < g.kp ? f : (f >= g.n - g.kn ? f - g.n + g.k2 : -1);
+}
+__host__ __device__ __forceinline__ int freq_of_kept(const Geom& g, int j) { return j < g.kp ? j : j + g.n - g.k2; }
+__host__ __device__ __forceinline__ int signed_of_kept(const Geom& g, int j) { return j < g.kp ? j : j - g.k2; }
+
+struct BlockSync {
+  __device__ __forceinline__ void operator()() const { __syncthreads(); }
+};
+
+struct ColArgs {
+  const float2* src;
+  float2* dst;
+  long long sF, sO, sR;  // source strides (complex elements): field/slot, outer, row
+  long long dF, dO, dR;  // destination strides
+  float scale;           // applied to every loaded value
+};
+
+// ------------------------------------------------------------------------------------------
+// Column pass: one length-n transform per (field, outer index, kx column); TX columns per CTA.
+// PIN: input rows are kept indices (pruned inverse input).  POUT: only kept outputs stored.
+// ------------------------------------------------------------------------------------------
+template <class P, int TX, int DIR, bool PIN, bool POUT>
+__global__ void __launch_bounds__(TX * P::G) col_pass_kernel(ColArgs a, Geom geo, const float2* __restrict__ tw) {
+  extern __shared__ float2 smem[];
+  constexpr int G = P::G, V = P::V;
+  const int tx = threadIdx.x % TX, g = threadIdx.x / TX;
+  const int kxg = blockIdx.x * TX + tx;
+  const bool colok = kxg < geo.kx;
+  const float2* src = a.src + blockIdx.z * a.sF + (long long)blockIdx.y * a.sO + kxg;
+  float2* dst = a.dst + blockIdx.z * a.dF + (long long)blockIdx.y * a.dO + kxg;
+  float2 v[1][V];
+#pragma unroll
+  for (int d = 0; d < P::DI; ++d)
+#pragma unroll
+    for (int n0 = 0; n0 < P::R0; ++n0) {
+      const int n = g + G * d + P::LI * n0;
+      const int row = PIN ? kept_of_freq(geo, n) : n;
+      float2 x = make_float2(0.f, 0.f);
+      if (colok && row >= 0) x = cscale(__ldg(src + row * a.sR), a.scale);
+      v[0][d * P::R0 + n0] = x;
+    }
+  fft_run<P, DIR, 1, 0, TX>(v, smem, tx, g, tw, BlockSync{});
+#pragma unroll
+  for (int d = 0; d < P::DF; ++d)
+#pragma unroll
+    for (int e = 0; e < P::RF; ++e) {
+      const int k = g + G * d + P::LF * e;
+      const int row = POUT ? kept_of_freq(geo, k) : k;
+      if (colok && row >= 0) dst[row * a.dR] = v[0][d * P::RF + e];
+    }
+}
+
+// ------------------------------------------------------------------------------------------
+// x rows: Hermitian two-for-one helpers.
+// ------------------------------------------------------------------------------------------
+// Input of an inverse (c2r) transform of two half-spectrum rows f1, f2 with kx kept modes:
+// z[n] = F1[n] + i F2[n] with F[n-n] = conj(F[n]); the kx = 0 imaginary parts are dropped,
+// which is what a c2r transform does with a non-Hermitian kx = 0 plane.
+template <class P>
+__device__ __forceinline__ void load_herm_pair(float2 (&v)[P::V], const float2* __restrict__ f1,
+                                               const float2* __restrict__ f2, int kx, int g) {
+#pragma unroll
+  for (int d = 0; d < P::DI; ++d)
+#pragma unroll
+    for (int n0 = 0; n0 < P::R0; ++n0) {
+      const int n = g + P::G * d + P::LI * n0;
+      float2 z = make_float2(0.f, 0.f);
+      if (n < kx) {
+        float2 a = __ldg(f1 + n), b = __ldg(f2 + n);
+        if (n == 0) { a.y = 0.f; b.y = 0.f; }
+        z = make_float2(a.x - b.y, a.y + b.x);
+      } else if (n > P::N - kx) {
+        const int m = P::N - n;
+        float2 a = __ldg(f1 + m), b = __ldg(f2 + m);
+        z = make_float2(a.x + b.y, b.x - a.y);
+      }
+      v[d * P::R0 + n0] = z;
+    }
+}
+
+// Split Z = FFT(pa + i pb) into the half spectra of pa and pb for k < kx and store them.
+// sb holds Z[k] for every needed k (k < kx and k > n - kx).
+__device__ __forceinline__ void store_split_pair(const float2* sb, int n, int kx, int g, int G,
+                                                 float2* outa, float2* outb) {
+  for (int k = g; k < kx; k += G) {
+    const float2 z = sb[k];
+    const float2 zc = cconj(sb[(n - k) % n]);
+    const float2 s = cadd(z, zc), df = csub(z, zc);
+    outa[k] = make_float2(0.5f * s.x, 0.5f * s.y);
+    outb[k] = make_float2(0.5f * df.y, -0.5f * df.x);
+  }
+}
+
+template <class P>
+struct RowCfg {
+  using PR = typename Reverse<P>::type;
+  static constexpr int a = P::SMEM > PR::SMEM ? P::SMEM : PR::SMEM;
+  static constexpr int TS = a > P::N ? a : P::N;  // words per transform buffer
+};
+
+// Fused x pass: per physical row (z, y): 3 inverse c2r pairs -> 6 physical fields -> 8 products
+// -> 4 forward r2c pairs -> 8 half-spectrum rows, written back over the same row slots.
+// Products: Dxz = (bx^2-ux^2)-(bz^2-uz^2), Dyz = (by^2-uy^2)-(bz^2-uz^2), Txy, Txz, Tyz with
+// Tij = bi*bj - ui*uj, and Axy, Axz, Ayz with Aij = ui*bj - bi*uj.
+template <class P, int ROWS>
+__global__ void __launch_bounds__(ROWS * P::G) x_fused_kernel(float2* buf, Geom geo, long long rowstride,
+                                                                long long slot, const float2* __restrict__ tw) {
+  using PR = typename Reverse<P>::type;
+  constexpr int G = P::G, V = P::V, N = P::N;
+  constexpr int TS = RowCfg<P>::TS;
+  extern __shared__ float2 smem[];
+  const int r = threadIdx.x / G, g = threadIdx.x % G;
+  const long long row = (long long)blockIdx.x * ROWS + r;
+  float2* rowp = buf + row * rowstride;
+  float2* sb = smem + r * 4 * TS;
+  const int kx = geo.kx;
+  auto sync = BlockSync{};
+
+  float2 v[3][V];
+#pragma unroll
+  for (int t = 0; t < 3; ++t) load_herm_pair<P>(v[t], rowp + (2 * t) * slot, rowp + (2 * t + 1) * slot, kx, g);
+  fft_run<P, +1, 3, TS, 1>(v, sb, 0, g, tw, sync);
+
+  float2 w[4][V];
+#pragma unroll
+  for (int i = 0; i < V; ++i) {
+    const float ux = v[0][i].x, uy = v[0][i].y, uz = v[1][i].x;
+    const float bx = v[1][i].y, by = v[2][i].x, bz = v[2][i].y;
+    const float tzz = bz * bz - uz * uz;
+    const float dxz = (bx * bx - ux * ux) - tzz;
+    const float dyz = (by * by - uy * uy) - tzz;
+    const float txy = bx * by - ux * uy;
+    const float txz = bx * bz - ux * uz;
+    const float tyz = by * bz - uy * uz;
+    const float axy = ux * by - bx * uy;
+    const float axz = ux * bz - bx * uz;
+    const float ayz = uy * bz - by * uz;
+    w[0][i] = make_float2(dxz, dyz);
+    w[1][i] = make_float2(txy, txz);
+    w[2][i] = make_float2(tyz, axy);
+    w[3][i] = make_float2(axz, ayz);
+  }
+  __syncthreads();
+  fft_run<PR, -1, 4, TS, 1>(w, sb, 0, g, tw, sync);
+  __syncthreads();
+#pragma unroll
+  for (int t = 0; t < 4; ++t)
+#pragma unroll
+    for (int d = 0; d < PR::DF; ++d)
+#pragma unroll
+      for (int e = 0; e < PR::RF; ++e) {
+        const int k = g + G * d + PR::LF * e;
+        if (k < kx || k > N - kx) sb[t * TS + k] = w[t][d * PR::RF + e];
+      }
+  __syncthreads();
+#pragma unroll
+  for (int t = 0; t < 4; ++t) store_split_pair(sb + t * TS, N, kx, g, G, rowp + (2 * t) * slot, rowp + (2 * t + 1) * slot);
+}
+
+// Plain c2r of row pairs: spectral rows (2q, 2q+1) -> physical rows, normalisation already applied.
+template <class P, int ROWS>
+__global__ void __launch_bounds__(ROWS * P::G) x_c2r_kernel(const float2* src, float* dst, Geom geo, long long srow,
+                                                              const float2* __restrict__ tw) {
+  constexpr int G = P::G, V = P::V, N = P::N;
+  constexpr int TS = RowCfg<P>::TS;
+  extern __shared__ float2 smem[];
+  const int r = threadIdx.x / G, g = threadIdx.x % G;
+  const long long q = (long long)blockIdx.x * ROWS + r;
+  float2 v[1][V];
+  load_herm_pair<P>(v[0], src + (2 * q) * srow, src + (2 * q + 1) * srow, geo.kx, g);
+  fft_run<P, +1, 1, TS, 1>(v, smem + r * TS, 0, g, tw, BlockSync{});
+  float* da = dst + (2 * q) * N;
+  float* db = dst + (2 * q + 1) * N;
+#pragma unroll
+  for (int d = 0; d < P::DF; ++d)
+#pragma unroll
+    for (int e = 0; e < P::RF; ++e) {
+      const int x = g + G * d + P::LF * e;
+      da[x] = v[0][d * P::RF + e].x;
+      db[x] = v[0][d * P::RF + e].y;
+    }
+}
+
+// Plain r2c of row pairs: physical rows (2q, 2q+1) -> half-spectrum rows (kx kept modes).
+template <class P, int ROWS>
+__global__ void __launch_bounds__(ROWS * P::G) x_r2c_kernel(const float* src, float2* dst, Geom geo, long long drow,
+                                                              const float2* __restrict__ tw) {
+  constexpr int G = P::G, V = P::V, N = P::N;
+  constexpr int TS = RowCfg<P>::TS;
+  extern __shared__ float2 smem[];
+  const int r = threadIdx.x / G, g = threadIdx.x % G;
+  const long long q = (long long)blockIdx.x * ROWS + r;
+  const float* sa = src + (2 * q) * N;
+  const float* sbp = src + (2 * q + 1) * N;
+  float2 v[1][V];
+#pragma unroll
+  for (int d = 0; d < P::DI; ++d)
+#pragma unroll
+    for (int n0 = 0; n0 < P::R0; ++n0) {
+      const int x = g + G * d + P::LI * n0;
+      v[0][d * P::R0 + n0] = make_float2(__ldg(sa + x), __ldg(sbp + x));
+    }
+  float2* sb = smem + r * TS;
+  fft_run<P, -1, 1, TS, 1>(v, sb, 0, g, tw, BlockSync{});
+  __syncthreads();
+#pragma unroll
+  for (int d = 0; d < P::DF; ++d)
+#pragma unroll
+    for (int e = 0; e < P::RF; ++e) {
+      const int k = g + G * d + P::LF * e;
+      if (k < geo.kx || k > N - geo.kx) sb[k] = v[0][d * P::RF + e];
+    }
+  __syncthreads();
+  store_split_pair(sb, N, geo.kx, g, G, dst + (2 * q) * drow, dst + (2 * q + 1) * drow);
+}
+
+// ------------------------------------------------------------------------------------------
+// z forward pass fused with the spectral right-hand side and the Runge-Kutta stage update.
+// ------------------------------------------------------------------------------------------
+enum StageOp : int {
+  OP_RHS = 0,       // out <- R
+  OP_RK4_FIRST = 1, // acc <- R/6 ; xn <- sol + h R            (X = sol)
+  OP_RK4_MID = 2,   // acc <- acc + R/3 ; xn <- sol + h R
+  OP_RK4_LAST = 3,  // sol <- sol + dt (acc + R/6)
+  OP_LS_FIRST = 4,  // du <- dt R ; u <- u + b du              (X = u)
+  OP_LS = 5,        // du <- a du + dt R ; u <- u + b du
+  OP_STORE = 6,     // out <- transformed product spectrum (plain forward transform)
+};
+
+struct EpiArgs {
+  const float2* prod;   // colbuf base
+  long long pO, pR, pS; // colbuf strides: ky' (outer), z (row), slot
+  int slot0;            // first product slot used by this kernel
+  // compact state arrays, already offset to the first field of this kernel's group
+  const float2* X;      // stage state (diffusion operand)
+  float2* sol;          // RK4: step-start state / LSRK4: unused
+  float2* acc;          // RK4 accumulator / LSRK4 du / OP_RHS,OP_STORE output
+  float2* xn;           // RK4 next stage state / LSRK4 u (updated in place)
+  long long fS, sKz, sKy;  // compact strides: field, kz', ky'
+  float visc;           // nu (momentum) or eta (induction)
+  float h;              // RK4 stage fraction * dt
+  float dt;
+  float ca, cb;         // LSRK4 coefficients
+  int op;
+};
+
+// NPROD = 5 (momentum: Dxz Dyz Txy Txz Tyz), 3 (induction: Axy Axz Ayz) or 1 (plain store).
+template <class P, int TX, int KIND>
+__global__ void __launch_bounds__(TX * P::G) z_epilogue_kernel(EpiArgs a, Geom geo, const float2* __restrict__ tw) {
+  constexpr int NPROD = KIND == 0 ? 5 : (KIND == 1 ? 3 : 1);
+  constexpr int G = P::G, V = P::V;
+  extern __shared__ float2 smem[];
+  float2* xb = smem;
+  float2* pb = smem + P::SMEM * TX;
+  const int tx = threadIdx.x % TX, g = threadIdx.x / TX;
+  const int kxg = blockIdx.x * TX + tx;
+  const bool colok = kxg < geo.kx;
+  const int ky = blockIdx.y;
+  const int K2 = geo.k2;
+  auto sync = BlockSync{};
+  for (int p = 0; p < NPROD; ++p) {
+    const float2* src = a.prod + (long long)ky * a.pO + (long long)(a.slot0 + p) * a.pS + kxg;
+    float2 v[1][V];
+#pragma unroll
+    for (int d = 0; d < P::DI; ++d)
+#pragma unroll
+      for (int n0 = 0; n0 < P::R0; ++n0) {
+        const int n = g + G * d + P::LI * n0;
+        v[0][d * P::R0 + n0] = colok ? __ldg(src + n * a.pR) : make_float2(0.f, 0.f);
+      }
+    fft_run<P, -1, 1, 0, TX>(v, xb, tx, g, tw, sync);
+#pragma unroll
+    for (int d = 0; d < P::DF; ++d)
+#pragma unroll
+      for (int e = 0; e < P::RF; ++e) {
+        const int k = g + G * d + P::LF * e;
+        const int j = kept_of_freq(geo, k);
+        if (j >= 0) pb[(p * K2 + j) * TX + tx] = v[0][d * P::RF + e];
+      }
+    __syncthreads();
+  }
+  if (!colok) return;
+  const float kxv = geo.kscale * (float)kxg;
+  const float kyv = geo.kscale * (float)signed_of_kept(geo, ky);
+  for (int j = g; j < K2; j += G) {
+    const long long idx = (long long)j * a.sKz + (long long)ky * a.sKy + kxg;
+    if (KIND == 2) {
+      a.acc[idx] = pb[j * TX + tx];
+      continue;
+    }
+    const float kzv = geo.kscale * (float)signed_of_kept(geo, j);
+    const float k2 = kxv * kxv + kyv * kyv + kzv * kzv;
+    float2 nl[3];
+    if (KIND == 0) {
+      const float2 dxz = pb[(0 * K2 + j) * TX + tx], dyz = pb[(1 * K2 + j) * TX + tx];
+      const float2 txy = pb[(2 * K2 + j) * TX + tx], txz = pb[(3 * K2 + j) * TX + tx];
+      const float2 tyz = pb[(4 * K2 + j) * TX + tx];
+      float2 Vx, Vy, Vz;
+      Vx.x = kxv * dxz.x + kyv * txy.x + kzv * txz.x;  Vx.y = kxv * dxz.y + kyv * txy.y + kzv * txz.y;
+      Vy.x = kxv * txy.x + kyv * dyz.x + kzv * tyz.x;  Vy.y = kxv * txy.y + kyv * dyz.y + kzv * tyz.y;
+      Vz.x = kxv * txz.x + kyv * tyz.x;                Vz.y = kxv * txz.y + kyv * tyz.y;
+      const float ik2 = k2 > 0.f ? 1.0f / k2 : 0.f;
+      float2 kv;
+      kv.x = (kxv * Vx.x + kyv * Vy.x + kzv * Vz.x) * ik2;
+      kv.y = (kxv * Vx.y + kyv * Vy.y + kzv * Vz.y) * ik2;
+      // i * (V - k (k.V)/k^2)
+      const float2 px = make_float2(Vx.x - kxv * kv.x, Vx.y - kxv * kv.y);
+      const float2 py = make_float2(Vy.x - kyv * kv.x, Vy.y - kyv * kv.y);
+      const float2 pz = make_float2(Vz.x - kzv * kv.x, Vz.y - kzv * kv.y);
+      nl[0] = make_float2(-px.y, px.x);
+      nl[1] = make_float2(-py.y, py.x);
+      nl[2] = make_float2(-pz.y, pz.x);
+    } else {
+      const float2 axy = pb[(0 * K2 + j) * TX + tx], axz = pb[(1 * K2 + j) * TX + tx];
+      const float2 ayz = pb[(2 * K2 + j) * TX + tx];
+      // Wx = i(ky Axy + kz Axz), Wy = i(-kx Axy + kz Ayz), Wz = -i(kx Axz + ky Ayz)
+      const float2 wx = make_float2(kyv * axy.x + kzv * axz.x, kyv * axy.y + kzv * axz.y);
+      const float2 wy = make_float2(-kxv * axy.x + kzv * ayz.x, -kxv * axy.y + kzv * ayz.y);
+      const float2 wz = make_float2(-kxv * axz.x - kyv * ayz.x, -kxv * axz.y - kyv * ayz.y);
+      nl[0] = make_float2(-wx.y, wx.x);
+      nl[1] = make_float2(-wy.y, wy.x);
+      nl[2] = make_float2(-wz.y, wz.x);
+    }
+    const float dk = -a.visc * k2;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      const long long o = idx + c * a.fS;
+      const float2 x = a.X[o];
+      const float2 R = make_float2(nl[c].x + dk * x.x, nl[c].y + dk * x.y);
+      switch (a.op) {
+        case OP_RHS: a.acc[o] = R; break;
+        case OP_RK4_FIRST: {
+          a.acc[o] = make_float2(R.x / 6.f, R.y / 6.f);
+          a.xn[o] = make_float2(x.x + a.h * R.x, x.y + a.h * R.y);
+        } break;
+        case OP_RK4_MID: {
+          const float2 s = a.sol[o], q = a.acc[o];
+          a.acc[o] = make_float2(q.x + R.x / 3.f, q.y + R.y / 3.f);
+          a.xn[o] = make_float2(s.x + a.h * R.x, s.y + a.h * R.y);
+        } break;
+        case OP_RK4_LAST: {
+          const float2 s = a.sol[o], q = a.acc[o];
+          const float2 tot = make_float2(q.x + R.x / 6.f, q.y + R.y / 6.f);
+          a.sol[o] = make_float2(s.x + a.dt * tot.x, s.y + a.dt * tot.y);
+        } break;
+        case OP_LS_FIRST: {
+          const float2 du = make_float2(a.dt * R.x, a.dt * R.y);
+          a.acc[o] = du;
+          a.xn[o] = make_float2(x.x + a.cb * du.x, x.y + a.cb * du.y);
+        } break;
+        case OP_LS: {
+          const float2 q = a.acc[o];
+          const float2 du = make_float2(a.ca * q.x + a.dt * R.x, a.ca * q.y + a.dt * R.y);
+          a.acc[o] = du;
+          a.xn[o] = make_float2(x.x + a.cb * du.x, x.y + a.cb * du.y);
+        } break;
+        default: break;
+      }
+    }
+  }
+}
+
+// ------------------------------------------------------------------------------------------
+// Layout conversion between the reference's column-major sol[kx, ky, kz, f] (half spectrum,
+// nkr = n/2+1) and the compact retained-band state.
+// ------------------------------------------------------------------------------------------
+__global__ void gather_state_kernel(const float2* __restrict__ ref, float2* __restrict__ S, Geom geo, int nf) {
+  const long long total = (long long)nf * geo.k2 * geo.k2 * geo.kxp;
+  const int nkr = geo.n / 2 + 1;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total; i += (long long)gridDim.x * blockDim.x) {
+    const int x = (int)(i % geo.kxp);
+    long long r = i / geo.kxp;
+    const int jy = (int)(r % geo.k2); r /= geo.k2;
+    const int jz = (int)(r % geo.k2);
+    const int f = (int)(r / geo.k2);
+    float2 val = make_float2(0.f, 0.f);
+    if (x < geo.kx) {
+      const int fy = freq_of_kept(geo, jy), fz = freq_of_kept(geo, jz);
+      val = ref[(((long long)f * geo.n + fz) * geo.n + fy) * nkr + x];
+    }
+    S[i] = val;
+  }
+}
+
+__global__ void scatter_state_kernel(const float2* __restrict__ S, float2* __restrict__ ref, Geom geo, int nf) {
+  const int nkr = geo.n / 2 + 1;
+  const long long total = (long long)nf * geo.n * geo.n * nkr;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total; i += (long long)gridDim.x * blockDim.x) {
+    const int x = (int)(i % nkr);
+    long long r = i / nkr;
+    const int fy = (int)(r % geo.n); r /= geo.n;
+    const int fz = (int)(r % geo.n);
+    const int f = (int)(r / geo.n);
+    float2 val = make_float2(0.f, 0.f);
+    const int jy = kept_of_freq(geo, fy), jz = kept_of_freq(geo, fz);
+    if (x < geo.kx && jy >= 0 && jz >= 0) val = S[(((long long)f * geo.k2 + jz) * geo.k2 + jy) * geo.kxp + x];
+    ref[i] = val;
+  }
+}
+
+// ------------------------------------------------------------------------------------------
+// Diagnostics.
+// ------------------------------------------------------------------------------------------
+// Per-block partial sums over the compact state (double accumulation, fixed order):
+//   [0] sum w|u|^2  [1] sum w|b|^2  [2] sum w Re(u.conj b)  [3] max|k.u|  [4] max|k.b|  [5] non-finite count
+// w = 1 on the kx = 0 plane and 2 elsewhere (the half spectrum stands for both +-kx).
+constexpr int kDiagSlots = 6;
+constexpr int kDiagThreads = 256;
+
+__device__ __forceinline__ void block_reduce_diag(double (&acc)[kDiagSlots], double* out) {
+  __shared__ double red[kDiagThreads / 32][kDiagSlots];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+  for (int s = 0; s < kDiagSlots; ++s) {
+    double x = acc[s];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const double y = __shfl_down_sync(0xffffffffu, x, o);
+      x = (s == 3 || s == 4) ? fmax(x, y) : x + y;
+    }
+    if (lane == 0) red[wid][s] = x;
+  }
+  __syncthreads();
+  if (threadIdx.x < kDiagSlots) {
+    const int s = threadIdx.x;
+    double x = red[0][s];
+    for (int w = 1; w < kDiagThreads / 32; ++w) x = (s == 3 || s == 4) ? fmax(x, red[w][s]) : x + red[w][s];
+    out[s] = x;
+  }
+}
+
+__global__ void __launch_bounds__(kDiagThreads) diag_partial_kernel(const float2* __restrict__ S, Geom geo, double* partial) {
+  const long long plane = (long long)geo.k2 * geo.k2 * geo.kxp;  // one field
+  double acc[kDiagSlots] = {0, 0, 0, 0, 0, 0};
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < plane; i += (long long)gridDim.x * blockDim.x) {
+    const int x = (int)(i % geo.kxp);
+    if (x >= geo.kx) continue;
+    long long r = i / geo.kxp;
+    const int jy = (int)(r % geo.k2);
+    const int jz = (int)(r / geo.k2);
+    const double w = x == 0 ? 1.0 : 2.0;
+    const double kx = (double)geo.kscale * x;
+    const double ky = (double)geo.kscale * signed_of_kept(geo, jy);
+    const double kz = (double)geo.kscale * signed_of_kept(geo, jz);
+    double2 ku = make_double2(0, 0), kb = make_double2(0, 0);
+    double eu = 0, eb = 0, hc = 0;
+    bool bad = false;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      const float2 u = S[c * plane + i], b = S[(c + 3) * plane + i];
+      bad |= !isfinite(u.x) || !isfinite(u.y) || !isfinite(b.x) || !isfinite(b.y);
+      eu += (double)u.x * u.x + (double)u.y * u.y;
+      eb += (double)b.x * b.x + (double)b.y * b.y;
+      hc += (double)u.x * b.x + (double)u.y * b.y;
+      const double kc = c == 0 ? kx : (c == 1 ? ky : kz);
+      ku.x += kc * u.x; ku.y += kc * u.y;
+      kb.x += kc * b.x; kb.y += kc * b.y;
+    }
+    acc[0] += w * eu;
+    acc[1] += w * eb;
+    acc[2] += w * hc;
+    acc[3] = fmax(acc[3], sqrt(ku.x * ku.x + ku.y * ku.y));
+    acc[4] = fmax(acc[4], sqrt(kb.x * kb.x + kb.y * kb.y));
+    acc[5] += bad ? 1.0 : 0.0;
+  }
+  block_reduce_diag(acc, partial + (long long)blockIdx.x * kDiagSlots);
+}
+
+// Second pass: reduce the block partials in block order (deterministic).
+__global__ void __launch_bounds__(kDiagThreads) diag_final_kernel(const double* __restrict__ partial, int nblocks, double* out) {
+  double acc[kDiagSlots] = {0, 0, 0, 0, 0, 0};
+  for (int b = threadIdx.x; b < nblocks; b += blockDim.x) {
+#pragma unroll
+    for (int s = 0; s < kDiagSlots; ++s) {
+      const double x = partial[b * kDiagSlots + s];
+      acc[s] = (s == 3 || s == 4) ? fmax(acc[s], x) : acc[s] + x;
+    }
+  }
+  block_reduce_diag(acc, out);
+}
+
+// i k.B into a one-field compact buffer (input of the div B inverse transform).
+__global__ void divb_spectrum_kernel(const float2* __restrict__ S, float2* __restrict__ out, Geom geo) {
+  const long long plane = (long long)geo.k2 * geo.k2 * geo.kxp;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < plane; i += (long long)gridDim.x * blockDim.x) {
+    const int x = (int)(i % geo.kxp);
+    long long r = i / geo.kxp;
+    const int jy = (int)(r % geo.k2);
+    const int jz = (int)(r / geo.k2);
+    const float kx = geo.kscale * x, ky = geo.kscale * signed_of_kept(geo, jy), kz = geo.kscale * signed_of_kept(geo, jz);
+    const float2 bx = S[3 * plane + i], by = S[4 * plane + i], bz = S[5 * plane + i];
+    const float re = kx * bx.x + ky * by.x + kz * bz.x;
+    const float im = kx * bx.y + ky * by.y + kz * bz.y;
+    out[i] = x < geo.kx ? make_float2(-im, re) : make_float2(0.f, 0.f);
+  }
+}
+
+// max |x| over a float array via the ordered bit pattern of non-negative floats (NaN wins).
+__global__ void maxabs_kernel(const float* __restrict__ a, long long n, unsigned int* out) {
+  unsigned int m = 0;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const unsigned int b = __float_as_uint(fabsf(a[i]));
+    m = b > m ? b : m;
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const unsigned int y = __shfl_down_sync(0xffffffffu, m, o);
+    m = y > m ? y : m;
+  }
+  if ((threadIdx.x & 31) == 0) atomicMax(out, m);
+}
+
+}  // namespace mhdgb

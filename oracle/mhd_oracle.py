@@ -1,0 +1,446 @@
+"""CPU oracle for the 3D incompressible MHD right-hand side and RK4 / LSRK4 step.
+
+TEST INFRASTRUCTURE ONLY.  Nothing in the product imports this module: only the
+tests, ``__graft_entry__.smoke()`` and the CPU-baseline / reference legs of
+``bench.py`` use it, and only as the checker or as the timed CPU restatement.
+
+Parity status: UNPINNED against the reference.  MHDFlows.jl ships no tests, no
+golden vectors and no fixtures, and Julia + FourierFlows cannot run here, so
+this restatement is pinned only by known-answer tests derived from the
+mathematics (exact decaying Beltrami flows, the exact Alfven wave, energy
+identities, symmetries) and by its own FP64 / FP32 agreement.
+
+What it restates (file:line into MHDFlows.jl):
+
+* ``calcN_literal``: ``MHDcalcN!`` (src/pgen.jl:153-162) = ``dealias!`` of the
+  state in place, then ``MHDcalcN_advection!`` (src/Solver/MHDSolver.jl:330-351):
+  six normalised inverse rffts of the state into ``vars``, ``UiUpdate!`` x3
+  (src/Solver/MHDSolver.jl:27-103; the i<=j product loop at :63-83, diffusion at
+  :90-99) and ``BiUpdate!`` x3 (src/Solver/MHDSolver.jl:106-177; the j!=a loop at
+  :147-158, resistivity at :165-173).  Same term order, same products, same
+  number of forward transforms (30 r2c + 6 c2r per RHS).
+* ``rk4_step``: FourierFlows' RK4 as restated in-repo at src/DyeModule.jl:62-89
+  (stage 1 evaluates the RHS on ``sol`` itself, so ``sol`` is dealiased in place
+  once per step; update ``sol += dt*(R1/6 + R2/3 + R3/3 + R4/6)``).
+* ``lsrk4_step``: FourierFlows' "LSRK4" = Carpenter & Kennedy (1994, NASA
+  TM-109112) five-stage fourth-order 2N-storage scheme, ``dU = A_i dU + dt R(U);
+  U += B_i dU``, RHS evaluated on ``sol`` itself (dealiased in place every stage).
+  FourierFlows itself is not vendored; the coefficients are the published ones.
+* ``Grid``: FourierFlows ``ThreeDGrid`` conventions mirrored in-repo at
+  src/utils/utils.jl:14-38,42-98 (``kr = rfftfreq``, ``l, m = fftfreq`` scaled by
+  2*pi/L*n, ``invKrsq[0,0,0] = 0``, centred ``x = -L/2 + i*dx``) and the alias
+  ranges of ``getaliasedwavenumbers`` (``iL = floor((1-a)/2*n)+1``,
+  ``iR = ceil((1+a)/2*n)``, 1-based, rfft axis ``iL:nkr``; recollection of
+  FourierFlows 0.10.1, unverified, same double arithmetic as Julia).
+* ``prob_diagnostic``: ``ProbDiagnostic`` (src/utils/UserInterface.jl:29,65-86),
+  KE = ME = sum(|.|^2)*dV with no 1/2, and ``Div`` (src/utils/VectorCalculus.jl:72-94).
+
+Array layout: numpy C order ``(nz, ny, nx)`` for physical fields and
+``(nz, ny, nkr)`` for half spectra, which is the same memory as Julia's
+column-major ``(nx, ny, nz)`` / ``(nkr, ny, nz)``.  A state is ``(6, nz, ny, nkr)``
+== Julia ``sol[i, j, k, f]`` with f = ux, uy, uz, bx, by, bz.
+"""
+from __future__ import annotations
+
+import math
+import os
+
+import numpy as np
+import scipy.fft as sfft
+
+FIELDS = ("ux", "uy", "uz", "bx", "by", "bz")
+
+# Carpenter & Kennedy (1994) LSRK(5,4) 2N-storage coefficients.
+LSRK4_A = (0.0,
+           -567301805773.0 / 1357537059087.0,
+           -2404267990393.0 / 2016746695238.0,
+           -3550918686646.0 / 2091501179385.0,
+           -1275806237668.0 / 842570457699.0)
+LSRK4_B = (1432997174477.0 / 9575080441755.0,
+           5161836677717.0 / 13612068292357.0,
+           1720146321549.0 / 2090206949498.0,
+           3134564353537.0 / 4481467310338.0,
+           2277821191437.0 / 14882151754819.0)
+LSRK4_C = (0.0,
+           1432997174477.0 / 9575080441755.0,
+           2526269341429.0 / 6820363962896.0,
+           2006345519317.0 / 3224310063776.0,
+           2802321613138.0 / 2924317926251.0)
+
+
+def _workers() -> int:
+    return int(os.environ.get("MHD_ORACLE_WORKERS", os.cpu_count() or 1))
+
+
+def alias_ranges(n: int, aliased_fraction: float = 1.0 / 3.0):
+    """0-based half-open alias ranges (full axis, rfft axis) for length n.
+
+    Mirrors getaliasedwavenumbers (FourierFlows 0.10.1; used by dealias! at
+    src/pgen.jl:155 and rebuilt in-repo at src/utils/utils.jl:82-84).
+    """
+    lo = (1 - aliased_fraction) / 2
+    hi = (1 + aliased_fraction) / 2
+    i_l = math.floor(lo * n) + 1          # 1-based first aliased index
+    i_r = math.ceil(hi * n)               # 1-based last aliased index
+    if not aliased_fraction < 1:
+        i_l += 1
+    nkr = n // 2 + 1
+    return (i_l - 1, i_r), (i_l - 1, nkr)
+
+
+def kept_counts(n: int):
+    """(Kx, Kpos, Kneg): kept rfft-axis modes, kept non-negative / negative full-axis modes."""
+    (a0, a1), (r0, _) = alias_ranges(n)
+    return r0, a0, n - a1
+
+
+class Grid:
+    """Periodic cube of side L with n points per axis (FourierFlows ThreeDGrid conventions)."""
+
+    def __init__(self, n: int, L: float = 2 * math.pi, dtype=np.float64, centred: bool = True):
+        self.n = n
+        self.L = L
+        self.nkr = n // 2 + 1
+        self.dtype = np.dtype(dtype)
+        self.cdtype = np.result_type(self.dtype, np.complex64)
+        self.dx = L / n
+        x0 = -L / 2 if centred else 0.0
+        self.x = (x0 + self.dx * np.arange(n)).astype(dtype)
+        # rfftfreq(n, 2pi/L*n) and fftfreq(n, 2pi/L*n), computed in float64 then cast (utils.jl:23-26)
+        kr = np.arange(self.nkr, dtype=np.float64) * (2 * math.pi / L)
+        kf = np.fft.fftfreq(n, 1.0 / n) * (2 * math.pi / L)
+        self.kr = kr.astype(dtype).reshape(1, 1, self.nkr)
+        self.l = kf.astype(dtype).reshape(1, n, 1)
+        self.m = kf.astype(dtype).reshape(n, 1, 1)
+        self.Krsq = self.kr ** 2 + self.l ** 2 + self.m ** 2
+        with np.errstate(divide="ignore"):
+            self.invKrsq = (1 / self.Krsq).astype(dtype)
+        self.invKrsq[0, 0, 0] = 0
+        (self.a0, self.a1), (self.r0, _) = alias_ranges(n)
+        self.ks = (self.kr, self.l, self.m)
+
+    # --- transforms (FourierFlows rfftplan: mul! unnormalised r2c, ldiv! normalised c2r)
+    def rfft(self, a):
+        return sfft.rfftn(a, axes=(0, 1, 2), workers=_workers())
+
+    def irfft(self, ah):
+        return sfft.irfftn(ah, s=(self.n,) * 3, axes=(0, 1, 2), workers=_workers())
+
+    def dealias(self, fh):
+        """In-place per-axis cube truncation of ``fh`` (..., nz, ny, nkr)."""
+        fh[..., :, :, self.r0:] = 0
+        fh[..., :, self.a0:self.a1, :] = 0
+        fh[..., self.a0:self.a1, :, :] = 0
+        return fh
+
+    def retained_mask(self):
+        m = np.ones((self.n, self.n, self.nkr), dtype=bool)
+        self.dealias(m)
+        return m
+
+    def mesh(self):
+        z, y, x = np.meshgrid(self.x, self.x, self.x, indexing="ij")
+        return x, y, z
+
+
+def _delta(a, b):
+    return 1 if a == b else 0
+
+
+def calcN_literal(N, sol, grid: Grid, nu, eta, nnu=0, neta=0, vars_out=None):
+    """Literal restatement of MHDcalcN! (src/pgen.jl:153-162); dealiases ``sol`` in place."""
+    g = grid
+    g.dealias(sol)
+    # MHDcalcN_advection! (src/Solver/MHDSolver.jl:333-338): vars <- ldiv!(rfftplan, copy(sol[f]))
+    v = [g.irfft(sol[f].copy()).astype(g.dtype) for f in range(6)]
+    if vars_out is not None:
+        for f in range(6):
+            vars_out[f][...] = v[f]
+    u = v[0:3]
+    b = v[3:6]
+    ks = g.ks
+    nu_s = np.float64(nu)
+    eta_s = np.float64(eta)
+    # UiUpdate! (src/Solver/MHDSolver.jl:27-103)
+    for a in range(3):
+        ka = ks[a]
+        out = N[a]
+        out[...] = 0
+        for i in range(3):
+            for j in range(3):
+                if j >= i:
+                    nl = b[i] * b[j] - u[i] * u[j]
+                    nlh = g.rfft(nl)
+                    out += 1j * ks[i] * (_delta(a, j) - ka * ks[j] * g.invKrsq) * nlh
+                    if i != j:
+                        out += 1j * ks[j] * (_delta(a, i) - ka * ks[i] * g.invKrsq) * nlh
+        uh = g.rfft(u[a])
+        out += (-g.Krsq * nu_s * uh).astype(out.dtype)
+        if nnu > 1:
+            out += (-g.Krsq ** nnu * nu_s * uh).astype(out.dtype)
+    # BiUpdate! (src/Solver/MHDSolver.jl:106-177)
+    for a in range(3):
+        out = N[3 + a]
+        out[...] = 0
+        for j in range(3):
+            if a != j:
+                nl = u[a] * b[j] - b[a] * u[j]
+                nlh = g.rfft(nl)
+                out += 1j * ks[j] * nlh
+        bh = g.rfft(b[a])
+        out += (-g.Krsq * eta_s * bh).astype(out.dtype)
+        if neta > 1:
+            out += (-g.Krsq ** neta * eta_s * bh).astype(out.dtype)
+    return N
+
+
+def calcN_fast(N, sol, grid: Grid, nu, eta):
+    """Same RHS as ``calcN_literal`` with the six unique stress products transformed once.
+
+    Used for larger FP64 checks; mathematically identical to the literal form.
+    """
+    g = grid
+    g.dealias(sol)
+    v = [g.irfft(sol[f]) for f in range(6)]
+    u, b = v[0:3], v[3:6]
+    ks = g.ks
+    T = {}
+    for i in range(3):
+        for j in range(i, 3):
+            T[(i, j)] = g.rfft(b[i] * b[j] - u[i] * u[j])
+            T[(j, i)] = T[(i, j)]
+    V = [sum(ks[i] * T[(i, j)] for i in range(3)) for j in range(3)]
+    kV = sum(ks[j] * V[j] for j in range(3)) * g.invKrsq
+    for a in range(3):
+        N[a] = 1j * (V[a] - ks[a] * kV) - g.Krsq * nu * sol[a]
+    E = {}
+    for a in range(3):
+        for j in range(a + 1, 3):
+            E[(a, j)] = g.rfft(u[a] * b[j] - b[a] * u[j])
+            E[(j, a)] = -E[(a, j)]
+    for a in range(3):
+        acc = 0
+        for j in range(3):
+            if j != a:
+                acc = acc + ks[j] * E[(a, j)]
+        N[3 + a] = 1j * acc - g.Krsq * eta * sol[3 + a]
+    return N
+
+
+class Stepper:
+    """RK4 / LSRK4 on the full half-spectrum state, as FourierFlows does it."""
+
+    def __init__(self, grid: Grid, nu, eta, dt, scheme="RK4", literal=True, nnu=0, neta=0):
+        self.g = grid
+        self.nu, self.eta, self.dt = nu, eta, dt
+        self.nnu, self.neta = nnu, neta
+        self.scheme = scheme.upper()
+        self.literal = literal
+        self.t = 0.0
+        self.step = 0
+        shape = (6, grid.n, grid.n, grid.nkr)
+        z = lambda: np.zeros(shape, dtype=grid.cdtype)
+        if self.scheme == "RK4":
+            self.R = [z() for _ in range(4)]
+            self.sol1 = z()
+        elif self.scheme == "LSRK4":
+            self.S2 = z()
+            self.RHS = z()
+        else:
+            raise ValueError(f"unknown stepper {scheme!r}")
+        self.vars = [np.zeros((grid.n,) * 3, dtype=grid.dtype) for _ in range(6)]
+
+    def calcN(self, N, X):
+        if self.literal:
+            return calcN_literal(N, X, self.g, self.nu, self.eta, self.nnu, self.neta, self.vars)
+        return calcN_fast(N, X, self.g, self.nu, self.eta)
+
+    def stepforward(self, sol):
+        dt = self.dt
+        if self.scheme == "RK4":
+            R1, R2, R3, R4 = self.R
+            s1 = self.sol1
+            self.calcN(R1, sol)
+            np.add(sol, (dt / 2) * R1, out=s1)
+            self.calcN(R2, s1)
+            np.add(sol, (dt / 2) * R2, out=s1)
+            self.calcN(R3, s1)
+            np.add(sol, dt * R3, out=s1)
+            self.calcN(R4, s1)
+            sol += dt * (R1 / 6 + R2 / 3 + R3 / 3 + R4 / 6)
+        else:
+            S2, R = self.S2, self.RHS
+            for i in range(5):
+                self.calcN(R, sol)
+                if i == 0:
+                    S2[...] = dt * R
+                else:
+                    S2[...] = LSRK4_A[i] * S2 + dt * R
+                sol += LSRK4_B[i] * S2
+        self.t += dt
+        self.step += 1
+        return sol
+
+
+# ----------------------------------------------------------------------------------------------
+# Initial conditions
+# ----------------------------------------------------------------------------------------------
+
+def taylor_green(grid: Grid, b_amp=0.5):
+    """Taylor-Green u and B on the grid points (centred by default, as the reference's grid)."""
+    x, y, z = grid.mesh()
+    ux = np.sin(x) * np.cos(y) * np.cos(z)
+    uy = -np.cos(x) * np.sin(y) * np.cos(z)
+    uz = np.zeros_like(x)
+    bx = b_amp * np.cos(x) * np.sin(y) * np.sin(z)
+    by = -b_amp * np.sin(x) * np.cos(y) * np.sin(z)
+    bz = np.zeros_like(x)
+    return [a.astype(grid.dtype) for a in (ux, uy, uz, bx, by, bz)]
+
+
+def physical_to_state(grid: Grid, fields):
+    """SetUpProblemIC! (src/utils/IC.jl:41-109): forward r2c of each physical field into ``sol``."""
+    sol = np.zeros((6, grid.n, grid.n, grid.nkr), dtype=grid.cdtype)
+    for f in range(6):
+        sol[f] = grid.rfft(np.asarray(fields[f], dtype=grid.dtype))
+    return sol
+
+
+def _splitmix64(x):
+    x = (x + np.uint64(0x9E3779B97F4A7C15)) & np.uint64(0xFFFFFFFFFFFFFFFF)
+    z = x
+    z = ((z ^ (z >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)) & np.uint64(0xFFFFFFFFFFFFFFFF)
+    z = ((z ^ (z >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)) & np.uint64(0xFFFFFFFFFFFFFFFF)
+    return z ^ (z >> np.uint64(31))
+
+
+def mode_phases(seed: int, field: int, kx, ky, kz):
+    """Uniform [0, 2pi) phase per (seed, field, integer wavevector), independent of n.
+
+    Counter-based (splitmix64 of a packed key) so the same mode gets the same phase on
+    every grid size: a 512^3 and a 128^3 spectrum share their common modes exactly.
+    """
+    kx = np.asarray(kx, dtype=np.int64) & 0xFFFF
+    ky = np.asarray(ky, dtype=np.int64) & 0xFFFF
+    kz = np.asarray(kz, dtype=np.int64) & 0xFFFF
+    key = (kx.astype(np.uint64) | (ky.astype(np.uint64) << np.uint64(16))
+           | (kz.astype(np.uint64) << np.uint64(32)) | (np.uint64(field & 0xFF) << np.uint64(48)))
+    with np.errstate(over="ignore"):
+        h = _splitmix64(key ^ _splitmix64(np.uint64(seed & 0xFFFFFFFFFFFFFFFF)))
+        h = _splitmix64(h)
+    return (h >> np.uint64(11)).astype(np.float64) * (2.0 ** -53) * (2 * math.pi)
+
+
+def random_spectrum_state(grid: Grid, seed: int, e_u: float = 0.5, b_ratio: float = 0.3,
+                          kpeak: float = 4.0):
+    """Seeded random-phase solenoidal u, B with shell spectrum E(k) ~ k^4 exp(-2 (k/kpeak)^2).
+
+    Every retained mode of the rfft half space gets amplitude sqrt(E(|k|)/(4 pi |k|^2)) and a
+    mode-indexed random phase per field component; the kx = 0 plane is made Hermitian (modes
+    whose partner lies in the alias band are zeroed), each triple is projected solenoidal
+    (F - k (k.F)/k^2), u is normalised to E_u = <|u|^2>/2 = e_u and B to b_ratio times u's rms.
+    Built in float64 and returned in the grid's complex dtype.
+    """
+    g = Grid(grid.n, grid.L, np.float64)
+    n = g.n
+    kf = np.fft.fftfreq(n, 1.0 / n).astype(np.int64)
+    KZ, KY, KX = np.meshgrid(kf, kf, np.arange(g.nkr), indexing="ij")
+    kx = KX * (2 * math.pi / g.L)
+    ky = KY * (2 * math.pi / g.L)
+    kz = KZ * (2 * math.pi / g.L)
+    k2 = kx ** 2 + ky ** 2 + kz ** 2
+    k = np.sqrt(k2)
+    with np.errstate(divide="ignore", invalid="ignore"):
+        amp = np.sqrt(k ** 4 * np.exp(-2 * (k / kpeak) ** 2) / (4 * math.pi * k2))
+    amp[0, 0, 0] = 0.0
+    keep = g.retained_mask()
+    amp = np.where(keep, amp, 0.0)
+    sol = np.zeros((6, n, n, g.nkr), dtype=np.complex128)
+    for f in range(6):
+        ph = mode_phases(seed, f, KX, KY, KZ)
+        sol[f] = amp * np.exp(1j * ph)
+    # Hermitian kx = 0 plane: F(0,-ky,-kz) = conj(F(0,ky,kz)); partner outside the band -> 0
+    for f in range(6):
+        p = sol[f, :, :, 0]
+        iz = (-np.arange(n)) % n
+        partner = np.conj(p[np.ix_(iz, iz)])
+        herm = 0.5 * (p + partner)
+        km = keep[:, :, 0] & keep[:, :, 0][np.ix_(iz, iz)]
+        sol[f, :, :, 0] = np.where(km, herm, 0.0)
+    # solenoidal projection
+    with np.errstate(invalid="ignore", divide="ignore"):
+        inv = np.where(k2 > 0, 1.0 / np.where(k2 > 0, k2, 1.0), 0.0)
+    kv = (kx, ky, kz)
+    for base in (0, 3):
+        dot = sum(kv[i] * sol[base + i] for i in range(3)) * inv
+        for i in range(3):
+            sol[base + i] -= kv[i] * dot
+    # normalisation via Parseval on the half spectrum (kx = 0 weight 1, else 2)
+    w = np.where(KX == 0, 1.0, 2.0)
+
+    def mean_sq(fs):
+        return float(sum(np.sum(w * np.abs(sol[f]) ** 2) for f in fs)) / float(n) ** 6
+
+    mu = mean_sq((0, 1, 2))
+    mb = mean_sq((3, 4, 5))
+    su = math.sqrt(2 * e_u / mu) if mu > 0 else 0.0
+    target_b = (b_ratio ** 2) * (2 * e_u)
+    sb = math.sqrt(target_b / mb) if mb > 0 else 0.0
+    sol[0:3] *= su
+    sol[3:6] *= sb
+    return sol.astype(grid.cdtype)
+
+
+# ----------------------------------------------------------------------------------------------
+# Diagnostics
+# ----------------------------------------------------------------------------------------------
+
+def prob_diagnostic(grid: Grid, vars6):
+    """ProbDiagnostic (src/utils/UserInterface.jl:65-86) without the 3-digit rounding: KE, ME."""
+    dV = grid.dx ** 3
+    ke = float(sum(np.sum(np.asarray(vars6[i], dtype=np.float64) ** 2) for i in range(3))) * dV
+    me = float(sum(np.sum(np.asarray(vars6[i], dtype=np.float64) ** 2) for i in range(3, 6))) * dV
+    if math.isnan(ke) or math.isnan(me):
+        raise FloatingPointError("detected NaN! Quit the simulation right now.")
+    return ke, me
+
+
+def spectral_diagnostics(grid: Grid, sol):
+    """Diagnostics of a (dealiased) state in float64.
+
+    Returns dict: E_u, E_B = sum(|u|^2) dV and sum(|B|^2) dV (the reference's KE / ME, no 1/2),
+    H_c = sum(u.B) dV, max|k.u_hat|, max|k.B_hat| (unnormalised spectra, like the state), and
+    max|div B| in physical space (Div, src/utils/VectorCalculus.jl:72-94).
+    """
+    g = Grid(grid.n, grid.L, np.float64)
+    s = np.asarray(sol, dtype=np.complex128).copy()
+    g.dealias(s)
+    n = g.n
+    w = np.ones((1, 1, g.nkr))
+    w[..., 1:] = 2.0
+    if n % 2 == 0:
+        w[..., -1] = 1.0
+    dV = g.dx ** 3
+    scale = dV / float(n) ** 3
+    e_u = float(sum(np.sum(w * np.abs(s[f]) ** 2) for f in range(3))) * scale
+    e_b = float(sum(np.sum(w * np.abs(s[f]) ** 2) for f in range(3, 6))) * scale
+    h_c = float(sum(np.sum(w * (s[f] * np.conj(s[f + 3])).real) for f in range(3))) * scale
+    ku = sum(g.ks[i] * s[i] for i in range(3))
+    kb = sum(g.ks[i] * s[3 + i] for i in range(3))
+    divb = g.irfft(1j * kb)
+    return {
+        "E_u": e_u, "E_B": e_b, "H_c": h_c,
+        "max_kdotu": float(np.max(np.abs(ku))), "max_kdotb": float(np.max(np.abs(kb))),
+        "max_divb": float(np.max(np.abs(divb))),
+        "nan": bool(not np.all(np.isfinite(s))),
+    }
+
+
+def rel_l2(a, b, mask=None):
+    a = np.asarray(a, dtype=np.complex128)
+    b = np.asarray(b, dtype=np.complex128)
+    if mask is not None:
+        a = a[..., mask]
+        b = b[..., mask]
+    den = np.linalg.norm(b)
+    return float(np.linalg.norm(a - b) / (den if den > 0 else 1.0))
