@@ -1,0 +1,381 @@
+"""Benchmark: MHD RK4 step, 256^3, FP32 (plain form), on N GPUs as independent replicas.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference] [--n 256]
+
+A step is one RK4 step (4 right-hand-side evaluations, 24 kernel launches) of the seeded random
+k^4 exp(-2(k/4)^2) problem with nu = eta = 1e-3, dt = 5e-4.  `value` is whole-job grid-point
+steps per second with the state resident in HBM; `e2e` is the same metric through the C ABI with
+host buffers (state uploaded from pinned host memory, stepped once and downloaded every step).
+The working set of a step (1.5 GB at 256^3) is larger than L2, so no flush is needed between steps.
+Multi-GPU runs are replicas (one independent problem per rank, no collectives on the data path);
+rank 0 prints one JSON line.  `--impl reference` times the CPU restatement of the reference path
+(oracle/, scipy FP32, all host cores) on the same workload instead.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "ms per RK4 MHD step at 256³/512³ & grid-pt·steps/s vs plain; p50/p99 latency"
+UNIT = "grid-pt·steps/s"
+NU = ETA = 1e-3
+DT = 5e-4
+SEED = 1
+# README.md:78 of the reference: MHD RK4 256^3 on an RTX 3080, 0.271 s per step
+PUBLISHED_256_S_PER_STEP = 0.271
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class Dist:
+    """Host-side control plane (gloo): barrier and max over ranks; no data-path collective."""
+
+    def __init__(self, world):
+        self.world = world
+        self.pg = None
+        if world > 1:
+            import torch.distributed as dist
+
+            os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+            dist.init_process_group("gloo")
+            self.dist = dist
+
+    def barrier(self):
+        if self.world > 1:
+            self.dist.barrier()
+
+    def max(self, x: float) -> float:
+        if self.world == 1:
+            return x
+        import torch
+
+        t = torch.tensor([x], dtype=torch.float64)
+        self.dist.all_reduce(t, op=self.dist.ReduceOp.MAX)
+        return float(t.item())
+
+    def sum(self, x: float) -> float:
+        if self.world == 1:
+            return x
+        import torch
+
+        t = torch.tensor([x], dtype=torch.float64)
+        self.dist.all_reduce(t, op=self.dist.ReduceOp.SUM)
+        return float(t.item())
+
+    def close(self):
+        if self.world > 1:
+            self.dist.destroy_process_group()
+
+
+class ClockMonitor:
+    """nvidia-smi clock / throttle sampling during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.idx = gpu_index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.idx}", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"], "samples": 0}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        rows = []
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 9 and parts[1].replace(".", "").isdigit():
+                rows.append(parts)
+        os.unlink(self.path)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        sm = [float(r[1]) for r in rows]
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            for name, val in zip(names, r[5:9]):
+                if val.lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": float(rows[0][2]), "reasons": sorted(reasons),
+                "samples": len(rows), "power_w_max": max(float(r[3]) for r in rows if r[3].replace(".", "").isdigit()) if rows else None}
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def ncu_traffic(cls_name: str, n: int):
+    """Per-launch DRAM bytes of a kernel class from a committed ncu summary, if any."""
+    path = os.path.join(ROOT, "profiles", f"{cls_name}_{n}.txt")
+    if not os.path.exists(path):
+        return None
+    for line in open(path):
+        if line.startswith("traffic_bytes_per_launch:"):
+            try:
+                return float(line.split(":", 1)[1].split()[0])
+            except ValueError:
+                return None
+    return None
+
+
+def initial_state(n: int):
+    from oracle import mhd_oracle as mo  # IC generator only (seeded input data)
+
+    g = mo.Grid(n)
+    return mo.random_spectrum_state(g, SEED).astype(np.complex64)
+
+
+def run_gpu(args, rank, world, local, dist: Dist):
+    import __graft_entry__ as ge
+
+    pkg = ge.load_package()
+    lib = pkg._lib.load()
+    n = args.n
+    s0 = initial_state(n)
+    prob = pkg.Problem(pkg.GPU(local), nx=n, Lx=2 * math.pi, nu=NU, eta=ETA, dt=DT, stepper="RK4")
+    h = prob.handle
+    chk = pkg._lib.check
+    prob.set_sol(s0.T)
+    stream = lib.mhd_get_stream(h)
+
+    # warm-up
+    pkg.stepforward(prob, args.warmup)
+    prob.synchronize()
+
+    nc = lib.mhd_kernel_class_count()
+    names = [lib.mhd_kernel_class_name(c).decode() for c in range(nc)]
+    mon = ClockMonitor(local)
+    dist.barrier()
+    prob.synchronize()
+    chk(lib.mhd_profile_enable(h, 1))
+    mon.start()
+    # timed region: K steps back to back on the library's stream; an event between consecutive
+    # steps gives per-step latency, events around every launch give per-kernel durations
+    arr = (C.c_double * args.steps)()
+    chk(lib.mhd_step_timed(h, args.steps, arr))
+    per_step = list(arr)
+    clocks = mon.stop()
+    L = (C.c_longlong * nc)()
+    T = (C.c_double * nc)()
+    chk(lib.mhd_profile_read(h, L, T, nc))
+    chk(lib.mhd_profile_enable(h, 0))
+    dist.barrier()
+    local_ms = sum(per_step)
+    max_ms = dist.max(local_ms)
+    total_pts = dist.sum(float(n) ** 3 * args.steps)
+    value = total_pts / (max_ms / 1e3)
+    ms_per_step = max_ms / args.steps
+    p50 = float(np.percentile(per_step, 50))
+    p99 = float(np.percentile(per_step, 99))
+    launches = int(sum(L[c] for c in range(nc)))
+
+    # dominant kernel roofline
+    shares = {names[c]: T[c] for c in range(nc) if L[c] > 0}
+    top = max(shares, key=shares.get)
+    ci = names.index(top)
+    b = C.c_double()
+    chk(lib.mhd_kernel_class_bytes(h, ci, C.byref(b)))
+    avg_s = T[ci] / L[ci] / 1e3
+    achieved = b.value / avg_s / 1e9
+    peak, peak_kind = measured_peaks()
+    kernels = {}
+    for c in range(nc):
+        if L[c] == 0:
+            continue
+        bb = C.c_double()
+        lib.mhd_kernel_class_bytes(h, c, C.byref(bb))
+        avg = T[c] / L[c] / 1e3
+        kernels[names[c]] = {"launches": int(L[c]), "avg_us": round(avg * 1e6, 2),
+                             "share": round(T[c] / sum(T), 4),
+                             "gbs": round(bb.value / avg / 1e9, 1) if bb.value else None}
+
+    # e2e through the C ABI with pinned host buffers: upload state, one step, download state
+    nbytes = s0.nbytes
+    pin_in = C.c_void_p()
+    pin_out = C.c_void_p()
+    chk(lib.mhd_host_alloc(nbytes, C.byref(pin_in)))
+    chk(lib.mhd_host_alloc(nbytes, C.byref(pin_out)))
+    C.memmove(pin_in, s0.ctypes.data, nbytes)
+    ke = max(3, min(args.steps, 30))
+    for _ in range(2):
+        chk(lib.mhd_set_state(h, pin_in)); chk(lib.mhd_step(h, 1)); chk(lib.mhd_get_state(h, pin_out))
+    dist.barrier()
+    t0 = time.perf_counter()
+    for _ in range(ke):
+        chk(lib.mhd_set_state(h, pin_in))
+        chk(lib.mhd_step(h, 1))
+        chk(lib.mhd_get_state(h, pin_out))
+    el = time.perf_counter() - t0
+    el_max = dist.max(el)
+    e2e_value = dist.sum(float(n) ** 3 * ke) / el_max
+    out_arr = np.frombuffer((C.c_char * nbytes).from_address(pin_out.value), dtype=np.complex64)
+    finite = bool(np.isfinite(out_arr).all())
+    chk(lib.mhd_host_free(pin_in))
+    chk(lib.mhd_host_free(pin_out))
+
+    # optional secondary size (512^3 ms per step)
+    secondary = None
+    if args.secondary and rank == 0:
+        n2 = 512
+        s2 = initial_state(n2)
+        p2 = pkg.Problem(pkg.GPU(local), nx=n2, Lx=2 * math.pi, nu=5e-4, eta=5e-4, dt=2.5e-4, stepper="RK4")
+        p2.set_sol(s2.T)
+        pkg.stepforward(p2, 3)
+        p2.synchronize()
+        ms2 = C.c_double()
+        chk(lib.mhd_time_steps(p2.handle, 10, C.byref(ms2)))
+        secondary = {"n": n2, "ms_per_step": round(ms2.value / 10, 3),
+                     "grid_pt_steps_per_s": n2 ** 3 / (ms2.value / 10 / 1e3)}
+        p2.close()
+    prob.close()
+    return {
+        "value": value, "ms_per_step": ms_per_step, "p50_ms": p50, "p99_ms": p99, "launches": launches,
+        "clocks": clocks, "top": top, "achieved": achieved, "bytes": b.value, "peak": peak, "peak_kind": peak_kind,
+        "kernels": kernels, "e2e": e2e_value, "e2e_bytes": nbytes, "e2e_steps": ke, "finite": finite,
+        "secondary": secondary,
+    }
+
+
+def cpu_baseline(n: int, stages: int = 1):
+    """CPU restatement of the reference path (oracle, scipy FP32 literal form), all host cores."""
+    from oracle import mhd_oracle as mo
+
+    g = mo.Grid(n, dtype=np.float32)
+    s = initial_state(n)
+    st = mo.Stepper(g, NU, ETA, DT, "RK4", literal=True)
+    N = np.zeros_like(s)
+    mo.calcN_literal(N, s.copy(), g, NU, ETA)  # warm FFT plans
+    t0 = time.perf_counter()
+    for _ in range(stages):
+        mo.calcN_literal(N, s, g, NU, ETA, vars_out=st.vars)
+        s1 = s + np.float32(DT / 2) * N
+    el = (time.perf_counter() - t0) / stages
+    return {"value": n ** 3 / (4 * el), "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
+            "sample": f"{stages} RK4 stage(s) (one RHS evaluation + stage update) at {n}^3, scaled x4 to an RK4 step; "
+                      f"scipy.fft float32 with workers={os.cpu_count()}"}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--n", type=int, default=256)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-secondary", dest="secondary", action="store_false")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    rank, world, local = dist_env()
+    config = {"workload": f"MHD RK4 step, {args.n}^3 FP32, nu=eta=1e-3, dt=5e-4, seeded k^4 exp(-2(k/4)^2) u and B",
+              "n": args.n, "scheme": "RK4", "l2": "inputs larger than L2 (step working set > 1 GB)",
+              "parallelism": "replicas" if args.gpus > 1 else "single"}
+
+    if args.impl == "reference":
+        if rank != 0:
+            return 0
+        os.environ.setdefault("MHD_ORACLE_WORKERS", str(os.cpu_count()))
+        from oracle import mhd_oracle as mo
+
+        n = args.n
+        g = mo.Grid(n, dtype=np.float32)
+        s = initial_state(n)
+        N = np.zeros_like(s)
+        for _ in range(args.warmup):
+            mo.calcN_literal(N, s.copy(), g, NU, ETA)
+        times = []
+        for _ in range(args.steps):
+            t0 = time.perf_counter()
+            mo.calcN_literal(N, s, g, NU, ETA)
+            s2 = s + np.float32(DT / 2) * N
+            times.append(time.perf_counter() - t0)
+        stage = sum(times) / len(times)
+        value = n ** 3 / (4 * stage)
+        line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": 4 * stage * 1e3, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+                "config": config,
+                "cpu_baseline": {"value": value, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
+                                 "sample": f"each step = one RK4 stage (RHS evaluation + stage update) at {n}^3, "
+                                           "scaled x4 to an RK4 step; oracle literal restatement, scipy.fft float32, "
+                                           f"workers={os.cpu_count()}"},
+                "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+                "p50_ms": 4e3 * float(np.percentile(times, 50)), "p99_ms": 4e3 * float(np.percentile(times, 99))}
+        print(json.dumps(line), flush=True)
+        return 0
+
+    dist = Dist(world)
+    r = run_gpu(args, rank, world, local, dist)
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(args.n)
+    if rank == 0:
+        pub = args.n ** 3 / PUBLISHED_256_S_PER_STEP if args.n == 256 else None
+        line = {
+            "metric": METRIC, "value": r["value"], "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": r["ms_per_step"], "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": (r["value"] / world / pub) if pub else None,
+            "dtype": "f32", "data": "synthetic (seeded random-phase solenoidal spectrum)", "config": config,
+            "p50_ms": r["p50_ms"], "p99_ms": r["p99_ms"],
+            "clocks": {"sm_mhz": r["clocks"]["sm_mhz"], "sm_max_mhz": r["clocks"]["sm_max_mhz"],
+                       "reasons": r["clocks"]["reasons"], "samples": r["clocks"]["samples"]},
+            "e2e": {"value": r["e2e"], "unit": UNIT, "h2d_bytes_per_step": r["e2e_bytes"],
+                    "d2h_bytes_per_step": r["e2e_bytes"], "steps": r["e2e_steps"],
+                    "path": "mhd_set_state(pinned host) + mhd_step(1) + mhd_get_state(pinned host)"},
+            "gpu_launches": r["launches"],
+            "roofline": {"bound": "hbm", "kernel": r["top"], "achieved": r["achieved"], "peak": r["peak"],
+                         "unit": "GB/s", "frac": r["achieved"] / r["peak"], "peak_kind": r["peak_kind"],
+                         "traffic": ncu_traffic(r["top"], args.n), "algorithmic_bytes_per_launch": r["bytes"]},
+            "kernels": r["kernels"],
+            "cpu_baseline": cpu,
+            "baseline_note": "vs_baseline = per-GPU value / (256^3 / 0.271 s), the reference README's RTX 3080 MHD RK4 256^3 figure",
+        }
+        if r["secondary"]:
+            line["secondary"] = r["secondary"]
+        print(json.dumps(line), flush=True)
+    dist.close()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

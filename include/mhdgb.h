@@ -135,6 +135,10 @@ int mhd_kernel_class_bytes(mhd_handle h, int cls, double* bytes);
 /* Timing helper: elapsed device milliseconds of nsteps steps measured with events on the stream. */
 int mhd_time_steps(mhd_handle h, int nsteps, double* ms);
 
+/* Timing helper: nsteps steps back to back with an event between consecutive steps; fills
+ * ms_per_step[0..nsteps) with each step's device milliseconds (synchronises at the end). */
+int mhd_step_timed(mhd_handle h, int nsteps, double* ms_per_step);
+
 /* Last error message of the calling thread ("" if none). */
 const char* mhd_last_error(void);
 

@@ -74,6 +74,7 @@ _SIGS = {
     "mhd_kernel_class_count": (C.c_int, []),
     "mhd_kernel_class_bytes": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_double)]),
     "mhd_time_steps": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_double)]),
+    "mhd_step_timed": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_double)]),
     "mhd_last_error": (C.c_char_p, []),
 }
 

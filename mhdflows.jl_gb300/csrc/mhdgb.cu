@@ -287,7 +287,7 @@ struct mhd_problem {
       f();
       cudaEventRecord(r.b, stream);
       recs.push_back(r);
-      if (recs.size() > 4096) { int rc = fold_records(); if (rc) return rc; }
+      if (recs.size() > (1u << 16)) { int rc = fold_records(); if (rc) return rc; }
     } else {
       f();
     }
@@ -694,6 +694,29 @@ int mhd_kernel_class_bytes(mhd_handle h, int cls, double* bytes) {
     default: b = 0;
   }
   *bytes = b;
+  return MHD_OK;
+}
+
+int mhd_step_timed(mhd_handle h, int nsteps, double* ms_per_step) {
+  int rc = check_handle(h);
+  if (rc) return rc;
+  if (nsteps < 1 || !ms_per_step) return fail(MHD_ERR_INVALID, "nsteps >= 1 and a non-null output are required");
+  std::vector<cudaEvent_t> ev(nsteps + 1);
+  for (auto& e : ev) MHD_CUDA(cudaEventCreate(&e));
+  cudaEventRecord(ev[0], h->stream);
+  for (int i = 0; i < nsteps && rc == MHD_OK; ++i) {
+    rc = mhd_step(h, 1);
+    cudaEventRecord(ev[i + 1], h->stream);
+  }
+  cudaError_t e = cudaEventSynchronize(ev[nsteps]);
+  for (int i = 0; i < nsteps; ++i) {
+    float f = 0.f;
+    if (e == cudaSuccess) cudaEventElapsedTime(&f, ev[i], ev[i + 1]);
+    ms_per_step[i] = f;
+  }
+  for (auto& x : ev) cudaEventDestroy(x);
+  if (rc) return rc;
+  if (e != cudaSuccess) return fail(MHD_ERR_CUDA, std::string("cudaEventSynchronize: ") + cudaGetErrorString(e));
   return MHD_OK;
 }
 

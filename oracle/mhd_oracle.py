@@ -331,6 +331,69 @@ def mode_phases(seed: int, field: int, kx, ky, kz):
     return (h >> np.uint64(11)).astype(np.float64) * (2.0 ** -53) * (2 * math.pi)
 
 
+def kept_wavenumbers(n: int):
+    """Integer wavenumbers of the kept rfft-axis modes and of the kept full-axis modes (kept-index order)."""
+    kx, kp, kn = kept_counts(n)
+    full = np.concatenate([np.arange(kp), np.arange(-kn, 0)]).astype(np.int64)
+    return np.arange(kx, dtype=np.int64), full
+
+
+def random_spectrum_compact(n: int, seed: int, L: float = 2 * math.pi, e_u: float = 0.5,
+                            b_ratio: float = 0.3, kpeak: float = 4.0):
+    """Retained band (6, K2, K2, Kx) [f, kz', ky', kx] of ``random_spectrum_state`` (float64)."""
+    kxs, kfs = kept_wavenumbers(n)
+    K2, Kx = len(kfs), len(kxs)
+    KZ, KY, KX = np.meshgrid(kfs, kfs, kxs, indexing="ij")
+    s2p = 2 * math.pi / L
+    kx, ky, kz = KX * s2p, KY * s2p, KZ * s2p
+    k2 = kx ** 2 + ky ** 2 + kz ** 2
+    k = np.sqrt(k2)
+    with np.errstate(divide="ignore", invalid="ignore"):
+        amp = np.sqrt(k ** 4 * np.exp(-2 * (k / kpeak) ** 2) / (4 * math.pi * k2))
+    amp[k2 == 0] = 0.0
+    sol = np.empty((6, K2, K2, Kx), dtype=np.complex128)
+    for f in range(6):
+        sol[f] = amp * np.exp(1j * mode_phases(seed, f, KX, KY, KZ))
+    # Hermitian kx = 0 plane: F(0,-ky,-kz) = conj(F(0,ky,kz)); partner outside the band -> 0
+    pos = {int(v): i for i, v in enumerate(kfs)}
+    partner = np.array([pos.get(int(-v), -1) for v in kfs])
+    has = partner >= 0
+    pz, py = np.meshgrid(partner, partner, indexing="ij")
+    both = has[:, None] & has[None, :]
+    for f in range(6):
+        p = sol[f, :, :, 0]
+        herm = np.zeros_like(p)
+        herm[both] = 0.5 * (p[both] + np.conj(p[pz[both], py[both]]))
+        sol[f, :, :, 0] = herm
+    inv = np.where(k2 > 0, 1.0 / np.where(k2 > 0, k2, 1.0), 0.0)
+    kv = (kx, ky, kz)
+    for base in (0, 3):
+        dot = (kv[0] * sol[base] + kv[1] * sol[base + 1] + kv[2] * sol[base + 2]) * inv
+        for i in range(3):
+            sol[base + i] -= kv[i] * dot
+    w = np.where(KX == 0, 1.0, 2.0)
+
+    def mean_sq(fs):
+        return float(sum(np.sum(w * (sol[f].real ** 2 + sol[f].imag ** 2)) for f in fs)) / float(n) ** 6
+
+    mu, mb = mean_sq((0, 1, 2)), mean_sq((3, 4, 5))
+    su = math.sqrt(2 * e_u / mu) if mu > 0 else 0.0
+    sb = math.sqrt((b_ratio ** 2) * (2 * e_u) / mb) if mb > 0 else 0.0
+    sol[0:3] *= su
+    sol[3:6] *= sb
+    return sol
+
+
+def expand_compact(n: int, compact, dtype=np.complex128):
+    """Full half-spectrum state (6, n, n, nkr) from a retained-band array (alias band zero)."""
+    kxs, kfs = kept_wavenumbers(n)
+    idx = kfs % n
+    out = np.zeros((compact.shape[0], n, n, n // 2 + 1), dtype=dtype)
+    for f in range(compact.shape[0]):
+        out[f][np.ix_(idx, idx, np.arange(len(kxs)))] = compact[f]
+    return out
+
+
 def random_spectrum_state(grid: Grid, seed: int, e_u: float = 0.5, b_ratio: float = 0.3,
                           kpeak: float = 4.0):
     """Seeded random-phase solenoidal u, B with shell spectrum E(k) ~ k^4 exp(-2 (k/kpeak)^2).
@@ -341,54 +404,8 @@ def random_spectrum_state(grid: Grid, seed: int, e_u: float = 0.5, b_ratio: floa
     (F - k (k.F)/k^2), u is normalised to E_u = <|u|^2>/2 = e_u and B to b_ratio times u's rms.
     Built in float64 and returned in the grid's complex dtype.
     """
-    g = Grid(grid.n, grid.L, np.float64)
-    n = g.n
-    kf = np.fft.fftfreq(n, 1.0 / n).astype(np.int64)
-    KZ, KY, KX = np.meshgrid(kf, kf, np.arange(g.nkr), indexing="ij")
-    kx = KX * (2 * math.pi / g.L)
-    ky = KY * (2 * math.pi / g.L)
-    kz = KZ * (2 * math.pi / g.L)
-    k2 = kx ** 2 + ky ** 2 + kz ** 2
-    k = np.sqrt(k2)
-    with np.errstate(divide="ignore", invalid="ignore"):
-        amp = np.sqrt(k ** 4 * np.exp(-2 * (k / kpeak) ** 2) / (4 * math.pi * k2))
-    amp[0, 0, 0] = 0.0
-    keep = g.retained_mask()
-    amp = np.where(keep, amp, 0.0)
-    sol = np.zeros((6, n, n, g.nkr), dtype=np.complex128)
-    for f in range(6):
-        ph = mode_phases(seed, f, KX, KY, KZ)
-        sol[f] = amp * np.exp(1j * ph)
-    # Hermitian kx = 0 plane: F(0,-ky,-kz) = conj(F(0,ky,kz)); partner outside the band -> 0
-    for f in range(6):
-        p = sol[f, :, :, 0]
-        iz = (-np.arange(n)) % n
-        partner = np.conj(p[np.ix_(iz, iz)])
-        herm = 0.5 * (p + partner)
-        km = keep[:, :, 0] & keep[:, :, 0][np.ix_(iz, iz)]
-        sol[f, :, :, 0] = np.where(km, herm, 0.0)
-    # solenoidal projection
-    with np.errstate(invalid="ignore", divide="ignore"):
-        inv = np.where(k2 > 0, 1.0 / np.where(k2 > 0, k2, 1.0), 0.0)
-    kv = (kx, ky, kz)
-    for base in (0, 3):
-        dot = sum(kv[i] * sol[base + i] for i in range(3)) * inv
-        for i in range(3):
-            sol[base + i] -= kv[i] * dot
-    # normalisation via Parseval on the half spectrum (kx = 0 weight 1, else 2)
-    w = np.where(KX == 0, 1.0, 2.0)
-
-    def mean_sq(fs):
-        return float(sum(np.sum(w * np.abs(sol[f]) ** 2) for f in fs)) / float(n) ** 6
-
-    mu = mean_sq((0, 1, 2))
-    mb = mean_sq((3, 4, 5))
-    su = math.sqrt(2 * e_u / mu) if mu > 0 else 0.0
-    target_b = (b_ratio ** 2) * (2 * e_u)
-    sb = math.sqrt(target_b / mb) if mb > 0 else 0.0
-    sol[0:3] *= su
-    sol[3:6] *= sb
-    return sol.astype(grid.cdtype)
+    c = random_spectrum_compact(grid.n, seed, grid.L, e_u, b_ratio, kpeak)
+    return expand_compact(grid.n, c, dtype=grid.cdtype)
 
 
 # ----------------------------------------------------------------------------------------------
