@@ -221,10 +221,14 @@ struct Plan {
   static constexpr int LF = N / RF;                    // output label count
   static constexpr int DI = V / R0;                    // input slots per thread
   static constexpr int DF = V / RF;                    // output slots per thread
-  // shared-memory exchange strides (padding spreads 8-byte words over banks for row layouts)
-  static constexpr int P1 = 1;
+  // Shared-memory exchange strides.  Padding spreads the 8-byte words a half-warp touches over the
+  // 16 bank pairs when consecutive lanes hold consecutive labels (row layouts): stage-2 readers
+  // of one instruction differ in k0 (stride E1S) and n2 (stride 1), so E1S = 16/R0 (mod 16)
+  // interleaves them; stage-3 writers differ in k0 (stride 1) and n2 (stride E2S), so E2S = R0.
+  static constexpr bool kPow2R0 = R0 <= 16 && (16 % R0) == 0;
+  static constexpr int P1 = kPow2R0 ? ((16 / R0) % 16 - (R1 * R2) % 16 + 32) % 16 : 1;
   static constexpr int E1S = R1 * R2 + P1;
-  static constexpr int P2 = (R0 * R1) % 16 == 0 ? (R0 % 16) : 0;
+  static constexpr int P2 = kPow2R0 ? ((R0 % 16) - (R0 * R1) % 16 + 32) % 16 : 0;
   static constexpr int E2S = R0 * R1 + P2;
   static constexpr int SMEM1 = R0 * E1S;              // words used by exchange 1
   static constexpr int SMEM2 = R2 * E2S;              // words used by exchange 2

@@ -5,8 +5,8 @@
 //   y_inverse  (colbuf -> rowbuf, 6 fields, pruned input)
 //   x_fused    (rowbuf -> rowbuf: c2r, 8 quadratic products, r2c; physical fields never leave chip)
 //   y_forward  (rowbuf -> colbuf, 8 products, pruned output)
-//   z_epi_mom  (colbuf -> state: z r2c of 5 stress products, Leray projection, -nu k^2, RK update)
-//   z_epi_ind  (colbuf -> state: z r2c of 3 EMF products, curl, -eta k^2, RK update)
+//   z_forward  (colbuf -> compact product spectra: z r2c of the 8 products, pruned output)
+//   rk_epilogue (Leray projection, curl, -nu k^2 / -eta k^2 and the RK stage update, streaming)
 // The state is kept only on the retained (2/3-rule) band, which is all the reference's dynamics
 // ever read: dealias! zeroes the alias band of the stage state before every RHS evaluation.
 #include <cuda_runtime.h>
@@ -66,7 +66,6 @@ struct OpsBase {
   virtual void x_fused(float2* buf, const Geom& g, long long rowstride, long long slot, const float2* tw, cudaStream_t s) = 0;
   virtual void x_c2r(const float2* src, float* dst, const Geom& g, long long srow, const float2* tw, cudaStream_t s) = 0;
   virtual void x_r2c(const float* src, float2* dst, const Geom& g, long long drow, const float2* tw, cudaStream_t s) = 0;
-  virtual void z_epi(int kind, const EpiArgs& a, const Geom& g, const float2* tw, cudaStream_t s) = 0;
 };
 
 template <class K>
@@ -85,7 +84,6 @@ struct Ops : OpsBase {
   static constexpr int TX = Cfg<N>::TX, TXE = Cfg<N>::TXE, ROWS = Cfg<N>::ROWS;
   static constexpr size_t kColSmem = sizeof(float2) * C::SMEM * TX;
   static constexpr size_t kRowSmem = sizeof(float2) * RowCfg<R>::TS;
-  static size_t epi_smem(int nprod, int k2) { return sizeof(float2) * ((size_t)C::SMEM * TXE + (size_t)nprod * k2 * TXE); }
 
   int setup() override {
     int rc = MHD_OK;
@@ -94,10 +92,6 @@ struct Ops : OpsBase {
     if ((rc = set_smem(x_fused_kernel<R, ROWS>, kRowSmem * 4 * ROWS))) return rc;
     if ((rc = set_smem(x_c2r_kernel<R, ROWS>, kRowSmem * ROWS))) return rc;
     if ((rc = set_smem(x_r2c_kernel<R, ROWS>, kRowSmem * ROWS))) return rc;
-    const int k2max = N;  // upper bound of kept modes per axis
-    if ((rc = set_smem(z_epilogue_kernel<C, TXE, 0>, epi_smem(5, k2max)))) return rc;
-    if ((rc = set_smem(z_epilogue_kernel<C, TXE, 1>, epi_smem(3, k2max)))) return rc;
-    if ((rc = set_smem(z_epilogue_kernel<C, TXE, 2>, epi_smem(1, k2max)))) return rc;
     return MHD_OK;
   }
   void col_inv(const ColArgs& a, const Geom& g, int outer, int nf, const float2* tw, cudaStream_t s) override {
@@ -119,14 +113,6 @@ struct Ops : OpsBase {
   void x_r2c(const float* src, float2* dst, const Geom& g, long long drow, const float2* tw, cudaStream_t s) override {
     const long long pairs = (long long)N * N / 2;
     x_r2c_kernel<R, ROWS><<<(unsigned)(pairs / ROWS), ROWS * R::G, kRowSmem * ROWS, s>>>(src, dst, g, drow, tw);
-  }
-  void z_epi(int kind, const EpiArgs& a, const Geom& g, const float2* tw, cudaStream_t s) override {
-    dim3 grid((g.kx + TXE - 1) / TXE, g.k2, 1);
-    const int nprod = kind == 0 ? 5 : (kind == 1 ? 3 : 1);
-    const size_t sm = epi_smem(nprod, g.k2);
-    if (kind == 0) z_epilogue_kernel<C, TXE, 0><<<grid, TXE * C::G, sm, s>>>(a, g, tw);
-    else if (kind == 1) z_epilogue_kernel<C, TXE, 1><<<grid, TXE * C::G, sm, s>>>(a, g, tw);
-    else z_epilogue_kernel<C, TXE, 2><<<grid, TXE * C::G, sm, s>>>(a, g, tw);
   }
 };
 
@@ -169,8 +155,8 @@ Geom make_geom(int n, double L) {
 }
 
 // Kernel classes for per-launch timing.
-enum KClass { KC_ZINV = 0, KC_YINV, KC_XFUSED, KC_YFWD, KC_ZEPI_MOM, KC_ZEPI_IND, KC_OTHER, KC_COUNT };
-const char* kClassNames[KC_COUNT] = {"z_inverse", "y_inverse", "x_fused", "y_forward", "z_epi_momentum", "z_epi_induction", "other"};
+enum KClass { KC_ZINV = 0, KC_YINV, KC_XFUSED, KC_YFWD, KC_ZFWD, KC_RKEPI, KC_OTHER, KC_COUNT };
+const char* kClassNames[KC_COUNT] = {"z_inverse", "y_inverse", "x_fused", "y_forward", "z_forward", "rk_epilogue", "other"};
 
 const double kLsA[5] = {0.0, -567301805773.0 / 1357537059087.0, -2404267990393.0 / 2016746695238.0,
                         -3550918686646.0 / 2091501179385.0, -1275806237668.0 / 842570457699.0};
@@ -319,39 +305,35 @@ struct mhd_problem {
     ColArgs a{rowbuf, colbuf, (long long)g.kxp, BZ(), SLK(), (long long)g.kxp, AZ(), SLK(), 1.0f};
     return launch(KC_YFWD, [&] { ops->col_fwd(a, g, g.n, nf, tw, stream); });
   }
-  EpiArgs epi_base(int slot0, int field0) const {
-    EpiArgs a{};
-    a.prod = colbuf;
-    a.pO = SLK();
-    a.pR = AZ();
-    a.pS = g.kxp;
-    a.slot0 = slot0;
-    a.fS = FS();
-    a.sKz = (long long)g.k2 * g.kxp;
-    a.sKy = g.kxp;
-    (void)field0;
-    return a;
+  // colbuf slots -> compact planes (nf fields/products) of dst, pruned output
+  int z_forward(float2* dst, int nf) {
+    ColArgs a{colbuf, dst, (long long)g.kxp, SLK(), AZ(), FS(), (long long)g.kxp, (long long)g.k2 * g.kxp, 1.0f};
+    return launch(KC_ZFWD, [&] { ops->col_fwd(a, g, g.k2, nf, tw, stream); });
   }
-  // Epilogues of one stage: X stage state, op, coefficients.
+  // Stage epilogue: RHS from the 8 compact product planes (in rowbuf) and the stage state X.
+  int epilogue(const float2* X, int op, float h, float ca, float cb) {
+    RkArgs a{};
+    a.prod = rowbuf;
+    a.X = X;
+    a.sol = sol;
+    a.acc = acc;
+    a.xn = (op == OP_LS_FIRST || op == OP_LS) ? sol : xs;
+    a.fs = FS();
+    a.nu = (float)p.nu;
+    a.eta = (float)p.eta;
+    a.h = h;
+    a.dt = (float)p.dt;
+    a.ca = ca;
+    a.cb = cb;
+    a.op = op;
+    const long long blocks = (FS() + 255) / 256;
+    const unsigned grid = (unsigned)(blocks < 152 * 16 ? blocks : 152 * 16);
+    return launch(KC_RKEPI, [&] { rk_epilogue_kernel<<<grid, 256, 0, stream>>>(a, g); });
+  }
   int epilogues(const float2* X, int op, float h, float ca, float cb) {
-    const float dtf = (float)p.dt;
-    for (int grp = 0; grp < 2; ++grp) {
-      EpiArgs a = epi_base(grp == 0 ? 0 : 5, grp * 3);
-      const long long off = (long long)grp * 3 * FS();
-      a.X = X + off;
-      a.sol = sol + off;
-      a.acc = acc + off;
-      a.xn = (op == OP_LS_FIRST || op == OP_LS) ? sol + off : xs + off;
-      a.visc = (float)(grp == 0 ? p.nu : p.eta);
-      a.h = h;
-      a.dt = dtf;
-      a.ca = ca;
-      a.cb = cb;
-      a.op = op;
-      int rc = launch(grp == 0 ? KC_ZEPI_MOM : KC_ZEPI_IND, [&] { ops->z_epi(grp, a, g, tw, stream); });
-      if (rc) return rc;
-    }
-    return MHD_OK;
+    int rc;
+    if ((rc = z_forward(rowbuf, kSlots))) return rc;
+    return epilogue(X, op, h, ca, cb);
   }
   int rhs_passes(const float2* X) {
     int rc;
@@ -395,11 +377,7 @@ struct mhd_problem {
     int rc;
     if ((rc = launch(KC_OTHER, [&] { ops->x_r2c(phys, rowbuf, g, SLK(), tw, stream); }))) return rc;
     if ((rc = y_forward(1))) return rc;
-    EpiArgs a = epi_base(0, 0);
-    a.X = dst;
-    a.acc = dst;
-    a.op = OP_STORE;
-    return launch(KC_OTHER, [&] { ops->z_epi(2, a, g, tw, stream); });
+    return z_forward(dst, 1);
   }
 };
 
@@ -682,15 +660,15 @@ int mhd_kernel_class_bytes(mhd_handle h, int cls, double* bytes) {
   const double n = h->g.n, kx = h->g.kx, k2 = h->g.k2, c = 8.0;
   const double state_field = k2 * k2 * kx * c;
   double b = 0;
-  // state arrays touched by one epilogue launch (3 fields), averaged over the scheme's stages
-  const double rk4_arrays = h->p.scheme == MHD_RK4 ? (3 + 5 + 5 + 4) / 4.0 : (3 + 4 * 4) / 5.0;
+  // state arrays (6 fields each) one epilogue launch touches, averaged over the scheme's stages
+  const double arrays = h->p.scheme == MHD_RK4 ? (3 + 5 + 5 + 4) / 4.0 : (3 + 4 * 4) / 5.0;
   switch (cls) {
     case KC_ZINV: b = 6 * (state_field + n * k2 * kx * c); break;
     case KC_YINV: b = 6 * (n * k2 * kx * c + n * n * kx * c); break;
     case KC_XFUSED: b = (6 + 8) * n * n * kx * c; break;
     case KC_YFWD: b = 8 * (n * n * kx * c + n * k2 * kx * c); break;
-    case KC_ZEPI_MOM: b = 5 * n * k2 * kx * c + rk4_arrays * 3 * state_field; break;
-    case KC_ZEPI_IND: b = 3 * n * k2 * kx * c + rk4_arrays * 3 * state_field; break;
+    case KC_ZFWD: b = 8 * (n * k2 * kx * c + state_field); break;
+    case KC_RKEPI: b = 8 * state_field + arrays * 6 * state_field; break;
     default: b = 0;
   }
   *bytes = b;

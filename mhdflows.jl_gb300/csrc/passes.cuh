@@ -31,6 +31,20 @@ struct BlockSync {
   __device__ __forceinline__ void operator()() const { __syncthreads(); }
 };
 
+// Barrier over the threads that share one row's shared-memory buffers: a warp when a row (or
+// several rows) fits in one warp, otherwise a named barrier over the row's G threads.
+template <int G>
+struct RowSync {
+  int id;
+  __device__ __forceinline__ void operator()() const {
+    if constexpr (G <= 32) {
+      __syncwarp();
+    } else {
+      asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(G) : "memory");
+    }
+  }
+};
+
 struct ColArgs {
   const float2* src;
   float2* dst;
@@ -138,7 +152,7 @@ __global__ void __launch_bounds__(ROWS * P::G) x_fused_kernel(float2* buf, Geom 
   float2* rowp = buf + row * rowstride;
   float2* sb = smem + r * 4 * TS;
   const int kx = geo.kx;
-  auto sync = BlockSync{};
+  const RowSync<G> sync{1 + r};
 
   float2 v[3][V];
 #pragma unroll
@@ -164,9 +178,9 @@ __global__ void __launch_bounds__(ROWS * P::G) x_fused_kernel(float2* buf, Geom 
     w[2][i] = make_float2(tyz, axy);
     w[3][i] = make_float2(axz, ayz);
   }
-  __syncthreads();
+  sync();
   fft_run<PR, -1, 4, TS, 1>(w, sb, 0, g, tw, sync);
-  __syncthreads();
+  sync();
 #pragma unroll
   for (int t = 0; t < 4; ++t)
 #pragma unroll
@@ -176,7 +190,7 @@ __global__ void __launch_bounds__(ROWS * P::G) x_fused_kernel(float2* buf, Geom 
         const int k = g + G * d + PR::LF * e;
         if (k < kx || k > N - kx) sb[t * TS + k] = w[t][d * PR::RF + e];
       }
-  __syncthreads();
+  sync();
 #pragma unroll
   for (int t = 0; t < 4; ++t) store_split_pair(sb + t * TS, N, kx, g, G, rowp + (2 * t) * slot, rowp + (2 * t + 1) * slot);
 }
@@ -192,7 +206,7 @@ __global__ void __launch_bounds__(ROWS * P::G) x_c2r_kernel(const float2* src, f
   const long long q = (long long)blockIdx.x * ROWS + r;
   float2 v[1][V];
   load_herm_pair<P>(v[0], src + (2 * q) * srow, src + (2 * q + 1) * srow, geo.kx, g);
-  fft_run<P, +1, 1, TS, 1>(v, smem + r * TS, 0, g, tw, BlockSync{});
+  fft_run<P, +1, 1, TS, 1>(v, smem + r * TS, 0, g, tw, RowSync<G>{1 + r});
   float* da = dst + (2 * q) * N;
   float* db = dst + (2 * q + 1) * N;
 #pragma unroll
@@ -225,8 +239,9 @@ __global__ void __launch_bounds__(ROWS * P::G) x_r2c_kernel(const float* src, fl
       v[0][d * P::R0 + n0] = make_float2(__ldg(sa + x), __ldg(sbp + x));
     }
   float2* sb = smem + r * TS;
-  fft_run<P, -1, 1, TS, 1>(v, sb, 0, g, tw, BlockSync{});
-  __syncthreads();
+  const RowSync<G> sync{1 + r};
+  fft_run<P, -1, 1, TS, 1>(v, sb, 0, g, tw, sync);
+  sync();
 #pragma unroll
   for (int d = 0; d < P::DF; ++d)
 #pragma unroll
@@ -234,13 +249,11 @@ __global__ void __launch_bounds__(ROWS * P::G) x_r2c_kernel(const float* src, fl
       const int k = g + G * d + P::LF * e;
       if (k < geo.kx || k > N - geo.kx) sb[k] = v[0][d * P::RF + e];
     }
-  __syncthreads();
+  sync();
   store_split_pair(sb, N, geo.kx, g, G, dst + (2 * q) * drow, dst + (2 * q + 1) * drow);
 }
 
-// ------------------------------------------------------------------------------------------
-// z forward pass fused with the spectral right-hand side and the Runge-Kutta stage update.
-// ------------------------------------------------------------------------------------------
+// Runge-Kutta stage operations of the epilogue.
 enum StageOp : int {
   OP_RHS = 0,       // out <- R
   OP_RK4_FIRST = 1, // acc <- R/6 ; xn <- sol + h R            (X = sol)
@@ -248,138 +261,101 @@ enum StageOp : int {
   OP_RK4_LAST = 3,  // sol <- sol + dt (acc + R/6)
   OP_LS_FIRST = 4,  // du <- dt R ; u <- u + b du              (X = u)
   OP_LS = 5,        // du <- a du + dt R ; u <- u + b du
-  OP_STORE = 6,     // out <- transformed product spectrum (plain forward transform)
 };
 
-struct EpiArgs {
-  const float2* prod;   // colbuf base
-  long long pO, pR, pS; // colbuf strides: ky' (outer), z (row), slot
-  int slot0;            // first product slot used by this kernel
-  // compact state arrays, already offset to the first field of this kernel's group
-  const float2* X;      // stage state (diffusion operand)
-  float2* sol;          // RK4: step-start state / LSRK4: unused
-  float2* acc;          // RK4 accumulator / LSRK4 du / OP_RHS,OP_STORE output
-  float2* xn;           // RK4 next stage state / LSRK4 u (updated in place)
-  long long fS, sKz, sKy;  // compact strides: field, kz', ky'
-  float visc;           // nu (momentum) or eta (induction)
-  float h;              // RK4 stage fraction * dt
-  float dt;
-  float ca, cb;         // LSRK4 coefficients
+// ------------------------------------------------------------------------------------------
+// Streaming right-hand side + Runge-Kutta stage update over the compact retained band.
+// prod: compact spectra of the 8 products [p][kz'][ky'][kx] (Dxz Dyz Txy Txz Tyz Axy Axz Ayz).
+// Momentum: R_u = i (V - k (k.V)/k^2) - nu k^2 X_u with V = (kx Dxz + ky Txy + kz Txz,
+// kx Txy + ky Dyz + kz Tyz, kx Txz + ky Tyz) (the stress tensor minus Tzz*I, whose gradient the
+// projection removes).  Induction: R_b = i k x E - eta k^2 X_b with E = (Ayz, -Axz, Axy) = u x B.
+// ------------------------------------------------------------------------------------------
+struct RkArgs {
+  const float2* prod;   // 8 compact planes
+  const float2* X;      // stage state (6 fields)
+  float2* sol;          // RK4 step-start state
+  float2* acc;          // RK4 accumulator / LSRK4 du / OP_RHS output
+  float2* xn;           // RK4 next stage state / LSRK4 u
+  long long fs;         // compact field stride (complex elements)
+  float nu, eta, h, dt, ca, cb;
   int op;
 };
 
-// NPROD = 5 (momentum: Dxz Dyz Txy Txz Tyz), 3 (induction: Axy Axz Ayz) or 1 (plain store).
-template <class P, int TX, int KIND>
-__global__ void __launch_bounds__(TX * P::G) z_epilogue_kernel(EpiArgs a, Geom geo, const float2* __restrict__ tw) {
-  constexpr int NPROD = KIND == 0 ? 5 : (KIND == 1 ? 3 : 1);
-  constexpr int G = P::G, V = P::V;
-  extern __shared__ float2 smem[];
-  float2* xb = smem;
-  float2* pb = smem + P::SMEM * TX;
-  const int tx = threadIdx.x % TX, g = threadIdx.x / TX;
-  const int kxg = blockIdx.x * TX + tx;
-  const bool colok = kxg < geo.kx;
-  const int ky = blockIdx.y;
-  const int K2 = geo.k2;
-  auto sync = BlockSync{};
-  for (int p = 0; p < NPROD; ++p) {
-    const float2* src = a.prod + (long long)ky * a.pO + (long long)(a.slot0 + p) * a.pS + kxg;
-    float2 v[1][V];
-#pragma unroll
-    for (int d = 0; d < P::DI; ++d)
-#pragma unroll
-      for (int n0 = 0; n0 < P::R0; ++n0) {
-        const int n = g + G * d + P::LI * n0;
-        v[0][d * P::R0 + n0] = colok ? __ldg(src + n * a.pR) : make_float2(0.f, 0.f);
-      }
-    fft_run<P, -1, 1, 0, TX>(v, xb, tx, g, tw, sync);
-#pragma unroll
-    for (int d = 0; d < P::DF; ++d)
-#pragma unroll
-      for (int e = 0; e < P::RF; ++e) {
-        const int k = g + G * d + P::LF * e;
-        const int j = kept_of_freq(geo, k);
-        if (j >= 0) pb[(p * K2 + j) * TX + tx] = v[0][d * P::RF + e];
-      }
-    __syncthreads();
+__device__ __forceinline__ float2 rk_apply(int op, const RkArgs& a, long long o, float2 x, float2 R) {
+  switch (op) {
+    case OP_RHS: a.acc[o] = R; break;
+    case OP_RK4_FIRST:
+      a.acc[o] = make_float2(R.x / 6.f, R.y / 6.f);
+      a.xn[o] = make_float2(x.x + a.h * R.x, x.y + a.h * R.y);
+      break;
+    case OP_RK4_MID: {
+      const float2 s = a.sol[o], q = a.acc[o];
+      a.acc[o] = make_float2(q.x + R.x / 3.f, q.y + R.y / 3.f);
+      a.xn[o] = make_float2(s.x + a.h * R.x, s.y + a.h * R.y);
+    } break;
+    case OP_RK4_LAST: {
+      const float2 s = a.sol[o], q = a.acc[o];
+      const float2 tot = make_float2(q.x + R.x / 6.f, q.y + R.y / 6.f);
+      a.sol[o] = make_float2(s.x + a.dt * tot.x, s.y + a.dt * tot.y);
+    } break;
+    case OP_LS_FIRST: {
+      const float2 du = make_float2(a.dt * R.x, a.dt * R.y);
+      a.acc[o] = du;
+      a.xn[o] = make_float2(x.x + a.cb * du.x, x.y + a.cb * du.y);
+    } break;
+    case OP_LS: {
+      const float2 q = a.acc[o];
+      const float2 du = make_float2(a.ca * q.x + a.dt * R.x, a.ca * q.y + a.dt * R.y);
+      a.acc[o] = du;
+      a.xn[o] = make_float2(x.x + a.cb * du.x, x.y + a.cb * du.y);
+    } break;
+    default: break;
   }
-  if (!colok) return;
-  const float kxv = geo.kscale * (float)kxg;
-  const float kyv = geo.kscale * (float)signed_of_kept(geo, ky);
-  for (int j = g; j < K2; j += G) {
-    const long long idx = (long long)j * a.sKz + (long long)ky * a.sKy + kxg;
-    if (KIND == 2) {
-      a.acc[idx] = pb[j * TX + tx];
-      continue;
-    }
-    const float kzv = geo.kscale * (float)signed_of_kept(geo, j);
+  return R;
+}
+
+__global__ void __launch_bounds__(256) rk_epilogue_kernel(RkArgs a, Geom geo) {
+  const long long fs = a.fs;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < fs; i += (long long)gridDim.x * blockDim.x) {
+    const int x = (int)(i % geo.kxp);
+    if (x >= geo.kx) continue;
+    long long r = i / geo.kxp;
+    const int jy = (int)(r % geo.k2);
+    const int jz = (int)(r / geo.k2);
+    const float kxv = geo.kscale * (float)x;
+    const float kyv = geo.kscale * (float)signed_of_kept(geo, jy);
+    const float kzv = geo.kscale * (float)signed_of_kept(geo, jz);
     const float k2 = kxv * kxv + kyv * kyv + kzv * kzv;
-    float2 nl[3];
-    if (KIND == 0) {
-      const float2 dxz = pb[(0 * K2 + j) * TX + tx], dyz = pb[(1 * K2 + j) * TX + tx];
-      const float2 txy = pb[(2 * K2 + j) * TX + tx], txz = pb[(3 * K2 + j) * TX + tx];
-      const float2 tyz = pb[(4 * K2 + j) * TX + tx];
-      float2 Vx, Vy, Vz;
-      Vx.x = kxv * dxz.x + kyv * txy.x + kzv * txz.x;  Vx.y = kxv * dxz.y + kyv * txy.y + kzv * txz.y;
-      Vy.x = kxv * txy.x + kyv * dyz.x + kzv * tyz.x;  Vy.y = kxv * txy.y + kyv * dyz.y + kzv * tyz.y;
-      Vz.x = kxv * txz.x + kyv * tyz.x;                Vz.y = kxv * txz.y + kyv * tyz.y;
-      const float ik2 = k2 > 0.f ? 1.0f / k2 : 0.f;
-      float2 kv;
-      kv.x = (kxv * Vx.x + kyv * Vy.x + kzv * Vz.x) * ik2;
-      kv.y = (kxv * Vx.y + kyv * Vy.y + kzv * Vz.y) * ik2;
-      // i * (V - k (k.V)/k^2)
-      const float2 px = make_float2(Vx.x - kxv * kv.x, Vx.y - kxv * kv.y);
-      const float2 py = make_float2(Vy.x - kyv * kv.x, Vy.y - kyv * kv.y);
-      const float2 pz = make_float2(Vz.x - kzv * kv.x, Vz.y - kzv * kv.y);
-      nl[0] = make_float2(-px.y, px.x);
-      nl[1] = make_float2(-py.y, py.x);
-      nl[2] = make_float2(-pz.y, pz.x);
-    } else {
-      const float2 axy = pb[(0 * K2 + j) * TX + tx], axz = pb[(1 * K2 + j) * TX + tx];
-      const float2 ayz = pb[(2 * K2 + j) * TX + tx];
-      // Wx = i(ky Axy + kz Axz), Wy = i(-kx Axy + kz Ayz), Wz = -i(kx Axz + ky Ayz)
-      const float2 wx = make_float2(kyv * axy.x + kzv * axz.x, kyv * axy.y + kzv * axz.y);
-      const float2 wy = make_float2(-kxv * axy.x + kzv * ayz.x, -kxv * axy.y + kzv * ayz.y);
-      const float2 wz = make_float2(-kxv * axz.x - kyv * ayz.x, -kxv * axz.y - kyv * ayz.y);
-      nl[0] = make_float2(-wx.y, wx.x);
-      nl[1] = make_float2(-wy.y, wy.x);
-      nl[2] = make_float2(-wz.y, wz.x);
-    }
-    const float dk = -a.visc * k2;
+    float2 p[8];
 #pragma unroll
-    for (int c = 0; c < 3; ++c) {
-      const long long o = idx + c * a.fS;
-      const float2 x = a.X[o];
-      const float2 R = make_float2(nl[c].x + dk * x.x, nl[c].y + dk * x.y);
-      switch (a.op) {
-        case OP_RHS: a.acc[o] = R; break;
-        case OP_RK4_FIRST: {
-          a.acc[o] = make_float2(R.x / 6.f, R.y / 6.f);
-          a.xn[o] = make_float2(x.x + a.h * R.x, x.y + a.h * R.y);
-        } break;
-        case OP_RK4_MID: {
-          const float2 s = a.sol[o], q = a.acc[o];
-          a.acc[o] = make_float2(q.x + R.x / 3.f, q.y + R.y / 3.f);
-          a.xn[o] = make_float2(s.x + a.h * R.x, s.y + a.h * R.y);
-        } break;
-        case OP_RK4_LAST: {
-          const float2 s = a.sol[o], q = a.acc[o];
-          const float2 tot = make_float2(q.x + R.x / 6.f, q.y + R.y / 6.f);
-          a.sol[o] = make_float2(s.x + a.dt * tot.x, s.y + a.dt * tot.y);
-        } break;
-        case OP_LS_FIRST: {
-          const float2 du = make_float2(a.dt * R.x, a.dt * R.y);
-          a.acc[o] = du;
-          a.xn[o] = make_float2(x.x + a.cb * du.x, x.y + a.cb * du.y);
-        } break;
-        case OP_LS: {
-          const float2 q = a.acc[o];
-          const float2 du = make_float2(a.ca * q.x + a.dt * R.x, a.ca * q.y + a.dt * R.y);
-          a.acc[o] = du;
-          a.xn[o] = make_float2(x.x + a.cb * du.x, x.y + a.cb * du.y);
-        } break;
-        default: break;
-      }
+    for (int q = 0; q < 8; ++q) p[q] = __ldg(a.prod + q * fs + i);
+    const float2 dxz = p[0], dyz = p[1], txy = p[2], txz = p[3], tyz = p[4];
+    const float2 axy = p[5], axz = p[6], ayz = p[7];
+    float2 Vx, Vy, Vz;
+    Vx.x = kxv * dxz.x + kyv * txy.x + kzv * txz.x;  Vx.y = kxv * dxz.y + kyv * txy.y + kzv * txz.y;
+    Vy.x = kxv * txy.x + kyv * dyz.x + kzv * tyz.x;  Vy.y = kxv * txy.y + kyv * dyz.y + kzv * tyz.y;
+    Vz.x = kxv * txz.x + kyv * tyz.x;                Vz.y = kxv * txz.y + kyv * tyz.y;
+    const float ik2 = k2 > 0.f ? 1.0f / k2 : 0.f;
+    const float kvx = (kxv * Vx.x + kyv * Vy.x + kzv * Vz.x) * ik2;
+    const float kvy = (kxv * Vx.y + kyv * Vy.y + kzv * Vz.y) * ik2;
+    float2 nl[6];
+    nl[0] = make_float2(-(Vx.y - kxv * kvy), Vx.x - kxv * kvx);
+    nl[1] = make_float2(-(Vy.y - kyv * kvy), Vy.x - kyv * kvx);
+    nl[2] = make_float2(-(Vz.y - kzv * kvy), Vz.x - kzv * kvx);
+    // W = i k x E with E = (Ayz, -Axz, Axy): Wx = i(ky Axy + kz Axz), Wy = i(kz Ayz - kx Axy), Wz = -i(kx Axz + ky Ayz)
+    const float2 wx = make_float2(kyv * axy.x + kzv * axz.x, kyv * axy.y + kzv * axz.y);
+    const float2 wy = make_float2(kzv * ayz.x - kxv * axy.x, kzv * ayz.y - kxv * axy.y);
+    const float2 wz = make_float2(-(kxv * axz.x + kyv * ayz.x), -(kxv * axz.y + kyv * ayz.y));
+    nl[3] = make_float2(-wx.y, wx.x);
+    nl[4] = make_float2(-wy.y, wy.x);
+    nl[5] = make_float2(-wz.y, wz.x);
+    const float du = -a.nu * k2, db = -a.eta * k2;
+#pragma unroll
+    for (int c = 0; c < 6; ++c) {
+      const long long o = c * fs + i;
+      const float2 xv = a.X[o];
+      const float dk = c < 3 ? du : db;
+      rk_apply(a.op, a, o, xv, make_float2(nl[c].x + dk * xv.x, nl[c].y + dk * xv.y));
     }
   }
 }
