@@ -235,6 +235,15 @@ struct Plan {
   static constexpr int SMEM = (STAGES == 3 && SMEM2 > SMEM1) ? SMEM2 : SMEM1;
 };
 
+// The same plan without bank padding: column layouts put the TX columns of a tile in consecutive
+// words, so any exchange address pattern is conflict-free and the exchange fits in N*TX words.
+template <class P>
+struct Unpadded : P {
+  static constexpr int E1S = P::R1 * P::R2;
+  static constexpr int E2S = P::R0 * P::R1;
+  static constexpr int SMEM = P::N;
+};
+
 // Reversed-radix plan: its input layout equals the output layout of P.
 template <class P>
 struct Reverse;
@@ -244,6 +253,15 @@ template <int N, int G, int R0, int R1, int R2>
 struct Reverse<Plan<N, G, R0, R1, R2>> { using type = Plan<N, G, R2, R1, R0>; };
 
 __device__ __forceinline__ float2 ldtw(const float2* __restrict__ tw, int j) { return __ldg(tw + j); }
+
+// 16-byte asynchronous global -> shared copy (L2 only) and its group fences.
+__device__ __forceinline__ void cp_async16(void* smem_dst, const void* gmem_src) {
+  const unsigned int d = (unsigned int)__cvta_generic_to_shared(smem_dst);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(d), "l"(gmem_src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int NPEND>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(NPEND) : "memory"); }
 
 // Executes stages of plan P on NT independent transforms held as v[t][V] by this thread.
 // Shared memory word address of logical element a for transform t is  buf[t*TS + a*STR + OFF].

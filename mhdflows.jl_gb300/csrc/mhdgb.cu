@@ -60,7 +60,7 @@ constexpr int kSlots = 8;
 
 struct OpsBase {
   virtual ~OpsBase() {}
-  virtual int setup() = 0;
+  virtual int setup(const Geom& g) = 0;
   virtual void col_inv(const ColArgs& a, const Geom& g, int outer, int nf, const float2* tw, cudaStream_t s) = 0;
   virtual void col_fwd(const ColArgs& a, const Geom& g, int outer, int nf, const float2* tw, cudaStream_t s) = 0;
   virtual void x_fused(float2* buf, const Geom& g, long long rowstride, long long slot, const float2* tw, cudaStream_t s) = 0;
@@ -77,40 +77,66 @@ int set_smem(K kernel, size_t bytes) {
   return MHD_OK;
 }
 
+// Resident CTAs of a kernel on the whole device (persistent grid size).
+template <class K>
+int resident_ctas(K kernel, int threads, size_t smem, int* out) {
+  int dev = 0, sms = 0, per = 0;
+  cudaGetDevice(&dev);
+  cudaError_t e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, threads, smem);
+  if (e != cudaSuccess) return fail(MHD_ERR_CUDA, std::string("occupancy query: ") + cudaGetErrorString(e));
+  *out = (per < 1 ? 1 : per) * sms;
+  return MHD_OK;
+}
+
 template <int N>
 struct Ops : OpsBase {
   using C = typename Cfg<N>::C;
   using R = typename Cfg<N>::R;
-  static constexpr int TX = Cfg<N>::TX, TXE = Cfg<N>::TXE, ROWS = Cfg<N>::ROWS;
-  static constexpr size_t kColSmem = sizeof(float2) * C::SMEM * TX;
+  using XC = XCfg<R>;
+  static constexpr int TX = Cfg<N>::TX;
+  static constexpr int GROUPS = XC::TPG >= 64 ? 2 : 4;  // x row groups per CTA (128 threads)
+  static constexpr size_t kColSmem = sizeof(float2) * 2 * N * TX;
   static constexpr size_t kRowSmem = sizeof(float2) * RowCfg<R>::TS;
+  size_t x_smem = 0;
+  int col_inv_ctas = 0, col_fwd_ctas = 0, x_ctas = 0;
 
-  int setup() override {
+  int setup(const Geom& g) override {
     int rc = MHD_OK;
+    x_smem = sizeof(float2) * (size_t)GROUPS * XC::group_words(g.kxp);
     if ((rc = set_smem(col_pass_kernel<C, TX, +1, true, false>, kColSmem))) return rc;
     if ((rc = set_smem(col_pass_kernel<C, TX, -1, false, true>, kColSmem))) return rc;
-    if ((rc = set_smem(x_fused_kernel<R, ROWS>, kRowSmem * 4 * ROWS))) return rc;
-    if ((rc = set_smem(x_c2r_kernel<R, ROWS>, kRowSmem * ROWS))) return rc;
-    if ((rc = set_smem(x_r2c_kernel<R, ROWS>, kRowSmem * ROWS))) return rc;
+    if ((rc = set_smem(x_fused_kernel<R, GROUPS>, x_smem))) return rc;
+    if ((rc = set_smem(x_c2r_kernel<R, Cfg<N>::ROWS>, kRowSmem * Cfg<N>::ROWS))) return rc;
+    if ((rc = set_smem(x_r2c_kernel<R, Cfg<N>::ROWS>, kRowSmem * Cfg<N>::ROWS))) return rc;
+    if ((rc = resident_ctas(col_pass_kernel<C, TX, +1, true, false>, TX * C::G, kColSmem, &col_inv_ctas))) return rc;
+    if ((rc = resident_ctas(col_pass_kernel<C, TX, -1, false, true>, TX * C::G, kColSmem, &col_fwd_ctas))) return rc;
+    if ((rc = resident_ctas(x_fused_kernel<R, GROUPS>, GROUPS * XC::TPG, x_smem, &x_ctas))) return rc;
     return MHD_OK;
   }
   void col_inv(const ColArgs& a, const Geom& g, int outer, int nf, const float2* tw, cudaStream_t s) override {
-    dim3 grid((g.kx + TX - 1) / TX, outer, nf);
-    col_pass_kernel<C, TX, +1, true, false><<<grid, TX * C::G, kColSmem, s>>>(a, g, tw);
+    ColWork w{(g.kx + TX - 1) / TX, outer, nf, g.k2};
+    const int total = w.tiles_x * w.outer * w.nf;
+    col_pass_kernel<C, TX, +1, true, false><<<total < col_inv_ctas ? total : col_inv_ctas, TX * C::G, kColSmem, s>>>(a, g, w, tw);
   }
   void col_fwd(const ColArgs& a, const Geom& g, int outer, int nf, const float2* tw, cudaStream_t s) override {
-    dim3 grid((g.kx + TX - 1) / TX, outer, nf);
-    col_pass_kernel<C, TX, -1, false, true><<<grid, TX * C::G, kColSmem, s>>>(a, g, tw);
+    ColWork w{(g.kx + TX - 1) / TX, outer, nf, N};
+    const int total = w.tiles_x * w.outer * w.nf;
+    col_pass_kernel<C, TX, -1, false, true><<<total < col_fwd_ctas ? total : col_fwd_ctas, TX * C::G, kColSmem, s>>>(a, g, w, tw);
   }
   void x_fused(float2* buf, const Geom& g, long long rowstride, long long slot, const float2* tw, cudaStream_t s) override {
-    const long long rows = (long long)N * N;
-    x_fused_kernel<R, ROWS><<<(unsigned)(rows / ROWS), ROWS * R::G, kRowSmem * 4 * ROWS, s>>>(buf, g, rowstride, slot, tw);
+    const long long groups = (long long)N * N / XC::RPG;
+    const long long need = (groups + GROUPS - 1) / GROUPS;
+    const int grid = (int)(need < x_ctas ? need : x_ctas);
+    x_fused_kernel<R, GROUPS><<<grid, GROUPS * XC::TPG, x_smem, s>>>(buf, g, rowstride, slot, tw);
   }
   void x_c2r(const float2* src, float* dst, const Geom& g, long long srow, const float2* tw, cudaStream_t s) override {
+    constexpr int ROWS = Cfg<N>::ROWS;
     const long long pairs = (long long)N * N / 2;
     x_c2r_kernel<R, ROWS><<<(unsigned)(pairs / ROWS), ROWS * R::G, kRowSmem * ROWS, s>>>(src, dst, g, srow, tw);
   }
   void x_r2c(const float* src, float2* dst, const Geom& g, long long drow, const float2* tw, cudaStream_t s) override {
+    constexpr int ROWS = Cfg<N>::ROWS;
     const long long pairs = (long long)N * N / 2;
     x_r2c_kernel<R, ROWS><<<(unsigned)(pairs / ROWS), ROWS * R::G, kRowSmem * ROWS, s>>>(src, dst, g, drow, tw);
   }
@@ -299,6 +325,7 @@ struct mhd_problem {
     return launch(KC_YINV, [&] { ops->col_inv(a, g, g.n, nf, tw, stream); });
   }
   int x_fused() {
+    // the six field rows of a physical row are contiguous (slot stride == kxp)
     return launch(KC_XFUSED, [&] { ops->x_fused(rowbuf, g, SLK(), g.kxp, tw, stream); });
   }
   int y_forward(int nf) {
@@ -326,9 +353,18 @@ struct mhd_problem {
     a.ca = ca;
     a.cb = cb;
     a.op = op;
-    const long long blocks = (FS() + 255) / 256;
-    const unsigned grid = (unsigned)(blocks < 152 * 16 ? blocks : 152 * 16);
-    return launch(KC_RKEPI, [&] { rk_epilogue_kernel<<<grid, 256, 0, stream>>>(a, g); });
+    const int bx = g.kx <= 256 ? (g.kx + 31) / 32 * 32 : 256;
+    const dim3 grid((g.kx + bx - 1) / bx, g.k2, g.k2);
+    return launch(KC_RKEPI, [&] {
+      switch (op) {
+        case OP_RHS: rk_epilogue_kernel<OP_RHS><<<grid, bx, 0, stream>>>(a, g); break;
+        case OP_RK4_FIRST: rk_epilogue_kernel<OP_RK4_FIRST><<<grid, bx, 0, stream>>>(a, g); break;
+        case OP_RK4_MID: rk_epilogue_kernel<OP_RK4_MID><<<grid, bx, 0, stream>>>(a, g); break;
+        case OP_RK4_LAST: rk_epilogue_kernel<OP_RK4_LAST><<<grid, bx, 0, stream>>>(a, g); break;
+        case OP_LS_FIRST: rk_epilogue_kernel<OP_LS_FIRST><<<grid, bx, 0, stream>>>(a, g); break;
+        default: rk_epilogue_kernel<OP_LS><<<grid, bx, 0, stream>>>(a, g); break;
+      }
+    });
   }
   int epilogues(const float2* X, int op, float h, float ca, float cb) {
     int rc;
@@ -439,7 +475,7 @@ int mhd_create(const mhd_params* params, mhd_handle* out) {
   h->sz = sizes_of(h->g);
   h->ops.reset(make_ops(params->n));
   if (!h->ops) return fail(MHD_ERR_INVALID, "no plan for n");
-  if ((rc = h->ops->setup())) return rc;
+  if ((rc = h->ops->setup(h->g))) return rc;
   MHD_CUDA(cudaStreamCreateWithFlags(&h->own_stream, cudaStreamNonBlocking));
   h->stream = h->own_stream;
   const Sizes& s = h->sz;

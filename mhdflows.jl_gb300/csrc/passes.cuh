@@ -54,38 +54,92 @@ struct ColArgs {
 };
 
 // ------------------------------------------------------------------------------------------
-// Column pass: one length-n transform per (field, outer index, kx column); TX columns per CTA.
+// Column pass: one length-n transform per (field, outer index, kx column); TX columns per tile.
+// Persistent CTAs walk the tiles; the next tile's rows are fetched with cp.async into a second
+// shared-memory buffer while the current one is transformed, and the buffer that was just read
+// into registers doubles as the exchange space of the transform.
 // PIN: input rows are kept indices (pruned inverse input).  POUT: only kept outputs stored.
 // ------------------------------------------------------------------------------------------
-template <class P, int TX, int DIR, bool PIN, bool POUT>
-__global__ void __launch_bounds__(TX * P::G) col_pass_kernel(ColArgs a, Geom geo, const float2* __restrict__ tw) {
+struct ColWork {
+  int tiles_x;  // kx tiles
+  int outer;    // outer index count
+  int nf;       // fields / slots
+  int rows_in;  // rows staged per tile (K2 for pruned input, n otherwise)
+};
+
+template <int TX>
+__device__ __forceinline__ void col_prefetch(float2* buf, const float2* src, long long sR, int rows, int col0, int kxp) {
+  constexpr int CH = TX / 2;  // 16-byte chunks per row
+  const int nch = rows * CH;
+  for (int c = threadIdx.x; c < nch; c += blockDim.x) {
+    const int row = c / CH, q = c % CH;
+    if (col0 + 2 * q < kxp) cp_async16(buf + row * TX + 2 * q, src + row * sR + col0 + 2 * q);
+  }
+}
+
+template <class P0, int TX, int DIR, bool PIN, bool POUT>
+__global__ void __launch_bounds__(TX * P0::G, TX * P0::G <= 256 ? 2 : 1)
+    col_pass_kernel(ColArgs a, Geom geo, ColWork w, const float2* __restrict__ tw) {
+  using P = Unpadded<P0>;
   extern __shared__ float2 smem[];
-  constexpr int G = P::G, V = P::V;
+  constexpr int G = P::G, V = P::V, N = P::N;
   const int tx = threadIdx.x % TX, g = threadIdx.x / TX;
-  const int kxg = blockIdx.x * TX + tx;
-  const bool colok = kxg < geo.kx;
-  const float2* src = a.src + blockIdx.z * a.sF + (long long)blockIdx.y * a.sO + kxg;
-  float2* dst = a.dst + blockIdx.z * a.dF + (long long)blockIdx.y * a.dO + kxg;
-  float2 v[1][V];
-#pragma unroll
-  for (int d = 0; d < P::DI; ++d)
-#pragma unroll
-    for (int n0 = 0; n0 < P::R0; ++n0) {
-      const int n = g + G * d + P::LI * n0;
-      const int row = PIN ? kept_of_freq(geo, n) : n;
-      float2 x = make_float2(0.f, 0.f);
-      if (colok && row >= 0) x = cscale(__ldg(src + row * a.sR), a.scale);
-      v[0][d * P::R0 + n0] = x;
+  const int total = w.tiles_x * w.outer * w.nf;
+  auto tile_src = [&](int t, int& col0) {
+    const int tx_t = t % w.tiles_x;
+    const int r = t / w.tiles_x;
+    const int o = r % w.outer, f = r / w.outer;
+    col0 = tx_t * TX;
+    return a.src + f * a.sF + (long long)o * a.sO;
+  };
+  int t = blockIdx.x;
+  if (t < total) {
+    int c0;
+    const float2* s0 = tile_src(t, c0);
+    col_prefetch<TX>(smem, s0, a.sR, w.rows_in, c0, geo.kxp);
+  }
+  cp_async_commit();
+  for (int it = 0; t < total; t += gridDim.x, ++it) {
+    float2* cur = smem + (it & 1) * (N * TX);
+    const int tn = t + gridDim.x;
+    if (tn < total) {
+      int c1;
+      const float2* s1 = tile_src(tn, c1);
+      col_prefetch<TX>(smem + ((it + 1) & 1) * (N * TX), s1, a.sR, w.rows_in, c1, geo.kxp);
     }
-  fft_run<P, DIR, 1, 0, TX>(v, smem, tx, g, tw, BlockSync{});
+    cp_async_commit();
+    cp_async_wait<1>();
+    __syncthreads();
+    const int tx_t = t % w.tiles_x;
+    const int r = t / w.tiles_x;
+    const int o = r % w.outer, f = r / w.outer;
+    const int kxg = tx_t * TX + tx;
+    const bool colok = kxg < geo.kx;
+    float2 v[1][V];
 #pragma unroll
-  for (int d = 0; d < P::DF; ++d)
+    for (int d = 0; d < P::DI; ++d)
 #pragma unroll
-    for (int e = 0; e < P::RF; ++e) {
-      const int k = g + G * d + P::LF * e;
-      const int row = POUT ? kept_of_freq(geo, k) : k;
-      if (colok && row >= 0) dst[row * a.dR] = v[0][d * P::RF + e];
-    }
+      for (int n0 = 0; n0 < P::R0; ++n0) {
+        const int n = g + G * d + P::LI * n0;
+        const int row = PIN ? kept_of_freq(geo, n) : n;
+        float2 x = make_float2(0.f, 0.f);
+        if (colok && row >= 0) x = cscale(cur[row * TX + tx], a.scale);
+        v[0][d * P::R0 + n0] = x;
+      }
+    __syncthreads();  // cur is now free: reuse it as the exchange buffer
+    fft_run<P, DIR, 1, 0, TX>(v, cur, tx, g, tw, BlockSync{});
+    float2* dst = a.dst + f * a.dF + (long long)o * a.dO + kxg;
+#pragma unroll
+    for (int d = 0; d < P::DF; ++d)
+#pragma unroll
+      for (int e = 0; e < P::RF; ++e) {
+        const int k = g + G * d + P::LF * e;
+        const int row = POUT ? kept_of_freq(geo, k) : k;
+        if (colok && row >= 0) dst[row * a.dR] = v[0][d * P::RF + e];
+      }
+    __syncthreads();  // all exchange reads of cur done before it is refilled
+  }
+  cp_async_wait<0>();
 }
 
 // ------------------------------------------------------------------------------------------
@@ -133,66 +187,102 @@ template <class P>
 struct RowCfg {
   using PR = typename Reverse<P>::type;
   static constexpr int a = P::SMEM > PR::SMEM ? P::SMEM : PR::SMEM;
-  static constexpr int TS = a > P::N ? a : P::N;  // words per transform buffer
+  static constexpr int b = a > P::N ? a : P::N;
+  static constexpr int TS = (b + 1) / 2 * 2;  // words per transform buffer (even: 16-byte aligned)
 };
 
 // Fused x pass: per physical row (z, y): 3 inverse c2r pairs -> 6 physical fields -> 8 products
 // -> 4 forward r2c pairs -> 8 half-spectrum rows, written back over the same row slots.
 // Products: Dxz = (bx^2-ux^2)-(bz^2-uz^2), Dyz = (by^2-uy^2)-(bz^2-uz^2), Txy, Txz, Tyz with
 // Tij = bi*bj - ui*uj, and Axy, Axz, Ayz with Aij = ui*bj - bi*uj.
-template <class P, int ROWS>
-__global__ void __launch_bounds__(ROWS * P::G) x_fused_kernel(float2* buf, Geom geo, long long rowstride,
-                                                                long long slot, const float2* __restrict__ tw) {
+// A row group is RPG = max(1, 32/G) consecutive rows handled by one warp (G <= 32) or one row
+// handled by G/32 warps.  Groups are persistent: while a group transforms its rows, cp.async
+// brings the six field rows of its next rows into the other half of a double buffer.
+template <class P>
+struct XCfg {
+  static constexpr int G = P::G;
+  static constexpr int RPG = G >= 32 ? 1 : 32 / G;        // rows per group
+  static constexpr int TPG = G >= 32 ? G : 32;            // threads per group
+  static constexpr int TS = RowCfg<P>::TS;                // exchange words per row
+  static __host__ __device__ int stage_words(int kxp) { return RPG * 6 * kxp; }
+  static __host__ __device__ int group_words(int kxp) { return 2 * stage_words(kxp) + RPG * TS; }
+};
+
+template <class P, int GROUPS>
+__global__ void __launch_bounds__(GROUPS * XCfg<P>::TPG, 4) x_fused_kernel(float2* buf, Geom geo, long long rowstride,
+                                                                             long long slot, const float2* __restrict__ tw) {
   using PR = typename Reverse<P>::type;
-  constexpr int G = P::G, V = P::V, N = P::N;
-  constexpr int TS = RowCfg<P>::TS;
+  using XC = XCfg<P>;
+  constexpr int G = P::G, V = P::V, N = P::N, RPG = XC::RPG, TPG = XC::TPG, TS = XC::TS;
   extern __shared__ float2 smem[];
-  const int r = threadIdx.x / G, g = threadIdx.x % G;
-  const long long row = (long long)blockIdx.x * ROWS + r;
-  float2* rowp = buf + row * rowstride;
-  float2* sb = smem + r * 4 * TS;
-  const int kx = geo.kx;
-  const RowSync<G> sync{1 + r};
+  const int kxp = geo.kxp, kx = geo.kx;
+  const int grp = threadIdx.x / TPG;
+  const int gt = threadIdx.x % TPG;          // thread within group
+  const int rr = gt / G, g = gt % G;         // row within group, lane within row
+  const int sw = XC::stage_words(kxp);
+  float2* gs = smem + grp * XC::group_words(kxp);
+  float2* sb = gs + 2 * sw + rr * TS;
+  const RowSync<G> sync{1 + grp};
+  const long long ngroups = (long long)N * N / RPG;
+  const int chunks_row = 3 * kxp;  // 16-byte chunks of the six contiguous field rows (slot == kxp)
 
-  float2 v[3][V];
-#pragma unroll
-  for (int t = 0; t < 3; ++t) load_herm_pair<P>(v[t], rowp + (2 * t) * slot, rowp + (2 * t + 1) * slot, kx, g);
-  fft_run<P, +1, 3, TS, 1>(v, sb, 0, g, tw, sync);
+  // rows q*RPG .. q*RPG+RPG-1 -> dst (each row's six fields contiguous)
+  auto prefetch = [&](long long q, float2* dst) {
+    for (int c = gt; c < RPG * chunks_row; c += TPG) {
+      const int r = RPG == 1 ? 0 : c / chunks_row;
+      const int cc = RPG == 1 ? c : c - r * chunks_row;
+      cp_async16(dst + r * 6 * kxp + 2 * cc, buf + (q * RPG + r) * rowstride + 2 * cc);
+    }
+  };
 
-  float2 w[4][V];
+  long long q = (long long)blockIdx.x * GROUPS + grp;
+  const long long qstep = (long long)gridDim.x * GROUPS;
+  if (q < ngroups) prefetch(q, gs);
+  cp_async_commit();
+  for (int it = 0; q < ngroups; q += qstep, ++it) {
+    const float2* cur = gs + (it & 1) * sw;
+    if (q + qstep < ngroups) prefetch(q + qstep, gs + ((it + 1) & 1) * sw);
+    cp_async_commit();
+    cp_async_wait<1>();
+    sync();
+    const float2* rin = cur + rr * 6 * kxp;
+    float2 v[3][V];
 #pragma unroll
-  for (int i = 0; i < V; ++i) {
-    const float ux = v[0][i].x, uy = v[0][i].y, uz = v[1][i].x;
-    const float bx = v[1][i].y, by = v[2][i].x, bz = v[2][i].y;
-    const float tzz = bz * bz - uz * uz;
-    const float dxz = (bx * bx - ux * ux) - tzz;
-    const float dyz = (by * by - uy * uy) - tzz;
-    const float txy = bx * by - ux * uy;
-    const float txz = bx * bz - ux * uz;
-    const float tyz = by * bz - uy * uz;
-    const float axy = ux * by - bx * uy;
-    const float axz = ux * bz - bx * uz;
-    const float ayz = uy * bz - by * uz;
-    w[0][i] = make_float2(dxz, dyz);
-    w[1][i] = make_float2(txy, txz);
-    w[2][i] = make_float2(tyz, axy);
-    w[3][i] = make_float2(axz, ayz);
+    for (int t = 0; t < 3; ++t) load_herm_pair<P>(v[t], rin + (2 * t) * kxp, rin + (2 * t + 1) * kxp, kx, g);
+#pragma unroll
+    for (int t = 0; t < 3; ++t) {
+      fft_run<P, +1, 1, TS, 1>(reinterpret_cast<float2(&)[1][V]>(v[t]), sb, 0, g, tw, sync);
+      sync();
+    }
+    float2 w[4][V];
+#pragma unroll
+    for (int i = 0; i < V; ++i) {
+      const float ux = v[0][i].x, uy = v[0][i].y, uz = v[1][i].x;
+      const float bx = v[1][i].y, by = v[2][i].x, bz = v[2][i].y;
+      const float tzz = bz * bz - uz * uz;
+      w[0][i] = make_float2((bx * bx - ux * ux) - tzz, (by * by - uy * uy) - tzz);
+      w[1][i] = make_float2(bx * by - ux * uy, bx * bz - ux * uz);
+      w[2][i] = make_float2(by * bz - uy * uz, ux * by - bx * uy);
+      w[3][i] = make_float2(ux * bz - bx * uz, uy * bz - by * uz);
+    }
+    float2* rowp = buf + (q * RPG + rr) * rowstride;
+#pragma unroll
+    for (int t = 0; t < 4; ++t) {
+      fft_run<PR, -1, 1, TS, 1>(reinterpret_cast<float2(&)[1][V]>(w[t]), sb, 0, g, tw, sync);
+      sync();
+#pragma unroll
+      for (int d = 0; d < PR::DF; ++d)
+#pragma unroll
+        for (int e = 0; e < PR::RF; ++e) {
+          const int k = g + G * d + PR::LF * e;
+          if (k < kx || k > N - kx) sb[k] = w[t][d * PR::RF + e];
+        }
+      sync();
+      store_split_pair(sb, N, kx, g, G, rowp + (2 * t) * slot, rowp + (2 * t + 1) * slot);
+      sync();
+    }
   }
-  sync();
-  fft_run<PR, -1, 4, TS, 1>(w, sb, 0, g, tw, sync);
-  sync();
-#pragma unroll
-  for (int t = 0; t < 4; ++t)
-#pragma unroll
-    for (int d = 0; d < PR::DF; ++d)
-#pragma unroll
-      for (int e = 0; e < PR::RF; ++e) {
-        const int k = g + G * d + PR::LF * e;
-        if (k < kx || k > N - kx) sb[t * TS + k] = w[t][d * PR::RF + e];
-      }
-  sync();
-#pragma unroll
-  for (int t = 0; t < 4; ++t) store_split_pair(sb + t * TS, N, kx, g, G, rowp + (2 * t) * slot, rowp + (2 * t + 1) * slot);
+  cp_async_wait<0>();
 }
 
 // Plain c2r of row pairs: spectral rows (2q, 2q+1) -> physical rows, normalisation already applied.
@@ -281,82 +371,76 @@ struct RkArgs {
   int op;
 };
 
-__device__ __forceinline__ float2 rk_apply(int op, const RkArgs& a, long long o, float2 x, float2 R) {
-  switch (op) {
-    case OP_RHS: a.acc[o] = R; break;
-    case OP_RK4_FIRST:
-      a.acc[o] = make_float2(R.x / 6.f, R.y / 6.f);
-      a.xn[o] = make_float2(x.x + a.h * R.x, x.y + a.h * R.y);
-      break;
-    case OP_RK4_MID: {
-      const float2 s = a.sol[o], q = a.acc[o];
-      a.acc[o] = make_float2(q.x + R.x / 3.f, q.y + R.y / 3.f);
-      a.xn[o] = make_float2(s.x + a.h * R.x, s.y + a.h * R.y);
-    } break;
-    case OP_RK4_LAST: {
-      const float2 s = a.sol[o], q = a.acc[o];
-      const float2 tot = make_float2(q.x + R.x / 6.f, q.y + R.y / 6.f);
-      a.sol[o] = make_float2(s.x + a.dt * tot.x, s.y + a.dt * tot.y);
-    } break;
-    case OP_LS_FIRST: {
-      const float2 du = make_float2(a.dt * R.x, a.dt * R.y);
-      a.acc[o] = du;
-      a.xn[o] = make_float2(x.x + a.cb * du.x, x.y + a.cb * du.y);
-    } break;
-    case OP_LS: {
-      const float2 q = a.acc[o];
-      const float2 du = make_float2(a.ca * q.x + a.dt * R.x, a.ca * q.y + a.dt * R.y);
-      a.acc[o] = du;
-      a.xn[o] = make_float2(x.x + a.cb * du.x, x.y + a.cb * du.y);
-    } break;
-    default: break;
+template <int OP>
+__device__ __forceinline__ void rk_apply(const RkArgs& a, long long o, float2 x, float2 R) {
+  if constexpr (OP == OP_RHS) {
+    a.acc[o] = R;
+  } else if constexpr (OP == OP_RK4_FIRST) {
+    a.acc[o] = make_float2(R.x / 6.f, R.y / 6.f);
+    a.xn[o] = make_float2(x.x + a.h * R.x, x.y + a.h * R.y);
+  } else if constexpr (OP == OP_RK4_MID) {
+    const float2 s = a.sol[o], q = a.acc[o];
+    a.acc[o] = make_float2(q.x + R.x / 3.f, q.y + R.y / 3.f);
+    a.xn[o] = make_float2(s.x + a.h * R.x, s.y + a.h * R.y);
+  } else if constexpr (OP == OP_RK4_LAST) {
+    const float2 s = a.sol[o], q = a.acc[o];
+    const float2 tot = make_float2(q.x + R.x / 6.f, q.y + R.y / 6.f);
+    a.sol[o] = make_float2(s.x + a.dt * tot.x, s.y + a.dt * tot.y);
+  } else if constexpr (OP == OP_LS_FIRST) {
+    const float2 du = make_float2(a.dt * R.x, a.dt * R.y);
+    a.acc[o] = du;
+    a.xn[o] = make_float2(x.x + a.cb * du.x, x.y + a.cb * du.y);
+  } else if constexpr (OP == OP_LS) {
+    const float2 q = a.acc[o];
+    const float2 du = make_float2(a.ca * q.x + a.dt * R.x, a.ca * q.y + a.dt * R.y);
+    a.acc[o] = du;
+    a.xn[o] = make_float2(x.x + a.cb * du.x, x.y + a.cb * du.y);
   }
-  return R;
 }
 
+// grid (ceil(kx / blockDim.x), k2, k2): one thread per retained mode, no index division.
+template <int OP>
 __global__ void __launch_bounds__(256) rk_epilogue_kernel(RkArgs a, Geom geo) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  if (x >= geo.kx) return;
+  const int jy = blockIdx.y, jz = blockIdx.z;
   const long long fs = a.fs;
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < fs; i += (long long)gridDim.x * blockDim.x) {
-    const int x = (int)(i % geo.kxp);
-    if (x >= geo.kx) continue;
-    long long r = i / geo.kxp;
-    const int jy = (int)(r % geo.k2);
-    const int jz = (int)(r / geo.k2);
-    const float kxv = geo.kscale * (float)x;
-    const float kyv = geo.kscale * (float)signed_of_kept(geo, jy);
-    const float kzv = geo.kscale * (float)signed_of_kept(geo, jz);
-    const float k2 = kxv * kxv + kyv * kyv + kzv * kzv;
-    float2 p[8];
+  const long long i = ((long long)jz * geo.k2 + jy) * geo.kxp + x;
+  const float kxv = geo.kscale * (float)x;
+  const float kyv = geo.kscale * (float)signed_of_kept(geo, jy);
+  const float kzv = geo.kscale * (float)signed_of_kept(geo, jz);
+  const float k2 = kxv * kxv + kyv * kyv + kzv * kzv;
+  float2 p[8];
 #pragma unroll
-    for (int q = 0; q < 8; ++q) p[q] = __ldg(a.prod + q * fs + i);
-    const float2 dxz = p[0], dyz = p[1], txy = p[2], txz = p[3], tyz = p[4];
-    const float2 axy = p[5], axz = p[6], ayz = p[7];
-    float2 Vx, Vy, Vz;
-    Vx.x = kxv * dxz.x + kyv * txy.x + kzv * txz.x;  Vx.y = kxv * dxz.y + kyv * txy.y + kzv * txz.y;
-    Vy.x = kxv * txy.x + kyv * dyz.x + kzv * tyz.x;  Vy.y = kxv * txy.y + kyv * dyz.y + kzv * tyz.y;
-    Vz.x = kxv * txz.x + kyv * tyz.x;                Vz.y = kxv * txz.y + kyv * tyz.y;
-    const float ik2 = k2 > 0.f ? 1.0f / k2 : 0.f;
-    const float kvx = (kxv * Vx.x + kyv * Vy.x + kzv * Vz.x) * ik2;
-    const float kvy = (kxv * Vx.y + kyv * Vy.y + kzv * Vz.y) * ik2;
-    float2 nl[6];
-    nl[0] = make_float2(-(Vx.y - kxv * kvy), Vx.x - kxv * kvx);
-    nl[1] = make_float2(-(Vy.y - kyv * kvy), Vy.x - kyv * kvx);
-    nl[2] = make_float2(-(Vz.y - kzv * kvy), Vz.x - kzv * kvx);
-    // W = i k x E with E = (Ayz, -Axz, Axy): Wx = i(ky Axy + kz Axz), Wy = i(kz Ayz - kx Axy), Wz = -i(kx Axz + ky Ayz)
-    const float2 wx = make_float2(kyv * axy.x + kzv * axz.x, kyv * axy.y + kzv * axz.y);
-    const float2 wy = make_float2(kzv * ayz.x - kxv * axy.x, kzv * ayz.y - kxv * axy.y);
-    const float2 wz = make_float2(-(kxv * axz.x + kyv * ayz.x), -(kxv * axz.y + kyv * ayz.y));
-    nl[3] = make_float2(-wx.y, wx.x);
-    nl[4] = make_float2(-wy.y, wy.x);
-    nl[5] = make_float2(-wz.y, wz.x);
-    const float du = -a.nu * k2, db = -a.eta * k2;
+  for (int q = 0; q < 8; ++q) p[q] = __ldcs(a.prod + q * fs + i);
+  float2 xv[6];
 #pragma unroll
-    for (int c = 0; c < 6; ++c) {
-      const long long o = c * fs + i;
-      const float2 xv = a.X[o];
-      const float dk = c < 3 ? du : db;
-      rk_apply(a.op, a, o, xv, make_float2(nl[c].x + dk * xv.x, nl[c].y + dk * xv.y));
-    }
+  for (int c = 0; c < 6; ++c) xv[c] = a.X[c * fs + i];
+  const float2 dxz = p[0], dyz = p[1], txy = p[2], txz = p[3], tyz = p[4];
+  const float2 axy = p[5], axz = p[6], ayz = p[7];
+  float2 Vx, Vy, Vz;
+  Vx.x = kxv * dxz.x + kyv * txy.x + kzv * txz.x;  Vx.y = kxv * dxz.y + kyv * txy.y + kzv * txz.y;
+  Vy.x = kxv * txy.x + kyv * dyz.x + kzv * tyz.x;  Vy.y = kxv * txy.y + kyv * dyz.y + kzv * tyz.y;
+  Vz.x = kxv * txz.x + kyv * tyz.x;                Vz.y = kxv * txz.y + kyv * tyz.y;
+  const float ik2 = k2 > 0.f ? 1.0f / k2 : 0.f;
+  const float kvx = (kxv * Vx.x + kyv * Vy.x + kzv * Vz.x) * ik2;
+  const float kvy = (kxv * Vx.y + kyv * Vy.y + kzv * Vz.y) * ik2;
+  float2 nl[6];
+  nl[0] = make_float2(-(Vx.y - kxv * kvy), Vx.x - kxv * kvx);
+  nl[1] = make_float2(-(Vy.y - kyv * kvy), Vy.x - kyv * kvx);
+  nl[2] = make_float2(-(Vz.y - kzv * kvy), Vz.x - kzv * kvx);
+  // W = i k x E with E = (Ayz, -Axz, Axy): Wx = i(ky Axy + kz Axz), Wy = i(kz Ayz - kx Axy), Wz = -i(kx Axz + ky Ayz)
+  const float2 wx = make_float2(kyv * axy.x + kzv * axz.x, kyv * axy.y + kzv * axz.y);
+  const float2 wy = make_float2(kzv * ayz.x - kxv * axy.x, kzv * ayz.y - kxv * axy.y);
+  const float2 wz = make_float2(-(kxv * axz.x + kyv * ayz.x), -(kxv * axz.y + kyv * ayz.y));
+  nl[3] = make_float2(-wx.y, wx.x);
+  nl[4] = make_float2(-wy.y, wy.x);
+  nl[5] = make_float2(-wz.y, wz.x);
+  const float du = -a.nu * k2, db = -a.eta * k2;
+#pragma unroll
+  for (int c = 0; c < 6; ++c) {
+    const float dk = c < 3 ? du : db;
+    rk_apply<OP>(a, c * fs + i, xv[c], make_float2(nl[c].x + dk * xv[c].x, nl[c].y + dk * xv[c].y));
   }
 }
 
