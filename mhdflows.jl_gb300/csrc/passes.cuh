@@ -145,7 +145,8 @@ __global__ void __launch_bounds__(TX * P0::G, TX * P0::G <= 256 ? 2 : 1)
 // ------------------------------------------------------------------------------------------
 // x rows: Hermitian two-for-one helpers.
 // ------------------------------------------------------------------------------------------
-// Input of an inverse (c2r) transform of two half-spectrum rows f1, f2 with kx kept modes:
+// Input of an inverse (c2r) transform of two half-spectrum rows f1, f2 with kx kept modes
+// (plain loads: the rows may live in global or in shared memory):
 // z[n] = F1[n] + i F2[n] with F[n-n] = conj(F[n]); the kx = 0 imaginary parts are dropped,
 // which is what a c2r transform does with a non-Hermitian kx = 0 plane.
 template <class P>
@@ -158,12 +159,12 @@ __device__ __forceinline__ void load_herm_pair(float2 (&v)[P::V], const float2* 
       const int n = g + P::G * d + P::LI * n0;
       float2 z = make_float2(0.f, 0.f);
       if (n < kx) {
-        float2 a = __ldg(f1 + n), b = __ldg(f2 + n);
+        float2 a = f1[n], b = f2[n];
         if (n == 0) { a.y = 0.f; b.y = 0.f; }
         z = make_float2(a.x - b.y, a.y + b.x);
       } else if (n > P::N - kx) {
         const int m = P::N - n;
-        float2 a = __ldg(f1 + m), b = __ldg(f2 + m);
+        float2 a = f1[m], b = f2[m];
         z = make_float2(a.x + b.y, b.x - a.y);
       }
       v[d * P::R0 + n0] = z;
