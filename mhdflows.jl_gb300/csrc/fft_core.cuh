@@ -263,15 +263,26 @@ __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commi
 template <int NPEND>
 __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(NPEND) : "memory"); }
 
+// Stage twiddles of a plan, laid out in the order the lanes of a warp read them, so one warp
+// load touches one or two 128-byte lines:
+//   tw[n1*R0 + k0]                    = W_N^{(n1 k0 mod R0R1) R2}       (before stage 2)
+//   tw[R0R1 + k1*R0R2 + k0 + R0*n2]   = W_N^{n2 (k0 + R0 k1) mod N}     (before stage 3)
+// with W_N^j = cos(2 pi j/N) + i sin(2 pi j/N); the transform direction conjugates on use.
+template <class P>
+struct PlanTw {
+  static constexpr int T2 = P::R0 * P::R1;
+  static constexpr int SIZE = T2 + (P::R2 > 1 ? P::N : 0);
+};
+
 // Executes stages of plan P on NT independent transforms held as v[t][V] by this thread.
 // Shared memory word address of logical element a for transform t is  buf[t*TS + a*STR + OFF].
-// SYNC() must be a barrier over every thread that shares buf.
+// SYNC() must be a barrier over every thread that shares buf.  tw is the plan's PlanTw table.
 // Input: v[t][d*R0 + n0] = x[l1 + LI*n0] with l1 = g + G*d.
 // Output: v[t][d*RF + e] = X[lF + LF*e] with lF = g + G*d.
 template <class P, int DIR, int NT, int TS, int STR, class SyncF>
 __device__ __forceinline__ void fft_run(float2 (&v)[NT][P::V], float2* buf, int off, int g,
                                         const float2* __restrict__ tw, SyncF SYNC) {
-  constexpr int V = P::V, G = P::G, R0 = P::R0, R1 = P::R1, R2 = P::R2, N = P::N;
+  constexpr int V = P::V, G = P::G, R0 = P::R0, R1 = P::R1, R2 = P::R2;
   // ---- stage 1: DFT-R0 over n0
 #pragma unroll
   for (int t = 0; t < NT; ++t) dft_groups<R0, DIR>(v[t]);
@@ -295,9 +306,8 @@ __device__ __forceinline__ void fft_run(float2 (&v)[NT][P::V], float2* buf, int 
 #pragma unroll
       for (int n1 = 0; n1 < R1; ++n1) {
         float2 a = buf[t * TS + (k0 * P::E1S + n1 * R2 + n2) * STR + off];
-        const int e = ((n1 * k0) % (R0 * R1)) * R2;  // W_{R0R1}^{n1 k0} = W_N^{n1 k0 R2}
-        if (n1 != 0 && k0 != 0) {
-          float2 w = ldtw(tw, e);
+        if (n1 != 0) {  // W_{R0R1}^{n1 k0}
+          const float2 w = ldtw(tw, n1 * R0 + k0);
           a = cmul_cs<DIR>(a, w.x, w.y);
         }
         v[t][d * R1 + n1] = a;
@@ -319,10 +329,8 @@ __device__ __forceinline__ void fft_run(float2 (&v)[NT][P::V], float2* buf, int 
         for (int k1 = 0; k1 < R1; ++k1) {
           float2 a = v[t][d * R1 + k1];
           const int l3 = k0 + R0 * k1;
-          if (n2 != 0 && l3 != 0) {
-            float2 w = ldtw(tw, (n2 * l3) % N);
-            a = cmul_cs<DIR>(a, w.x, w.y);
-          }
+          const float2 w = ldtw(tw, PlanTw<P>::T2 + k1 * (R0 * R2) + l2);  // W_N^{n2 l3}
+          a = cmul_cs<DIR>(a, w.x, w.y);
           buf[t * TS + (n2 * P::E2S + l3) * STR + off] = a;
         }
       }

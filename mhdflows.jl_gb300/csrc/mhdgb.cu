@@ -61,12 +61,29 @@ constexpr int kSlots = 8;
 struct OpsBase {
   virtual ~OpsBase() {}
   virtual int setup(const Geom& g) = 0;
-  virtual void col_inv(const ColArgs& a, const Geom& g, int outer, int nf, const float2* tw, cudaStream_t s) = 0;
-  virtual void col_fwd(const ColArgs& a, const Geom& g, int outer, int nf, const float2* tw, cudaStream_t s) = 0;
-  virtual void x_fused(float2* buf, const Geom& g, long long rowstride, long long slot, const float2* tw, cudaStream_t s) = 0;
-  virtual void x_c2r(const float2* src, float* dst, const Geom& g, long long srow, const float2* tw, cudaStream_t s) = 0;
-  virtual void x_r2c(const float* src, float2* dst, const Geom& g, long long drow, const float2* tw, cudaStream_t s) = 0;
+  virtual void col_inv(const ColArgs& a, const Geom& g, int outer, int nf, cudaStream_t s) = 0;
+  virtual void col_fwd(const ColArgs& a, const Geom& g, int outer, int nf, cudaStream_t s) = 0;
+  virtual void x_fused(float2* buf, const Geom& g, long long rowstride, long long slot, cudaStream_t s) = 0;
+  virtual void x_c2r(const float2* src, float* dst, const Geom& g, long long srow, cudaStream_t s) = 0;
+  virtual void x_r2c(const float* src, float2* dst, const Geom& g, long long drow, cudaStream_t s) = 0;
 };
+
+// Host construction of a plan's stage-twiddle table (PlanTw layout), in double precision.
+template <class P>
+void plan_twiddles(std::vector<float2>& out) {
+  constexpr int N = P::N, R0 = P::R0, R1 = P::R1, R2 = P::R2;
+  out.assign(PlanTw<P>::SIZE, make_float2(1.f, 0.f));
+  auto w = [](long long j) {
+    const double ang = 2.0 * M_PI * (double)(j % N) / (double)N;
+    return make_float2((float)std::cos(ang), (float)std::sin(ang));
+  };
+  for (int n1 = 0; n1 < R1; ++n1)
+    for (int k0 = 0; k0 < R0; ++k0) out[n1 * R0 + k0] = w((long long)((n1 * k0) % (R0 * R1)) * R2);
+  if (R2 > 1)
+    for (int k1 = 0; k1 < R1; ++k1)
+      for (int n2 = 0; n2 < R2; ++n2)
+        for (int k0 = 0; k0 < R0; ++k0) out[R0 * R1 + k1 * (R0 * R2) + k0 + R0 * n2] = w((long long)n2 * (k0 + R0 * k1));
+}
 
 template <class K>
 int set_smem(K kernel, size_t bytes) {
@@ -93,6 +110,7 @@ template <int N>
 struct Ops : OpsBase {
   using C = typename Cfg<N>::C;
   using R = typename Cfg<N>::R;
+  using RR = typename Reverse<R>::type;
   using XC = XCfg<R>;
   static constexpr int TX = Cfg<N>::TX;
   static constexpr int GROUPS = XC::TPG >= 64 ? 2 : 4;  // x row groups per CTA (128 threads)
@@ -100,9 +118,27 @@ struct Ops : OpsBase {
   static constexpr size_t kRowSmem = sizeof(float2) * RowCfg<R>::TS;
   size_t x_smem = 0;
   int col_inv_ctas = 0, col_fwd_ctas = 0, x_ctas = 0;
+  float2* tw_all = nullptr;
+  const float2 *twC = nullptr, *twR = nullptr, *twRR = nullptr;
+
+  ~Ops() override {
+    if (tw_all) cudaFree(tw_all);
+  }
 
   int setup(const Geom& g) override {
     int rc = MHD_OK;
+    std::vector<float2> tc, tr, trr;
+    plan_twiddles<C>(tc);
+    plan_twiddles<R>(tr);
+    plan_twiddles<RR>(trr);
+    std::vector<float2> all(tc);
+    all.insert(all.end(), tr.begin(), tr.end());
+    all.insert(all.end(), trr.begin(), trr.end());
+    MHD_CUDA(cudaMalloc(&tw_all, all.size() * sizeof(float2)));
+    MHD_CUDA(cudaMemcpy(tw_all, all.data(), all.size() * sizeof(float2), cudaMemcpyHostToDevice));
+    twC = tw_all;
+    twR = tw_all + tc.size();
+    twRR = twR + tr.size();
     x_smem = sizeof(float2) * (size_t)GROUPS * XC::group_words(g.kxp);
     if ((rc = set_smem(col_pass_kernel<C, TX, +1, true, false>, kColSmem))) return rc;
     if ((rc = set_smem(col_pass_kernel<C, TX, -1, false, true>, kColSmem))) return rc;
@@ -114,31 +150,31 @@ struct Ops : OpsBase {
     if ((rc = resident_ctas(x_fused_kernel<R, GROUPS>, GROUPS * XC::TPG, x_smem, &x_ctas))) return rc;
     return MHD_OK;
   }
-  void col_inv(const ColArgs& a, const Geom& g, int outer, int nf, const float2* tw, cudaStream_t s) override {
+  void col_inv(const ColArgs& a, const Geom& g, int outer, int nf, cudaStream_t s) override {
     ColWork w{(g.kx + TX - 1) / TX, outer, nf, g.k2};
     const int total = w.tiles_x * w.outer * w.nf;
-    col_pass_kernel<C, TX, +1, true, false><<<total < col_inv_ctas ? total : col_inv_ctas, TX * C::G, kColSmem, s>>>(a, g, w, tw);
+    col_pass_kernel<C, TX, +1, true, false><<<total < col_inv_ctas ? total : col_inv_ctas, TX * C::G, kColSmem, s>>>(a, g, w, twC);
   }
-  void col_fwd(const ColArgs& a, const Geom& g, int outer, int nf, const float2* tw, cudaStream_t s) override {
+  void col_fwd(const ColArgs& a, const Geom& g, int outer, int nf, cudaStream_t s) override {
     ColWork w{(g.kx + TX - 1) / TX, outer, nf, N};
     const int total = w.tiles_x * w.outer * w.nf;
-    col_pass_kernel<C, TX, -1, false, true><<<total < col_fwd_ctas ? total : col_fwd_ctas, TX * C::G, kColSmem, s>>>(a, g, w, tw);
+    col_pass_kernel<C, TX, -1, false, true><<<total < col_fwd_ctas ? total : col_fwd_ctas, TX * C::G, kColSmem, s>>>(a, g, w, twC);
   }
-  void x_fused(float2* buf, const Geom& g, long long rowstride, long long slot, const float2* tw, cudaStream_t s) override {
+  void x_fused(float2* buf, const Geom& g, long long rowstride, long long slot, cudaStream_t s) override {
     const long long groups = (long long)N * N / XC::RPG;
     const long long need = (groups + GROUPS - 1) / GROUPS;
     const int grid = (int)(need < x_ctas ? need : x_ctas);
-    x_fused_kernel<R, GROUPS><<<grid, GROUPS * XC::TPG, x_smem, s>>>(buf, g, rowstride, slot, tw);
+    x_fused_kernel<R, GROUPS><<<grid, GROUPS * XC::TPG, x_smem, s>>>(buf, g, rowstride, slot, twR, twRR);
   }
-  void x_c2r(const float2* src, float* dst, const Geom& g, long long srow, const float2* tw, cudaStream_t s) override {
+  void x_c2r(const float2* src, float* dst, const Geom& g, long long srow, cudaStream_t s) override {
     constexpr int ROWS = Cfg<N>::ROWS;
     const long long pairs = (long long)N * N / 2;
-    x_c2r_kernel<R, ROWS><<<(unsigned)(pairs / ROWS), ROWS * R::G, kRowSmem * ROWS, s>>>(src, dst, g, srow, tw);
+    x_c2r_kernel<R, ROWS><<<(unsigned)(pairs / ROWS), ROWS * R::G, kRowSmem * ROWS, s>>>(src, dst, g, srow, twR);
   }
-  void x_r2c(const float* src, float2* dst, const Geom& g, long long drow, const float2* tw, cudaStream_t s) override {
+  void x_r2c(const float* src, float2* dst, const Geom& g, long long drow, cudaStream_t s) override {
     constexpr int ROWS = Cfg<N>::ROWS;
     const long long pairs = (long long)N * N / 2;
-    x_r2c_kernel<R, ROWS><<<(unsigned)(pairs / ROWS), ROWS * R::G, kRowSmem * ROWS, s>>>(src, dst, g, drow, tw);
+    x_r2c_kernel<R, ROWS><<<(unsigned)(pairs / ROWS), ROWS * R::G, kRowSmem * ROWS, s>>>(src, dst, g, drow, twR);
   }
 };
 
@@ -221,7 +257,7 @@ long long footprint(const Geom& g) {
   bytes += s.colbuf * 8 + s.rowbuf * 8;
   bytes += s.ref * 8;                // reference-layout staging
   bytes += s.phys * 4;               // physical staging
-  bytes += (long long)g.n * 8;       // twiddles
+  bytes += 6LL * g.n * 8;            // stage twiddle tables
   bytes += (long long)s.diag_blocks * kDiagSlots * 8 + 16 * 8 + 64;
   return bytes;
 }
@@ -244,7 +280,6 @@ struct mhd_problem {
   float2* rowbuf = nullptr;
   float2* ref = nullptr;
   float* phys = nullptr;
-  float2* tw = nullptr;
   double* diag_partial = nullptr;
   double* diag_out = nullptr;
   unsigned int* maxabs = nullptr;
@@ -266,9 +301,9 @@ struct mhd_problem {
     recs.clear();
     for (auto e : pool) cudaEventDestroy(e);
     pool.clear();
-    void* ptrs[] = {sol, xs, acc, aux, colbuf, rowbuf, ref, phys, tw, diag_partial, diag_out, maxabs};
+    void* ptrs[] = {sol, xs, acc, aux, colbuf, rowbuf, ref, phys, diag_partial, diag_out, maxabs};
     for (void* q : ptrs) if (q) cudaFree(q);
-    sol = xs = acc = aux = colbuf = rowbuf = ref = tw = nullptr;
+    sol = xs = acc = aux = colbuf = rowbuf = ref = nullptr;
     phys = nullptr; diag_partial = nullptr; diag_out = nullptr; maxabs = nullptr;
     if (own_stream) cudaStreamDestroy(own_stream);
     own_stream = nullptr;
@@ -318,24 +353,24 @@ struct mhd_problem {
   int z_inverse(const float2* src, int nf) {
     ColArgs a{src, colbuf, FS(), (long long)g.kxp, (long long)g.k2 * g.kxp, (long long)g.kxp, SLK(), AZ(),
               (float)(1.0 / ((double)g.n * g.n * g.n))};
-    return launch(KC_ZINV, [&] { ops->col_inv(a, g, g.k2, nf, tw, stream); });
+    return launch(KC_ZINV, [&] { ops->col_inv(a, g, g.k2, nf, stream); });
   }
   int y_inverse(int nf) {
     ColArgs a{colbuf, rowbuf, (long long)g.kxp, AZ(), SLK(), (long long)g.kxp, BZ(), SLK(), 1.0f};
-    return launch(KC_YINV, [&] { ops->col_inv(a, g, g.n, nf, tw, stream); });
+    return launch(KC_YINV, [&] { ops->col_inv(a, g, g.n, nf, stream); });
   }
   int x_fused() {
     // the six field rows of a physical row are contiguous (slot stride == kxp)
-    return launch(KC_XFUSED, [&] { ops->x_fused(rowbuf, g, SLK(), g.kxp, tw, stream); });
+    return launch(KC_XFUSED, [&] { ops->x_fused(rowbuf, g, SLK(), g.kxp, stream); });
   }
   int y_forward(int nf) {
     ColArgs a{rowbuf, colbuf, (long long)g.kxp, BZ(), SLK(), (long long)g.kxp, AZ(), SLK(), 1.0f};
-    return launch(KC_YFWD, [&] { ops->col_fwd(a, g, g.n, nf, tw, stream); });
+    return launch(KC_YFWD, [&] { ops->col_fwd(a, g, g.n, nf, stream); });
   }
   // colbuf slots -> compact planes (nf fields/products) of dst, pruned output
   int z_forward(float2* dst, int nf) {
     ColArgs a{colbuf, dst, (long long)g.kxp, SLK(), AZ(), FS(), (long long)g.kxp, (long long)g.k2 * g.kxp, 1.0f};
-    return launch(KC_ZFWD, [&] { ops->col_fwd(a, g, g.k2, nf, tw, stream); });
+    return launch(KC_ZFWD, [&] { ops->col_fwd(a, g, g.k2, nf, stream); });
   }
   // Stage epilogue: RHS from the 8 compact product planes (in rowbuf) and the stage state X.
   int epilogue(const float2* X, int op, float h, float ca, float cb) {
@@ -406,12 +441,12 @@ struct mhd_problem {
     int rc;
     if ((rc = z_inverse(src, 1))) return rc;
     if ((rc = y_inverse(1))) return rc;
-    return launch(KC_OTHER, [&] { ops->x_c2r(rowbuf, phys, g, SLK(), tw, stream); });
+    return launch(KC_OTHER, [&] { ops->x_c2r(rowbuf, phys, g, SLK(), stream); });
   }
   // One field: physical staging -> compact dst (unnormalised forward).
   int forward_field(float2* dst) {
     int rc;
-    if ((rc = launch(KC_OTHER, [&] { ops->x_r2c(phys, rowbuf, g, SLK(), tw, stream); }))) return rc;
+    if ((rc = launch(KC_OTHER, [&] { ops->x_r2c(phys, rowbuf, g, SLK(), stream); }))) return rc;
     if ((rc = y_forward(1))) return rc;
     return z_forward(dst, 1);
   }
@@ -487,20 +522,12 @@ int mhd_create(const mhd_params* params, mhd_handle* out) {
   MHD_CUDA(cudaMalloc(&h->rowbuf, s.rowbuf * sizeof(float2)));
   MHD_CUDA(cudaMalloc(&h->ref, s.ref * sizeof(float2)));
   MHD_CUDA(cudaMalloc(&h->phys, s.phys * sizeof(float)));
-  MHD_CUDA(cudaMalloc(&h->tw, (size_t)h->g.n * sizeof(float2)));
   MHD_CUDA(cudaMalloc(&h->diag_partial, (size_t)s.diag_blocks * kDiagSlots * sizeof(double)));
   MHD_CUDA(cudaMalloc(&h->diag_out, 16 * sizeof(double)));
   MHD_CUDA(cudaMalloc(&h->maxabs, 16 * sizeof(unsigned int)));
   MHD_CUDA(cudaMemsetAsync(h->sol, 0, s.state * sizeof(float2), h->stream));
   MHD_CUDA(cudaMemsetAsync(h->xs, 0, s.state * sizeof(float2), h->stream));
   MHD_CUDA(cudaMemsetAsync(h->acc, 0, s.state * sizeof(float2), h->stream));
-  // twiddles W_n^j = cos(2 pi j/n) + i sin(2 pi j/n), computed in double on the host
-  std::vector<float2> tw(h->g.n);
-  for (int j = 0; j < h->g.n; ++j) {
-    const double ang = 2.0 * M_PI * (double)j / (double)h->g.n;
-    tw[j] = make_float2((float)std::cos(ang), (float)std::sin(ang));
-  }
-  MHD_CUDA(cudaMemcpyAsync(h->tw, tw.data(), tw.size() * sizeof(float2), cudaMemcpyHostToDevice, h->stream));
   MHD_CUDA(cudaStreamSynchronize(h->stream));
   *out = h.release();
   return MHD_OK;

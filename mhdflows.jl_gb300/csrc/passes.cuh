@@ -211,7 +211,8 @@ struct XCfg {
 
 template <class P, int GROUPS>
 __global__ void __launch_bounds__(GROUPS * XCfg<P>::TPG, 4) x_fused_kernel(float2* buf, Geom geo, long long rowstride,
-                                                                             long long slot, const float2* __restrict__ tw) {
+                                                                             long long slot, const float2* __restrict__ tw,
+                                                                             const float2* __restrict__ twr) {
   using PR = typename Reverse<P>::type;
   using XC = XCfg<P>;
   constexpr int G = P::G, V = P::V, N = P::N, RPG = XC::RPG, TPG = XC::TPG, TS = XC::TS;
@@ -269,7 +270,7 @@ __global__ void __launch_bounds__(GROUPS * XCfg<P>::TPG, 4) x_fused_kernel(float
     float2* rowp = buf + (q * RPG + rr) * rowstride;
 #pragma unroll
     for (int t = 0; t < 4; ++t) {
-      fft_run<PR, -1, 1, TS, 1>(reinterpret_cast<float2(&)[1][V]>(w[t]), sb, 0, g, tw, sync);
+      fft_run<PR, -1, 1, TS, 1>(reinterpret_cast<float2(&)[1][V]>(w[t]), sb, 0, g, twr, sync);
       sync();
 #pragma unroll
       for (int d = 0; d < PR::DF; ++d)
