@@ -166,11 +166,20 @@ struct Dft {
 #pragma unroll
       for (int a = 0; a < P; ++a) t[a] = x[O + S * (Q * a + b)];
       Dft<P, DIR>::template run<1, 0>(t);
-      // twiddle W_R^{b*ka}
+      // twiddle W_R^{b*ka}; multiples of a quarter turn are exact sign/swap operations
 #pragma unroll
       for (int ka = 0; ka < P; ++ka) {
         const int e = (b * ka) % R;
-        if (e != 0) t[ka] = cmul_cs<DIR>(t[ka], tw.c[e], tw.s[e]);
+        if (e != 0) {
+          if ((4 * e) % R == 0) {
+            const int q = (4 * e) / R;  // W = (DIR i)^q
+            if (q == 2) t[ka] = make_float2(-t[ka].x, -t[ka].y);
+            else if (q == 1) t[ka] = cmul_diri<DIR>(t[ka]);
+            else t[ka] = cmul_diri<-DIR>(t[ka]);
+          } else {
+            t[ka] = cmul_cs<DIR>(t[ka], tw.c[e], tw.s[e]);
+          }
+        }
         x[O + S * (Q * ka + b)] = t[ka];
       }
     }

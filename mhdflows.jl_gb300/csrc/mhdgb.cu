@@ -1,7 +1,8 @@
 // Host orchestration and C ABI of the GB300-native MHD RK4 / LSRK4 step.
 //
 // One right-hand-side evaluation (MHDcalcN!, src/pgen.jl:153-162 of MHDFlows.jl) is six kernels:
-//   z_inverse  (state -> colbuf, 6 fields, pruned input, 1/n^3 scaling)
+//   z_inverse  (state -> colbuf, 6 fields, pruned input; no normalisation anywhere in the passes,
+//              the 1/n^6 of the two transforms is applied to the products in the epilogue)
 //   y_inverse  (colbuf -> rowbuf, 6 fields, pruned input)
 //   x_fused    (rowbuf -> rowbuf: c2r, 8 quadratic products, r2c; physical fields never leave chip)
 //   y_forward  (rowbuf -> colbuf, 8 products, pruned output)
@@ -64,7 +65,7 @@ struct OpsBase {
   virtual void col_inv(const ColArgs& a, const Geom& g, int outer, int nf, cudaStream_t s) = 0;
   virtual void col_fwd(const ColArgs& a, const Geom& g, int outer, int nf, cudaStream_t s) = 0;
   virtual void x_fused(float2* buf, const Geom& g, long long rowstride, long long slot, cudaStream_t s) = 0;
-  virtual void x_c2r(const float2* src, float* dst, const Geom& g, long long srow, cudaStream_t s) = 0;
+  virtual void x_c2r(const float2* src, float* dst, const Geom& g, long long srow, float scale, cudaStream_t s) = 0;
   virtual void x_r2c(const float* src, float2* dst, const Geom& g, long long drow, cudaStream_t s) = 0;
 };
 
@@ -166,10 +167,10 @@ struct Ops : OpsBase {
     const int grid = (int)(need < x_ctas ? need : x_ctas);
     x_fused_kernel<R, GROUPS><<<grid, GROUPS * XC::TPG, x_smem, s>>>(buf, g, rowstride, slot, twR, twRR);
   }
-  void x_c2r(const float2* src, float* dst, const Geom& g, long long srow, cudaStream_t s) override {
+  void x_c2r(const float2* src, float* dst, const Geom& g, long long srow, float scale, cudaStream_t s) override {
     constexpr int ROWS = Cfg<N>::ROWS;
     const long long pairs = (long long)N * N / 2;
-    x_c2r_kernel<R, ROWS><<<(unsigned)(pairs / ROWS), ROWS * R::G, kRowSmem * ROWS, s>>>(src, dst, g, srow, twR);
+    x_c2r_kernel<R, ROWS><<<(unsigned)(pairs / ROWS), ROWS * R::G, kRowSmem * ROWS, s>>>(src, dst, g, srow, scale, twR);
   }
   void x_r2c(const float* src, float2* dst, const Geom& g, long long drow, cudaStream_t s) override {
     constexpr int ROWS = Cfg<N>::ROWS;
@@ -351,12 +352,11 @@ struct mhd_problem {
 
   // state (nf fields starting at src) -> colbuf slots 0..nf-1
   int z_inverse(const float2* src, int nf) {
-    ColArgs a{src, colbuf, FS(), (long long)g.kxp, (long long)g.k2 * g.kxp, (long long)g.kxp, SLK(), AZ(),
-              (float)(1.0 / ((double)g.n * g.n * g.n))};
+    ColArgs a{src, colbuf, FS(), (long long)g.kxp, (long long)g.k2 * g.kxp, (long long)g.kxp, SLK(), AZ()};
     return launch(KC_ZINV, [&] { ops->col_inv(a, g, g.k2, nf, stream); });
   }
   int y_inverse(int nf) {
-    ColArgs a{colbuf, rowbuf, (long long)g.kxp, AZ(), SLK(), (long long)g.kxp, BZ(), SLK(), 1.0f};
+    ColArgs a{colbuf, rowbuf, (long long)g.kxp, AZ(), SLK(), (long long)g.kxp, BZ(), SLK()};
     return launch(KC_YINV, [&] { ops->col_inv(a, g, g.n, nf, stream); });
   }
   int x_fused() {
@@ -364,12 +364,12 @@ struct mhd_problem {
     return launch(KC_XFUSED, [&] { ops->x_fused(rowbuf, g, SLK(), g.kxp, stream); });
   }
   int y_forward(int nf) {
-    ColArgs a{rowbuf, colbuf, (long long)g.kxp, BZ(), SLK(), (long long)g.kxp, AZ(), SLK(), 1.0f};
+    ColArgs a{rowbuf, colbuf, (long long)g.kxp, BZ(), SLK(), (long long)g.kxp, AZ(), SLK()};
     return launch(KC_YFWD, [&] { ops->col_fwd(a, g, g.n, nf, stream); });
   }
   // colbuf slots -> compact planes (nf fields/products) of dst, pruned output
   int z_forward(float2* dst, int nf) {
-    ColArgs a{colbuf, dst, (long long)g.kxp, SLK(), AZ(), FS(), (long long)g.kxp, (long long)g.k2 * g.kxp, 1.0f};
+    ColArgs a{colbuf, dst, (long long)g.kxp, SLK(), AZ(), FS(), (long long)g.kxp, (long long)g.k2 * g.kxp};
     return launch(KC_ZFWD, [&] { ops->col_fwd(a, g, g.k2, nf, stream); });
   }
   // Stage epilogue: RHS from the 8 compact product planes (in rowbuf) and the stage state X.
@@ -388,6 +388,8 @@ struct mhd_problem {
     a.ca = ca;
     a.cb = cb;
     a.op = op;
+    const double n3 = (double)g.n * g.n * g.n;
+    a.pscale = (float)(1.0 / (n3 * n3));
     const int bx = g.kx <= 256 ? (g.kx + 31) / 32 * 32 : 256;
     const dim3 grid((g.kx + bx - 1) / bx, g.k2, g.k2);
     return launch(KC_RKEPI, [&] {
@@ -441,7 +443,7 @@ struct mhd_problem {
     int rc;
     if ((rc = z_inverse(src, 1))) return rc;
     if ((rc = y_inverse(1))) return rc;
-    return launch(KC_OTHER, [&] { ops->x_c2r(rowbuf, phys, g, SLK(), stream); });
+    return launch(KC_OTHER, [&] { ops->x_c2r(rowbuf, phys, g, SLK(), (float)(1.0 / ((double)g.n * g.n * g.n)), stream); });
   }
   // One field: physical staging -> compact dst (unnormalised forward).
   int forward_field(float2* dst) {

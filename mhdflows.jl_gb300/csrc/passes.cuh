@@ -50,7 +50,6 @@ struct ColArgs {
   float2* dst;
   long long sF, sO, sR;  // source strides (complex elements): field/slot, outer, row
   long long dF, dO, dR;  // destination strides
-  float scale;           // applied to every loaded value
 };
 
 // ------------------------------------------------------------------------------------------
@@ -67,14 +66,18 @@ struct ColWork {
   int rows_in;  // rows staged per tile (K2 for pruned input, n otherwise)
 };
 
-template <int TX>
+// Rows 0..rows-1 of a TX-column tile starting at column col0 -> buf[row][TX] (16-byte chunks;
+// chunks past the padded row length are skipped).  Each thread keeps one chunk column.
+template <int TX, int NT>
 __device__ __forceinline__ void col_prefetch(float2* buf, const float2* src, long long sR, int rows, int col0, int kxp) {
-  constexpr int CH = TX / 2;  // 16-byte chunks per row
-  const int nch = rows * CH;
-  for (int c = threadIdx.x; c < nch; c += blockDim.x) {
-    const int row = c / CH, q = c % CH;
-    if (col0 + 2 * q < kxp) cp_async16(buf + row * TX + 2 * q, src + row * sR + col0 + 2 * q);
-  }
+  constexpr int CH = TX / 2;       // 16-byte chunks per row
+  constexpr int RSTEP = NT / CH;   // rows advanced per sweep
+  const int q = threadIdx.x % CH;
+  if (col0 + 2 * q >= kxp) return;
+  int row = threadIdx.x / CH;
+  const float2* s = src + row * sR + col0 + 2 * q;
+  float2* d = buf + row * TX + 2 * q;
+  for (; row < rows; row += RSTEP, s += RSTEP * sR, d += RSTEP * TX) cp_async16(d, s);
 }
 
 template <class P0, int TX, int DIR, bool PIN, bool POUT>
@@ -96,7 +99,7 @@ __global__ void __launch_bounds__(TX * P0::G, TX * P0::G <= 256 ? 2 : 1)
   if (t < total) {
     int c0;
     const float2* s0 = tile_src(t, c0);
-    col_prefetch<TX>(smem, s0, a.sR, w.rows_in, c0, geo.kxp);
+    col_prefetch<TX, TX * G>(smem, s0, a.sR, w.rows_in, c0, geo.kxp);
   }
   cp_async_commit();
   for (int it = 0; t < total; t += gridDim.x, ++it) {
@@ -105,7 +108,7 @@ __global__ void __launch_bounds__(TX * P0::G, TX * P0::G <= 256 ? 2 : 1)
     if (tn < total) {
       int c1;
       const float2* s1 = tile_src(tn, c1);
-      col_prefetch<TX>(smem + ((it + 1) & 1) * (N * TX), s1, a.sR, w.rows_in, c1, geo.kxp);
+      col_prefetch<TX, TX * G>(smem + ((it + 1) & 1) * (N * TX), s1, a.sR, w.rows_in, c1, geo.kxp);
     }
     cp_async_commit();
     cp_async_wait<1>();
@@ -123,19 +126,20 @@ __global__ void __launch_bounds__(TX * P0::G, TX * P0::G <= 256 ? 2 : 1)
         const int n = g + G * d + P::LI * n0;
         const int row = PIN ? kept_of_freq(geo, n) : n;
         float2 x = make_float2(0.f, 0.f);
-        if (colok && row >= 0) x = cscale(cur[row * TX + tx], a.scale);
+        if (colok && row >= 0) x = cur[row * TX + tx];
         v[0][d * P::R0 + n0] = x;
       }
     __syncthreads();  // cur is now free: reuse it as the exchange buffer
     fft_run<P, DIR, 1, 0, TX>(v, cur, tx, g, tw, BlockSync{});
     float2* dst = a.dst + f * a.dF + (long long)o * a.dO + kxg;
+    const int dR = (int)a.dR;  // row offsets inside one buffer fit 32 bits for n <= 512
 #pragma unroll
     for (int d = 0; d < P::DF; ++d)
 #pragma unroll
       for (int e = 0; e < P::RF; ++e) {
         const int k = g + G * d + P::LF * e;
         const int row = POUT ? kept_of_freq(geo, k) : k;
-        if (colok && row >= 0) dst[row * a.dR] = v[0][d * P::RF + e];
+        if (colok && row >= 0) dst[row * dR] = v[0][d * P::RF + e];
       }
     __syncthreads();  // all exchange reads of cur done before it is refilled
   }
@@ -210,7 +214,7 @@ struct XCfg {
 };
 
 template <class P, int GROUPS>
-__global__ void __launch_bounds__(GROUPS * XCfg<P>::TPG, 4) x_fused_kernel(float2* buf, Geom geo, long long rowstride,
+__global__ void __launch_bounds__(GROUPS * XCfg<P>::TPG, (P::V > 8 ? 2 : 4)) x_fused_kernel(float2* buf, Geom geo, long long rowstride,
                                                                              long long slot, const float2* __restrict__ tw,
                                                                              const float2* __restrict__ twr) {
   using PR = typename Reverse<P>::type;
@@ -287,10 +291,11 @@ __global__ void __launch_bounds__(GROUPS * XCfg<P>::TPG, 4) x_fused_kernel(float
   cp_async_wait<0>();
 }
 
-// Plain c2r of row pairs: spectral rows (2q, 2q+1) -> physical rows, normalisation already applied.
+// Plain c2r of row pairs: spectral rows (2q, 2q+1) -> physical rows times scale (1/n^3: the
+// column passes do not normalise).
 template <class P, int ROWS>
 __global__ void __launch_bounds__(ROWS * P::G) x_c2r_kernel(const float2* src, float* dst, Geom geo, long long srow,
-                                                              const float2* __restrict__ tw) {
+                                                              float scale, const float2* __restrict__ tw) {
   constexpr int G = P::G, V = P::V, N = P::N;
   constexpr int TS = RowCfg<P>::TS;
   extern __shared__ float2 smem[];
@@ -306,8 +311,8 @@ __global__ void __launch_bounds__(ROWS * P::G) x_c2r_kernel(const float2* src, f
 #pragma unroll
     for (int e = 0; e < P::RF; ++e) {
       const int x = g + G * d + P::LF * e;
-      da[x] = v[0][d * P::RF + e].x;
-      db[x] = v[0][d * P::RF + e].y;
+      da[x] = scale * v[0][d * P::RF + e].x;
+      db[x] = scale * v[0][d * P::RF + e].y;
     }
 }
 
@@ -370,6 +375,7 @@ struct RkArgs {
   float2* xn;           // RK4 next stage state / LSRK4 u
   long long fs;         // compact field stride (complex elements)
   float nu, eta, h, dt, ca, cb;
+  float pscale;         // 1/n^6: the column and row passes are unnormalised in both directions
   int op;
 };
 
@@ -414,7 +420,7 @@ __global__ void __launch_bounds__(256) rk_epilogue_kernel(RkArgs a, Geom geo) {
   const float k2 = kxv * kxv + kyv * kyv + kzv * kzv;
   float2 p[8];
 #pragma unroll
-  for (int q = 0; q < 8; ++q) p[q] = __ldcs(a.prod + q * fs + i);
+  for (int q = 0; q < 8; ++q) p[q] = cscale(__ldcs(a.prod + q * fs + i), a.pscale);
   float2 xv[6];
 #pragma unroll
   for (int c = 0; c < 6; ++c) xv[c] = a.X[c * fs + i];
