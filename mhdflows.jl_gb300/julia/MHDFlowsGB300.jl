@@ -1,0 +1,92 @@
+# Julia binding of libmhdgb (include/mhdgb.h) for MHDFlows.jl.
+#
+# Provides a time stepper that plugs into MHDFlows the same way HM89TimeStepper does
+# (src/timestepper/HM89.jl:6-31 of MHDFlows.jl): a struct <: FourierFlows.AbstractTimeStepper
+# plus a stepforward! method, selected in MHDFLowsProblem (src/Problems.jl:124-129) by
+# stepper = "GB300RK4" or "GB300LSRK4".  The device state lives in the library; prob.sol is
+# refreshed from it on demand (sync_sol!) so savefile / Restart! / Diagnostic keep working.
+#
+# Not exercised in this repository's test suite (no Julia toolchain is available here); the
+# same C ABI is exercised from Python through ctypes with identical signatures.
+module MHDFlowsGB300
+
+using FourierFlows
+import FourierFlows: stepforward!
+
+export GB300TimeStepper, gb300_updatevars!, sync_sol!, push_sol!, gb300_diagnostics
+
+const libmhdgb = get(ENV, "MHDGB_LIB", joinpath(@__DIR__, "..", "lib", "libmhdgb.so"))
+
+struct MhdParams
+  n::Cint
+  L::Cdouble
+  nu::Cdouble
+  eta::Cdouble
+  nnu::Cint
+  neta::Cint
+  dt::Cdouble
+  scheme::Cint
+  precision::Cint
+  device::Cint
+end
+
+check(rc) = rc == 0 ? nothing : error(unsafe_string(ccall((:mhd_last_error, libmhdgb), Cstring, ())))
+
+mutable struct GB300TimeStepper{T} <: FourierFlows.AbstractTimeStepper{T}
+  handle::Ptr{Cvoid}
+  n::Int
+end
+
+function GB300TimeStepper(grid, params, dt; scheme::Symbol = :RK4, device::Integer = 0)
+  grid.nx == grid.ny == grid.nz || error("GB300TimeStepper needs a cubic grid")
+  p = MhdParams(grid.nx, grid.Lx, params.ν, params.η, params.nν, params.nη, dt,
+                scheme == :RK4 ? 0 : 1, 0, device)
+  h = Ref{Ptr{Cvoid}}(C_NULL)
+  check(ccall((:mhd_create, libmhdgb), Cint, (Ref{MhdParams}, Ref{Ptr{Cvoid}}), p, h))
+  ts = GB300TimeStepper{Array{ComplexF32,4}}(h[], grid.nx)
+  finalizer(t -> ccall((:mhd_destroy, libmhdgb), Cint, (Ptr{Cvoid},), t.handle), ts)
+  return ts
+end
+
+# prob.sol (host or device array, (nkr, n, n, 6) ComplexF32) <-> library state
+push_sol!(ts::GB300TimeStepper, sol) =
+  check(ccall((:mhd_set_state, libmhdgb), Cint, (Ptr{Cvoid}, Ptr{ComplexF32}), ts.handle, Array(sol)))
+
+function sync_sol!(sol, ts::GB300TimeStepper)
+  host = Array{ComplexF32}(undef, size(sol))
+  check(ccall((:mhd_get_state, libmhdgb), Cint, (Ptr{Cvoid}, Ptr{ComplexF32}), ts.handle, host))
+  copyto!(sol, host)
+  return nothing
+end
+
+# stepforward!(sol, clock, ts, equation, vars, params, grid): one step on the GPU; the host
+# sol is not touched (call sync_sol! before reading it), clock advances like FourierFlows'.
+function stepforward!(sol, clock, ts::GB300TimeStepper, equation, vars, params, grid)
+  check(ccall((:mhd_set_clock, libmhdgb), Cint, (Ptr{Cvoid}, Cdouble, Clonglong, Cdouble),
+              ts.handle, clock.t, clock.step, clock.dt))
+  check(ccall((:mhd_step, libmhdgb), Cint, (Ptr{Cvoid}, Cint), ts.handle, 1))
+  clock.t += clock.dt
+  clock.step += 1
+  return nothing
+end
+
+# updatevars!(prob): vars.ux..bz <- irfft(sol) of the current state
+function gb300_updatevars!(prob)
+  ts = prob.timestepper
+  for (f, name) in enumerate((:ux, :uy, :uz, :bx, :by, :bz))
+    host = Array{Float32}(undef, ts.n, ts.n, ts.n)
+    check(ccall((:mhd_get_physical, libmhdgb), Cint, (Ptr{Cvoid}, Cint, Ptr{Float32}), ts.handle, f - 1, host))
+    copyto!(getfield(prob.vars, name), host)
+  end
+  return nothing
+end
+
+# E_u, E_B, H_c, max|k.u|, max|k.B|, max|div B|, non-finite count, t
+function gb300_diagnostics(ts::GB300TimeStepper)
+  out = zeros(Float64, 8)
+  rc = ccall((:mhd_diagnostics, libmhdgb), Cint, (Ptr{Cvoid}, Ptr{Cdouble}, Cint), ts.handle, out, 8)
+  check(rc)
+  return out
+end
+
+end # module
