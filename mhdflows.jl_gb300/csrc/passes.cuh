@@ -66,18 +66,29 @@ struct ColWork {
   int rows_in;  // rows staged per tile (K2 for pruned input, n otherwise)
 };
 
-// Rows 0..rows-1 of a TX-column tile starting at column col0 -> buf[row][TX] (16-byte chunks;
-// chunks past the padded row length are skipped).  Each thread keeps one chunk column.
-template <int TX, int NT>
-__device__ __forceinline__ void col_prefetch(float2* buf, const float2* src, long long sR, int rows, int col0, int kxp) {
+// Rows 0..rows-1 of a TX-column tile starting at column col0 -> buf[row'][TX] (16-byte chunks;
+// chunks past the padded row length are skipped).  Each thread keeps one chunk column.  With
+// PIN the rows are kept indices and land at their frequency position row' (non-negative modes
+// in place, negative modes at row + n - K2); the alias rows in between are zero-filled, so the
+// transform reads every row unconditionally.
+template <int TX, int NT, int N, bool PIN>
+__device__ __forceinline__ void col_prefetch(float2* buf, const float2* src, long long sR, int rows, int col0,
+                                             const Geom& geo) {
   constexpr int CH = TX / 2;       // 16-byte chunks per row
   constexpr int RSTEP = NT / CH;   // rows advanced per sweep
   const int q = threadIdx.x % CH;
-  if (col0 + 2 * q >= kxp) return;
   int row = threadIdx.x / CH;
+  if (PIN) {
+    float4* zb = reinterpret_cast<float4*>(buf + geo.kp * TX);
+    const int nz = (N - geo.k2) * CH;
+    for (int c = threadIdx.x; c < nz; c += NT) zb[c] = make_float4(0.f, 0.f, 0.f, 0.f);
+  }
+  if (col0 + 2 * q >= geo.kxp) return;
   const float2* s = src + row * sR + col0 + 2 * q;
-  float2* d = buf + row * TX + 2 * q;
-  for (; row < rows; row += RSTEP, s += RSTEP * sR, d += RSTEP * TX) cp_async16(d, s);
+  for (; row < rows; row += RSTEP, s += RSTEP * sR) {
+    const int drow = PIN ? (row < geo.kp ? row : row + N - geo.k2) : row;
+    cp_async16(buf + drow * TX + 2 * q, s);
+  }
 }
 
 template <class P0, int TX, int DIR, bool PIN, bool POUT>
@@ -85,9 +96,21 @@ __global__ void __launch_bounds__(TX * P0::G, TX * P0::G <= 256 ? 2 : 1)
     col_pass_kernel(ColArgs a, Geom geo, ColWork w, const float2* __restrict__ tw) {
   using P = Unpadded<P0>;
   extern __shared__ float2 smem[];
-  constexpr int G = P::G, V = P::V, N = P::N;
+  constexpr int G = P::G, V = P::V, N = P::N, NT = TX * P0::G;
   const int tx = threadIdx.x % TX, g = threadIdx.x / TX;
   const int total = w.tiles_x * w.outer * w.nf;
+  // Kept-output bookkeeping (loop invariant): output element e of slot d has frequency
+  // k = g + G*d + LF*e; it is kept for e < e_lo[d] (k < Kp) or e >= e_hi[d] (k >= n - Kn),
+  // and its kept index is k (first range) or k - (n - K2) (second range).
+  int e_lo[P::DF], e_hi[P::DF];
+#pragma unroll
+  for (int d = 0; d < P::DF; ++d) {
+    const int l = g + G * d;
+    e_lo[d] = POUT ? (geo.kp - l + P::LF - 1) / P::LF : P::RF;
+    e_hi[d] = POUT ? (N - geo.kn - l + P::LF - 1) / P::LF : P::RF;
+  }
+  const int dR = (int)a.dR;  // row offsets inside one buffer fit 32 bits for n <= 512
+  const int shift = (N - geo.k2) * dR;
   auto tile_src = [&](int t, int& col0) {
     const int tx_t = t % w.tiles_x;
     const int r = t / w.tiles_x;
@@ -99,7 +122,7 @@ __global__ void __launch_bounds__(TX * P0::G, TX * P0::G <= 256 ? 2 : 1)
   if (t < total) {
     int c0;
     const float2* s0 = tile_src(t, c0);
-    col_prefetch<TX, TX * G>(smem, s0, a.sR, w.rows_in, c0, geo.kxp);
+    col_prefetch<TX, NT, N, PIN>(smem, s0, a.sR, w.rows_in, c0, geo);
   }
   cp_async_commit();
   for (int it = 0; t < total; t += gridDim.x, ++it) {
@@ -108,7 +131,7 @@ __global__ void __launch_bounds__(TX * P0::G, TX * P0::G <= 256 ? 2 : 1)
     if (tn < total) {
       int c1;
       const float2* s1 = tile_src(tn, c1);
-      col_prefetch<TX, TX * G>(smem + ((it + 1) & 1) * (N * TX), s1, a.sR, w.rows_in, c1, geo.kxp);
+      col_prefetch<TX, NT, N, PIN>(smem + ((it + 1) & 1) * (N * TX), s1, a.sR, w.rows_in, c1, geo);
     }
     cp_async_commit();
     cp_async_wait<1>();
@@ -117,30 +140,31 @@ __global__ void __launch_bounds__(TX * P0::G, TX * P0::G <= 256 ? 2 : 1)
     const int r = t / w.tiles_x;
     const int o = r % w.outer, f = r / w.outer;
     const int kxg = tx_t * TX + tx;
-    const bool colok = kxg < geo.kx;
     float2 v[1][V];
 #pragma unroll
     for (int d = 0; d < P::DI; ++d)
 #pragma unroll
-      for (int n0 = 0; n0 < P::R0; ++n0) {
-        const int n = g + G * d + P::LI * n0;
-        const int row = PIN ? kept_of_freq(geo, n) : n;
-        float2 x = make_float2(0.f, 0.f);
-        if (colok && row >= 0) x = cur[row * TX + tx];
-        v[0][d * P::R0 + n0] = x;
-      }
+      for (int n0 = 0; n0 < P::R0; ++n0) v[0][d * P::R0 + n0] = cur[(g + G * d + P::LI * n0) * TX + tx];
     __syncthreads();  // cur is now free: reuse it as the exchange buffer
     fft_run<P, DIR, 1, 0, TX>(v, cur, tx, g, tw, BlockSync{});
-    float2* dst = a.dst + f * a.dF + (long long)o * a.dO + kxg;
-    const int dR = (int)a.dR;  // row offsets inside one buffer fit 32 bits for n <= 512
+    if (kxg < geo.kx) {
+      float2* dst = a.dst + f * a.dF + (long long)o * a.dO + kxg;
 #pragma unroll
-    for (int d = 0; d < P::DF; ++d)
+      for (int d = 0; d < P::DF; ++d) {
+        const int base = (g + G * d) * dR;
 #pragma unroll
-      for (int e = 0; e < P::RF; ++e) {
-        const int k = g + G * d + P::LF * e;
-        const int row = POUT ? kept_of_freq(geo, k) : k;
-        if (colok && row >= 0) dst[row * dR] = v[0][d * P::RF + e];
+        for (int e = 0; e < P::RF; ++e) {
+          const int off = base + e * (P::LF * dR);
+          if (!POUT) {
+            dst[off] = v[0][d * P::RF + e];
+          } else if (e < e_lo[d]) {
+            dst[off] = v[0][d * P::RF + e];
+          } else if (e >= e_hi[d]) {
+            dst[off - shift] = v[0][d * P::RF + e];
+          }
+        }
       }
+    }
     __syncthreads();  // all exchange reads of cur done before it is refilled
   }
   cp_async_wait<0>();
