@@ -218,8 +218,9 @@ Geom make_geom(int n, double L) {
 }
 
 // Kernel classes for per-launch timing.
-enum KClass { KC_ZINV = 0, KC_YINV, KC_XFUSED, KC_YFWD, KC_ZFWD, KC_RKEPI, KC_OTHER, KC_COUNT };
-const char* kClassNames[KC_COUNT] = {"z_inverse", "y_inverse", "x_fused", "y_forward", "z_forward", "rk_epilogue", "other"};
+enum KClass { KC_ZINV = 0, KC_YINV, KC_XFUSED, KC_YFWD, KC_ZFWD, KC_RKEPI, KC_HERM, KC_OTHER, KC_COUNT };
+const char* kClassNames[KC_COUNT] = {"z_inverse", "y_inverse", "x_fused", "y_forward", "z_forward", "rk_epilogue",
+                                     "herm_kx0", "other"};
 
 const double kLsA[5] = {0.0, -567301805773.0 / 1357537059087.0, -2404267990393.0 / 2016746695238.0,
                         -3550918686646.0 / 2091501179385.0, -1275806237668.0 / 842570457699.0};
@@ -374,9 +375,15 @@ struct mhd_problem {
   }
   // Stage epilogue: RHS from the 8 compact product planes (in rowbuf) and the stage state X.
   int epilogue(const float2* X, int op, float h, float ca, float cb) {
+    int rc = launch(KC_HERM, [&] {
+      const int total = 6 * g.k2 * g.k2;
+      herm_kx0_kernel<<<(total + 255) / 256, 256, 0, stream>>>(X, aux, g, FS());
+    });
+    if (rc) return rc;
     RkArgs a{};
     a.prod = rowbuf;
     a.X = X;
+    a.H = aux;
     a.sol = sol;
     a.acc = acc;
     a.xn = (op == OP_LS_FIRST || op == OP_LS) ? sol : xs;
@@ -733,7 +740,8 @@ int mhd_kernel_class_bytes(mhd_handle h, int cls, double* bytes) {
     case KC_XFUSED: b = (6 + 8) * n * n * kx * c; break;
     case KC_YFWD: b = 8 * (n * n * kx * c + n * k2 * kx * c); break;
     case KC_ZFWD: b = 8 * (n * k2 * kx * c + state_field); break;
-    case KC_RKEPI: b = 8 * state_field + arrays * 6 * state_field; break;
+    case KC_RKEPI: b = 8 * state_field + arrays * 6 * state_field + 6 * k2 * k2 * c; break;
+    case KC_HERM: b = 2 * 6 * k2 * k2 * c; break;
     default: b = 0;
   }
   *bytes = b;

@@ -26,6 +26,10 @@ __host__ __device__ __forceinline__ int kept_of_freq(const Geom& g, int f) {
 }
 __host__ __device__ __forceinline__ int freq_of_kept(const Geom& g, int j) { return j < g.kp ? j : j + g.n - g.k2; }
 __host__ __device__ __forceinline__ int signed_of_kept(const Geom& g, int j) { return j < g.kp ? j : j - g.k2; }
+// kept index of a signed wavenumber, -1 if it lies in the alias band
+__host__ __device__ __forceinline__ int kept_of_signed(const Geom& g, int s) {
+  return s >= 0 ? (s < g.kp ? s : -1) : (s >= -g.kn ? s + g.k2 : -1);
+}
 
 struct BlockSync {
   __device__ __forceinline__ void operator()() const { __syncthreads(); }
@@ -394,6 +398,7 @@ enum StageOp : int {
 struct RkArgs {
   const float2* prod;   // 8 compact planes
   const float2* X;      // stage state (6 fields)
+  const float2* H;      // Hermitian part of X on the kx = 0 plane, [f][kz'][ky'] (diffusion operand)
   float2* sol;          // RK4 step-start state
   float2* acc;          // RK4 accumulator / LSRK4 du / OP_RHS output
   float2* xn;           // RK4 next stage state / LSRK4 u
@@ -445,9 +450,14 @@ __global__ void __launch_bounds__(256) rk_epilogue_kernel(RkArgs a, Geom geo) {
   float2 p[8];
 #pragma unroll
   for (int q = 0; q < 8; ++q) p[q] = cscale(__ldcs(a.prod + q * fs + i), a.pscale);
-  float2 xv[6];
+  float2 xv[6], xd[6];
 #pragma unroll
-  for (int c = 0; c < 6; ++c) xv[c] = a.X[c * fs + i];
+  for (int c = 0; c < 6; ++c) xv[c] = xd[c] = a.X[c * fs + i];
+  if (x == 0) {
+    const long long p = (long long)jz * geo.k2 + jy, pl = (long long)geo.k2 * geo.k2;
+#pragma unroll
+    for (int c = 0; c < 6; ++c) xd[c] = a.H[c * pl + p];
+  }
   const float2 dxz = p[0], dyz = p[1], txy = p[2], txz = p[3], tyz = p[4];
   const float2 axy = p[5], axz = p[6], ayz = p[7];
   float2 Vx, Vy, Vz;
@@ -472,7 +482,26 @@ __global__ void __launch_bounds__(256) rk_epilogue_kernel(RkArgs a, Geom geo) {
 #pragma unroll
   for (int c = 0; c < 6; ++c) {
     const float dk = c < 3 ? du : db;
-    rk_apply<OP>(a, c * fs + i, xv[c], make_float2(nl[c].x + dk * xv[c].x, nl[c].y + dk * xv[c].y));
+    rk_apply<OP>(a, c * fs + i, xv[c], make_float2(nl[c].x + dk * xd[c].x, nl[c].y + dk * xd[c].y));
+  }
+}
+
+// Hermitian part of the kx = 0 plane of the six fields: H(k) = (X(k) + conj X(-k)) / 2, with
+// X(-k) = 0 when -k is in the alias band.  The reference's diffusion term is computed from the
+// re-transformed physical field, rfft(irfft(X)), which is exactly this on the kx = 0 plane.
+__global__ void herm_kx0_kernel(const float2* __restrict__ X, float2* __restrict__ H, Geom geo, long long fs) {
+  const int total = 6 * geo.k2 * geo.k2;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
+    const int jy = i % geo.k2;
+    const int r = i / geo.k2;
+    const int jz = r % geo.k2, c = r / geo.k2;
+    const long long base = (long long)c * fs;
+    const float2 xk = X[base + ((long long)jz * geo.k2 + jy) * geo.kxp];
+    const int py = kept_of_signed(geo, -signed_of_kept(geo, jy));
+    const int pz = kept_of_signed(geo, -signed_of_kept(geo, jz));
+    float2 xp = make_float2(0.f, 0.f);
+    if (py >= 0 && pz >= 0) xp = X[base + ((long long)pz * geo.k2 + py) * geo.kxp];
+    H[i] = make_float2(0.5f * (xk.x + xp.x), 0.5f * (xk.y - xp.y));
   }
 }
 

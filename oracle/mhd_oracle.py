@@ -194,13 +194,31 @@ def calcN_literal(N, sol, grid: Grid, nu, eta, nnu=0, neta=0, vars_out=None):
     return N
 
 
+def hermitian_kx0(grid: Grid, X):
+    """X with its kx = 0 plane replaced by the Hermitian part (X(k) + conj X(-k))/2.
+
+    This is what rfft(irfft(X)) does to a dealiased state: the reference computes its diffusion
+    term from the re-transformed physical field (src/Solver/MHDSolver.jl:91-94, 166-168), so on
+    the kx = 0 plane it acts on the Hermitian part.  It matters on the edge modes ky or kz = -Kn,
+    whose partner +Kn is in the alias band (there the effective diffusion is halved).
+    """
+    Y = X.copy()
+    n = grid.n
+    iz = (-np.arange(n)) % n
+    p = X[..., :, :, 0]
+    Y[..., :, :, 0] = 0.5 * (p + np.conj(p[..., iz, :][..., :, iz]))
+    return Y
+
+
 def calcN_fast(N, sol, grid: Grid, nu, eta):
     """Same RHS as ``calcN_literal`` with the six unique stress products transformed once.
 
-    Used for larger FP64 checks; mathematically identical to the literal form.
+    Used for larger FP64 checks; mathematically identical to the literal form (the diffusion
+    acts on the Hermitian part of the kx = 0 plane, as rfft(irfft(.)) makes it do there).
     """
     g = grid
     g.dealias(sol)
+    H = hermitian_kx0(g, sol)
     v = [g.irfft(sol[f]) for f in range(6)]
     u, b = v[0:3], v[3:6]
     ks = g.ks
@@ -212,7 +230,7 @@ def calcN_fast(N, sol, grid: Grid, nu, eta):
     V = [sum(ks[i] * T[(i, j)] for i in range(3)) for j in range(3)]
     kV = sum(ks[j] * V[j] for j in range(3)) * g.invKrsq
     for a in range(3):
-        N[a] = 1j * (V[a] - ks[a] * kV) - g.Krsq * nu * sol[a]
+        N[a] = 1j * (V[a] - ks[a] * kV) - g.Krsq * nu * H[a]
     E = {}
     for a in range(3):
         for j in range(a + 1, 3):
@@ -223,7 +241,7 @@ def calcN_fast(N, sol, grid: Grid, nu, eta):
         for j in range(3):
             if j != a:
                 acc = acc + ks[j] * E[(a, j)]
-        N[3 + a] = 1j * acc - g.Krsq * eta * sol[3 + a]
+        N[3 + a] = 1j * acc - g.Krsq * eta * H[3 + a]
     return N
 
 
