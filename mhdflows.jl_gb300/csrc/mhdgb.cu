@@ -55,7 +55,7 @@ template <> struct Cfg<64>  { using C = Plan<64, 8, 8, 8>;       using R = Plan<
 template <> struct Cfg<96>  { using C = Plan<96, 8, 12, 4, 2>;   using R = Plan<96, 8, 12, 4, 2>;   static constexpr int TX = 16, TXE = 16, ROWS = 16; };
 template <> struct Cfg<128> { using C = Plan<128, 8, 16, 8>;     using R = Plan<128, 16, 8, 4, 4>;  static constexpr int TX = 16, TXE = 16, ROWS = 8; };
 template <> struct Cfg<256> { using C = Plan<256, 16, 16, 16>;   using R = Plan<256, 32, 8, 8, 4>;  static constexpr int TX = 16, TXE = 16, ROWS = 4; };
-template <> struct Cfg<512> { using C = Plan<512, 32, 16, 8, 4>; using R = Plan<512, 64, 8, 8, 8>;  static constexpr int TX = 16, TXE = 8, ROWS = 2; };
+template <> struct Cfg<512> { using C = Plan<512, 32, 16, 8, 4>; using R = Plan<512, 64, 8, 8, 8>;  static constexpr int TX = 8, TXE = 8, ROWS = 2; };
 
 constexpr int kSlots = 8;
 
