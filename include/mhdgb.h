@@ -65,6 +65,7 @@ typedef struct mhd_params {
 } mhd_params;
 
 typedef struct mhd_problem* mhd_handle;
+typedef struct mhd_ensemble_s* mhd_ensemble;
 
 /* Problem construction (Problem(GPU(); ...), src/pgen.jl:64-127). */
 int mhd_create(const mhd_params* params, mhd_handle* out);
@@ -131,6 +132,33 @@ const char* mhd_kernel_class_name(int cls);
 int mhd_kernel_class_count(void);
 /* Algorithmic HBM bytes one launch of a kernel class moves for this handle's size. */
 int mhd_kernel_class_bytes(mhd_handle h, int cls, double* bytes);
+
+/* ---- Batched solves (no counterpart in the reference, which runs one problem per process).
+ * A batch handle is a size class: `capacity` slots of one grid size n, box L and scheme, whose
+ * state stays resident in HBM.  mhd_step on a batch advances every active slot by one step in
+ * the same launches (persistent kernels walk the active (slot, tile) work-list); each slot has
+ * its own nu, eta, dt and clock.  mhd_create is the capacity-1 case with slot 0 active, and the
+ * single-problem functions above act on slot 0.  Results of a slot do not depend on which other
+ * slots are active (no reduction crosses slots). */
+int mhd_batch_create(const mhd_params* params, int capacity, mhd_handle* out);
+int mhd_batch_add(mhd_handle h, double nu, double eta, double dt, int* slot);   /* state zeroed */
+int mhd_batch_remove(mhd_handle h, int slot);
+int mhd_batch_info(mhd_handle h, int* capacity, int* active);
+/* Device bytes of one slot and of a size class's shared staging (admission control). */
+int mhd_slot_bytes(const mhd_params* params, long long* per_slot, long long* per_class);
+int mhd_slot_set_state(mhd_handle h, int slot, const float* sol);
+int mhd_slot_get_state(mhd_handle h, int slot, float* sol);
+int mhd_slot_set_physical(mhd_handle h, int slot, int field, const float* phys);
+int mhd_slot_get_physical(mhd_handle h, int slot, int field, float* phys);
+int mhd_slot_diagnostics(mhd_handle h, int slot, double* out, int nout);
+int mhd_slot_get_clock(mhd_handle h, int slot, double* t, long long* step, double* dt);
+int mhd_slot_set_clock(mhd_handle h, int slot, double t, long long step, double dt);
+
+/* Ensembles of size classes stepped together: one CUDA graph holds one step of every member,
+ * each member on its own stream, so boxes of different sizes run concurrently. */
+int mhd_ensemble_create(mhd_handle* handles, int count, mhd_ensemble* out);
+int mhd_ensemble_step(mhd_ensemble e, int nsteps);
+int mhd_ensemble_destroy(mhd_ensemble e);
 
 /* Timing helper: elapsed device milliseconds of nsteps steps measured with events on the stream. */
 int mhd_time_steps(mhd_handle h, int nsteps, double* ms);

@@ -29,6 +29,7 @@ from ._lib import MHDError, MHD_LSRK4, MHD_RK4
 __all__ = [
     "GPU", "CPU", "Problem", "SetUpProblemIC", "stepforward", "updatevars", "ProbDiagnostic",
     "Diagnostics", "TimeIntegrator", "MHDError", "kept_modes", "supported_sizes", "footprint_bytes",
+    "Batch", "Ensemble", "slot_bytes",
 ]
 
 FIELDS = ("ux", "uy", "uz", "bx", "by", "bz")
@@ -356,3 +357,147 @@ def TimeIntegrator(prob: Problem, t0: float, N0: int, *, usr_dt: float = 0.0, di
     prob.synchronize()
     el = time.perf_counter() - start
     return prob.clock.step * prob.n ** 3 / el if el > 0 else float("inf")
+
+
+# ---------------------------------------------------------------------------------------------
+# Batched solves (no counterpart in the reference): size classes of resident problems stepped
+# together, and ensembles of size classes stepped concurrently in one CUDA graph per step.
+# ---------------------------------------------------------------------------------------------
+
+def slot_bytes(n: int, L: float = 2 * math.pi):
+    """(bytes per slot, bytes per size class) on the device for grid size n."""
+    lib = _lib.load()
+    p = _params(n, L, 0.0, 0.0, 0, 0, 0.0, MHD_RK4, 0)
+    a, b = C.c_longlong(), C.c_longlong()
+    _lib.check(lib.mhd_slot_bytes(C.byref(p), C.byref(a), C.byref(b)))
+    return a.value, b.value
+
+
+class Batch:
+    """A size class: up to ``capacity`` problems of grid size n (one scheme) resident in HBM.
+
+    ``step`` advances every active slot by one time step in the same kernel launches; each slot
+    has its own nu, eta, dt and clock.  Slot arrays use the C-ordered reference layout
+    (6, n, n, nkr) complex64 for states and (n, n, n) float32 for physical fields.
+    """
+
+    def __init__(self, n: int, capacity: int, stepper: str = "RK4", L: float = 2 * math.pi, device: int = 0):
+        scheme = {"RK4": MHD_RK4, "LSRK4": MHD_LSRK4}.get(str(stepper).upper())
+        if scheme is None:
+            raise MHDError(_lib.MHD_ERR_INVALID, f"unknown stepper {stepper!r}")
+        self._lib = _lib.load()
+        self.n, self.L, self.stepper = int(n), float(L), str(stepper).upper()
+        self.nkr = self.n // 2 + 1
+        p = _params(self.n, self.L, 0.0, 0.0, 0, 0, 0.0, scheme, device)
+        h = C.c_void_p()
+        _lib.check(self._lib.mhd_batch_create(C.byref(p), int(capacity), C.byref(h)))
+        self._h = h
+
+    @property
+    def handle(self):
+        return self._h
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.mhd_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def info(self):
+        cap, act = C.c_int(), C.c_int()
+        _lib.check(self._lib.mhd_batch_info(self._h, C.byref(cap), C.byref(act)))
+        return cap.value, act.value
+
+    def add(self, nu: float, eta: float, dt: float) -> int:
+        s = C.c_int()
+        _lib.check(self._lib.mhd_batch_add(self._h, float(nu), float(eta), float(dt), C.byref(s)))
+        return s.value
+
+    def remove(self, slot: int):
+        _lib.check(self._lib.mhd_batch_remove(self._h, int(slot)))
+
+    def set_state(self, slot: int, sol_c):
+        a = np.ascontiguousarray(sol_c, dtype=np.complex64)
+        if a.shape != (6, self.n, self.n, self.nkr):
+            raise MHDError(_lib.MHD_ERR_INVALID, "state must be (6, n, n, nkr)")
+        _lib.check(self._lib.mhd_slot_set_state(self._h, int(slot), a.ctypes.data))
+
+    def get_state(self, slot: int):
+        out = np.empty((6, self.n, self.n, self.nkr), dtype=np.complex64)
+        _lib.check(self._lib.mhd_slot_get_state(self._h, int(slot), out.ctypes.data))
+        return out
+
+    def set_physical(self, slot: int, field: int, arr):
+        a = np.ascontiguousarray(arr, dtype=np.float32)
+        _lib.check(self._lib.mhd_slot_set_physical(self._h, int(slot), int(field), a.ctypes.data))
+
+    def get_physical(self, slot: int, field: int):
+        out = np.empty((self.n, self.n, self.n), dtype=np.float32)
+        _lib.check(self._lib.mhd_slot_get_physical(self._h, int(slot), int(field), out.ctypes.data))
+        return out
+
+    def diagnostics(self, slot: int):
+        out = (C.c_double * 8)()
+        rc = self._lib.mhd_slot_diagnostics(self._h, int(slot), out, 8)
+        if rc == _lib.MHD_ERR_NONFINITE:
+            raise MHDError(rc, self._lib.mhd_last_error().decode())
+        _lib.check(rc)
+        return Diagnostics(*list(out))
+
+    def clock(self, slot: int):
+        t, s, dt = C.c_double(), C.c_longlong(), C.c_double()
+        _lib.check(self._lib.mhd_slot_get_clock(self._h, int(slot), C.byref(t), C.byref(s), C.byref(dt)))
+        return t.value, s.value, dt.value
+
+    def step(self, nsteps: int = 1):
+        _lib.check(self._lib.mhd_step(self._h, int(nsteps)))
+
+    def synchronize(self):
+        _lib.check(self._lib.mhd_synchronize(self._h))
+
+    def memory_bytes(self):
+        b = C.c_longlong()
+        _lib.check(self._lib.mhd_memory_bytes(self._h, C.byref(b)))
+        return b.value
+
+
+class Ensemble:
+    """Size classes stepped together: one CUDA graph per step forks every member onto its own
+    stream, so boxes of different sizes advance concurrently."""
+
+    def __init__(self, batches):
+        self._lib = _lib.load()
+        self.batches = list(batches)
+        arr = (C.c_void_p * len(self.batches))(*[b.handle.value for b in self.batches])
+        e = C.c_void_p()
+        _lib.check(self._lib.mhd_ensemble_create(arr, len(self.batches), C.byref(e)))
+        self._e = e
+
+    def step(self, nsteps: int = 1):
+        _lib.check(self._lib.mhd_ensemble_step(self._e, int(nsteps)))
+
+    def synchronize(self):
+        for b in self.batches:
+            b.synchronize()
+
+    def close(self):
+        if getattr(self, "_e", None):
+            self._lib.mhd_ensemble_destroy(self._e)
+            self._e = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -75,6 +75,21 @@ _SIGS = {
     "mhd_kernel_class_bytes": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_double)]),
     "mhd_time_steps": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_double)]),
     "mhd_step_timed": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_double)]),
+    "mhd_batch_create": (C.c_int, [C.POINTER(MhdParams), C.c_int, C.POINTER(C.c_void_p)]),
+    "mhd_batch_add": (C.c_int, [C.c_void_p, C.c_double, C.c_double, C.c_double, C.POINTER(C.c_int)]),
+    "mhd_batch_remove": (C.c_int, [C.c_void_p, C.c_int]),
+    "mhd_batch_info": (C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
+    "mhd_slot_bytes": (C.c_int, [C.POINTER(MhdParams), C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)]),
+    "mhd_slot_set_state": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p]),
+    "mhd_slot_get_state": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p]),
+    "mhd_slot_set_physical": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_void_p]),
+    "mhd_slot_get_physical": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_void_p]),
+    "mhd_slot_diagnostics": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_double), C.c_int]),
+    "mhd_slot_get_clock": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_longlong), C.POINTER(C.c_double)]),
+    "mhd_slot_set_clock": (C.c_int, [C.c_void_p, C.c_int, C.c_double, C.c_longlong, C.c_double]),
+    "mhd_ensemble_create": (C.c_int, [C.POINTER(C.c_void_p), C.c_int, C.POINTER(C.c_void_p)]),
+    "mhd_ensemble_step": (C.c_int, [C.c_void_p, C.c_int]),
+    "mhd_ensemble_destroy": (C.c_int, [C.c_void_p]),
     "mhd_last_error": (C.c_char_p, []),
 }
 

@@ -48,23 +48,26 @@ int fail(int code, const std::string& msg) {
 // ------------------------------------------------------------------------------------------
 template <int N>
 struct Cfg;
-template <> struct Cfg<16>  { using C = Plan<16, 4, 4, 4>;       using R = Plan<16, 4, 4, 4>;       static constexpr int TX = 16, TXE = 16, ROWS = 32; };
-template <> struct Cfg<32>  { using C = Plan<32, 4, 8, 4>;       using R = Plan<32, 4, 8, 4>;       static constexpr int TX = 16, TXE = 16, ROWS = 32; };
-template <> struct Cfg<48>  { using C = Plan<48, 4, 12, 4>;      using R = Plan<48, 4, 12, 4>;      static constexpr int TX = 16, TXE = 16, ROWS = 32; };
-template <> struct Cfg<64>  { using C = Plan<64, 8, 8, 8>;       using R = Plan<64, 8, 8, 8>;       static constexpr int TX = 16, TXE = 16, ROWS = 16; };
-template <> struct Cfg<96>  { using C = Plan<96, 8, 12, 4, 2>;   using R = Plan<96, 8, 12, 4, 2>;   static constexpr int TX = 16, TXE = 16, ROWS = 16; };
-template <> struct Cfg<128> { using C = Plan<128, 8, 16, 8>;     using R = Plan<128, 16, 8, 4, 4>;  static constexpr int TX = 16, TXE = 16, ROWS = 8; };
-template <> struct Cfg<256> { using C = Plan<256, 16, 16, 16>;   using R = Plan<256, 32, 8, 8, 4>;  static constexpr int TX = 16, TXE = 16, ROWS = 4; };
-template <> struct Cfg<512> { using C = Plan<512, 32, 16, 8, 4>; using R = Plan<512, 64, 8, 8, 8>;  static constexpr int TX = 8, TXE = 8, ROWS = 2; };
+template <> struct Cfg<16>  { using C = Plan<16, 4, 4, 4>;       using R = Plan<16, 4, 4, 4>;       static constexpr int TX = 16, ROWS = 32; };
+template <> struct Cfg<32>  { using C = Plan<32, 4, 8, 4>;       using R = Plan<32, 4, 8, 4>;       static constexpr int TX = 16, ROWS = 32; };
+template <> struct Cfg<48>  { using C = Plan<48, 4, 12, 4>;      using R = Plan<48, 4, 12, 4>;      static constexpr int TX = 16, ROWS = 32; };
+template <> struct Cfg<64>  { using C = Plan<64, 8, 8, 8>;       using R = Plan<64, 8, 8, 8>;       static constexpr int TX = 16, ROWS = 16; };
+template <> struct Cfg<96>  { using C = Plan<96, 8, 12, 4, 2>;   using R = Plan<96, 8, 12, 4, 2>;   static constexpr int TX = 16, ROWS = 16; };
+template <> struct Cfg<128> { using C = Plan<128, 8, 16, 8>;     using R = Plan<128, 16, 8, 4, 4>;  static constexpr int TX = 16, ROWS = 8; };
+template <> struct Cfg<256> { using C = Plan<256, 16, 16, 16>;   using R = Plan<256, 32, 8, 8, 4>;  static constexpr int TX = 16, ROWS = 4; };
+template <> struct Cfg<512> { using C = Plan<512, 32, 16, 8, 4>; using R = Plan<512, 64, 8, 8, 8>;  static constexpr int TX = 16, ROWS = 2; };
 
 constexpr int kSlots = 8;
 
 struct OpsBase {
   virtual ~OpsBase() {}
   virtual int setup(const Geom& g) = 0;
-  virtual void col_inv(const ColArgs& a, const Geom& g, int outer, int nf, cudaStream_t s) = 0;
-  virtual void col_fwd(const ColArgs& a, const Geom& g, int outer, int nf, cudaStream_t s) = 0;
-  virtual void x_fused(float2* buf, const Geom& g, long long rowstride, long long slot, cudaStream_t s) = 0;
+  // cap: upper bound of the active instances (the grid covers cap instances; the kernels read
+  // the actual count from the BatchRef)
+  virtual void col_inv(const ColArgs& a, const Geom& g, int outer, int nf, BatchRef br, int cap, cudaStream_t s) = 0;
+  virtual void col_fwd(const ColArgs& a, const Geom& g, int outer, int nf, BatchRef br, int cap, cudaStream_t s) = 0;
+  virtual void x_fused(float2* pool, const Geom& g, long long rowstride, long long slot, long long istride, BatchRef br,
+                       int cap, cudaStream_t s) = 0;
   virtual void x_c2r(const float2* src, float* dst, const Geom& g, long long srow, float scale, cudaStream_t s) = 0;
   virtual void x_r2c(const float* src, float2* dst, const Geom& g, long long drow, cudaStream_t s) = 0;
 };
@@ -151,21 +154,24 @@ struct Ops : OpsBase {
     if ((rc = resident_ctas(x_fused_kernel<R, GROUPS>, GROUPS * XC::TPG, x_smem, &x_ctas))) return rc;
     return MHD_OK;
   }
-  void col_inv(const ColArgs& a, const Geom& g, int outer, int nf, cudaStream_t s) override {
+  void col_inv(const ColArgs& a, const Geom& g, int outer, int nf, BatchRef br, int cap, cudaStream_t s) override {
     ColWork w{(g.kx + TX - 1) / TX, outer, nf, g.k2};
-    const int total = w.tiles_x * w.outer * w.nf;
-    col_pass_kernel<C, TX, +1, true, false><<<total < col_inv_ctas ? total : col_inv_ctas, TX * C::G, kColSmem, s>>>(a, g, w, twC);
+    const long long total = (long long)cap * w.tiles_x * w.outer * w.nf;
+    const int grid = (int)(total < col_inv_ctas ? total : col_inv_ctas);
+    col_pass_kernel<C, TX, +1, true, false><<<grid, TX * C::G, kColSmem, s>>>(a, g, w, br, twC);
   }
-  void col_fwd(const ColArgs& a, const Geom& g, int outer, int nf, cudaStream_t s) override {
+  void col_fwd(const ColArgs& a, const Geom& g, int outer, int nf, BatchRef br, int cap, cudaStream_t s) override {
     ColWork w{(g.kx + TX - 1) / TX, outer, nf, N};
-    const int total = w.tiles_x * w.outer * w.nf;
-    col_pass_kernel<C, TX, -1, false, true><<<total < col_fwd_ctas ? total : col_fwd_ctas, TX * C::G, kColSmem, s>>>(a, g, w, twC);
+    const long long total = (long long)cap * w.tiles_x * w.outer * w.nf;
+    const int grid = (int)(total < col_fwd_ctas ? total : col_fwd_ctas);
+    col_pass_kernel<C, TX, -1, false, true><<<grid, TX * C::G, kColSmem, s>>>(a, g, w, br, twC);
   }
-  void x_fused(float2* buf, const Geom& g, long long rowstride, long long slot, cudaStream_t s) override {
-    const long long groups = (long long)N * N / XC::RPG;
+  void x_fused(float2* pool, const Geom& g, long long rowstride, long long slot, long long istride, BatchRef br, int cap,
+               cudaStream_t s) override {
+    const long long groups = (long long)cap * N * N / XC::RPG;
     const long long need = (groups + GROUPS - 1) / GROUPS;
     const int grid = (int)(need < x_ctas ? need : x_ctas);
-    x_fused_kernel<R, GROUPS><<<grid, GROUPS * XC::TPG, x_smem, s>>>(buf, g, rowstride, slot, twR, twRR);
+    x_fused_kernel<R, GROUPS><<<grid, GROUPS * XC::TPG, x_smem, s>>>(pool, g, rowstride, slot, istride, br, twR, twRR);
   }
   void x_c2r(const float2* src, float* dst, const Geom& g, long long srow, float scale, cudaStream_t s) override {
     constexpr int ROWS = Cfg<N>::ROWS;
@@ -230,9 +236,9 @@ const double kLsB[5] = {1432997174477.0 / 9575080441755.0, 5161836677717.0 / 136
 
 struct Sizes {
   long long fs;      // one compact field (complex)
-  long long state;   // six fields
-  long long colbuf;  // colbuf complex elements
-  long long rowbuf;  // rowbuf complex elements
+  long long state;   // six fields (slot stride of sol / xs / acc)
+  long long colbuf;  // colbuf complex elements per slot
+  long long rowbuf;  // rowbuf complex elements per slot
   long long ref;     // reference-layout sol (complex)
   long long phys;    // one physical field (floats)
   int diag_blocks;
@@ -251,42 +257,54 @@ Sizes sizes_of(const Geom& g) {
   return s;
 }
 
-long long footprint(const Geom& g) {
+// Device bytes of one slot (state, stage arrays, pass buffers) and of the per-class staging.
+long long slot_bytes(const Geom& g) {
   Sizes s = sizes_of(g);
-  long long bytes = 0;
-  bytes += 3 * s.state * 8;          // sol, stage state, accumulator
-  bytes += s.fs * 8;                 // aux (div B spectrum)
-  bytes += s.colbuf * 8 + s.rowbuf * 8;
-  bytes += s.ref * 8;                // reference-layout staging
-  bytes += s.phys * 4;               // physical staging
-  bytes += 6LL * g.n * 8;            // stage twiddle tables
-  bytes += (long long)s.diag_blocks * kDiagSlots * 8 + 16 * 8 + 64;
-  return bytes;
+  return (3 * s.state + s.fs + s.colbuf + s.rowbuf) * 8 + 16 * 4;
 }
+long long class_bytes(const Geom& g) {
+  Sizes s = sizes_of(g);
+  return s.ref * 8 + s.phys * 4 + 6LL * g.n * 8 + (long long)s.diag_blocks * kDiagSlots * 8 + 256;
+}
+long long footprint(const Geom& g, int cap) { return class_bytes(g) + (long long)cap * slot_bytes(g); }
 
 }  // namespace
 
+// A size class: `cap` slots of one grid size and scheme, stepped together.  The single-problem
+// API is the capacity-1 case with slot 0 active.
 struct mhd_problem {
   mhd_params p{};
   Geom g{};
   Sizes sz{};
+  int cap = 1;
   std::unique_ptr<OpsBase> ops;
   int device = 0;
   cudaStream_t own_stream = nullptr;
   cudaStream_t stream = nullptr;
+  // slot pools
   float2* sol = nullptr;
   float2* xs = nullptr;
   float2* acc = nullptr;
   float2* aux = nullptr;
   float2* colbuf = nullptr;
   float2* rowbuf = nullptr;
+  // per-class staging and reductions (one slot at a time)
   float2* ref = nullptr;
   float* phys = nullptr;
   double* diag_partial = nullptr;
   double* diag_out = nullptr;
   unsigned int* maxabs = nullptr;
-  double t = 0.0;
-  long long step = 0;
+  // work lists
+  SlotParams* dparams = nullptr;
+  int* dlist = nullptr;   // active slots, then the identity list (cap each), then counts
+  std::vector<SlotParams> hparams;
+  std::vector<char> used;
+  std::vector<int> active;
+  std::vector<double> t;
+  std::vector<long long> stepc;
+  bool list_dirty = true;
+  // step graph
+  cudaGraphExec_t graph = nullptr;
   // profiling
   bool profiling = false;
   struct Rec { int cls; cudaEvent_t a, b; };
@@ -299,16 +317,35 @@ struct mhd_problem {
 
   void release() {
     cudaSetDevice(device);
+    if (graph) cudaGraphExecDestroy(graph);
+    graph = nullptr;
     for (auto& r : recs) { cudaEventDestroy(r.a); cudaEventDestroy(r.b); }
     recs.clear();
     for (auto e : pool) cudaEventDestroy(e);
     pool.clear();
-    void* ptrs[] = {sol, xs, acc, aux, colbuf, rowbuf, ref, phys, diag_partial, diag_out, maxabs};
+    void* ptrs[] = {sol, xs, acc, aux, colbuf, rowbuf, ref, phys, diag_partial, diag_out, maxabs, dparams, dlist};
     for (void* q : ptrs) if (q) cudaFree(q);
     sol = xs = acc = aux = colbuf = rowbuf = ref = nullptr;
-    phys = nullptr; diag_partial = nullptr; diag_out = nullptr; maxabs = nullptr;
+    phys = nullptr; diag_partial = nullptr; diag_out = nullptr; maxabs = nullptr; dparams = nullptr; dlist = nullptr;
     if (own_stream) cudaStreamDestroy(own_stream);
     own_stream = nullptr;
+  }
+
+  // device work lists: dlist[0..cap) active, dlist[cap..2cap) identity, dlist[2cap] active count, dlist[2cap+1] = 1
+  BatchRef active_ref() const { return BatchRef{dlist, dlist + 2 * cap}; }
+  BatchRef slot_ref(int slot) const { return BatchRef{dlist + cap + slot, dlist + 2 * cap + 1}; }
+
+  int sync_lists() {
+    if (!list_dirty) return MHD_OK;
+    std::vector<int> h(2 * cap + 2, 0);
+    for (size_t i = 0; i < active.size(); ++i) h[i] = active[i];
+    for (int i = 0; i < cap; ++i) h[cap + i] = i;
+    h[2 * cap] = (int)active.size();
+    h[2 * cap + 1] = 1;
+    MHD_CUDA(cudaMemcpyAsync(dlist, h.data(), h.size() * sizeof(int), cudaMemcpyHostToDevice, stream));
+    MHD_CUDA(cudaMemcpyAsync(dparams, hparams.data(), hparams.size() * sizeof(SlotParams), cudaMemcpyHostToDevice, stream));
+    list_dirty = false;
+    return MHD_OK;
   }
 
   cudaEvent_t get_event() {
@@ -347,37 +384,39 @@ struct mhd_problem {
 
   // ---- strides (complex elements)
   long long FS() const { return sz.fs; }
+  long long ST() const { return sz.state; }
   long long AZ() const { return (long long)g.k2 * kSlots * g.kxp; }
   long long BZ() const { return (long long)g.n * kSlots * g.kxp; }
   long long SLK() const { return (long long)kSlots * g.kxp; }
 
-  // state (nf fields starting at src) -> colbuf slots 0..nf-1
-  int z_inverse(const float2* src, int nf) {
-    ColArgs a{src, colbuf, FS(), (long long)g.kxp, (long long)g.k2 * g.kxp, (long long)g.kxp, SLK(), AZ()};
-    return launch(KC_ZINV, [&] { ops->col_inv(a, g, g.k2, nf, stream); });
+  // compact fields (src + slot*sI, nf fields at stride FS) -> colbuf slots 0..nf-1
+  int z_inverse(const float2* src, long long sI, int nf, BatchRef br) {
+    ColArgs a{src, colbuf, FS(), (long long)g.kxp, (long long)g.k2 * g.kxp, (long long)g.kxp, SLK(), AZ(), sI, sz.colbuf};
+    return launch(KC_ZINV, [&] { ops->col_inv(a, g, g.k2, nf, br, cap, stream); });
   }
-  int y_inverse(int nf) {
-    ColArgs a{colbuf, rowbuf, (long long)g.kxp, AZ(), SLK(), (long long)g.kxp, BZ(), SLK()};
-    return launch(KC_YINV, [&] { ops->col_inv(a, g, g.n, nf, stream); });
+  int y_inverse(int nf, BatchRef br) {
+    ColArgs a{colbuf, rowbuf, (long long)g.kxp, AZ(), SLK(), (long long)g.kxp, BZ(), SLK(), sz.colbuf, sz.rowbuf};
+    return launch(KC_YINV, [&] { ops->col_inv(a, g, g.n, nf, br, cap, stream); });
   }
-  int x_fused() {
+  int x_fused(BatchRef br) {
     // the six field rows of a physical row are contiguous (slot stride == kxp)
-    return launch(KC_XFUSED, [&] { ops->x_fused(rowbuf, g, SLK(), g.kxp, stream); });
+    return launch(KC_XFUSED, [&] { ops->x_fused(rowbuf, g, SLK(), g.kxp, sz.rowbuf, br, cap, stream); });
   }
-  int y_forward(int nf) {
-    ColArgs a{rowbuf, colbuf, (long long)g.kxp, BZ(), SLK(), (long long)g.kxp, AZ(), SLK()};
-    return launch(KC_YFWD, [&] { ops->col_fwd(a, g, g.n, nf, stream); });
+  int y_forward(int nf, BatchRef br) {
+    ColArgs a{rowbuf, colbuf, (long long)g.kxp, BZ(), SLK(), (long long)g.kxp, AZ(), SLK(), sz.rowbuf, sz.colbuf};
+    return launch(KC_YFWD, [&] { ops->col_fwd(a, g, g.n, nf, br, cap, stream); });
   }
-  // colbuf slots -> compact planes (nf fields/products) of dst, pruned output
-  int z_forward(float2* dst, int nf) {
-    ColArgs a{colbuf, dst, (long long)g.kxp, SLK(), AZ(), FS(), (long long)g.kxp, (long long)g.k2 * g.kxp};
-    return launch(KC_ZFWD, [&] { ops->col_fwd(a, g, g.k2, nf, stream); });
+  // colbuf slots -> compact planes (nf fields/products) at dst + slot*dI, pruned output
+  int z_forward(float2* dst, long long dI, int nf, BatchRef br) {
+    ColArgs a{colbuf, dst, (long long)g.kxp, SLK(), AZ(), FS(), (long long)g.kxp, (long long)g.k2 * g.kxp, sz.colbuf, dI};
+    return launch(KC_ZFWD, [&] { ops->col_fwd(a, g, g.k2, nf, br, cap, stream); });
   }
   // Stage epilogue: RHS from the 8 compact product planes (in rowbuf) and the stage state X.
-  int epilogue(const float2* X, int op, float h, float ca, float cb) {
+  int epilogue(const float2* X, int op, float hf, float ca, float cb, BatchRef br) {
     int rc = launch(KC_HERM, [&] {
-      const int total = 6 * g.k2 * g.k2;
-      herm_kx0_kernel<<<(total + 255) / 256, 256, 0, stream>>>(X, aux, g, FS());
+      const long long total = (long long)cap * 6 * g.k2 * g.k2;
+      const long long blocks = (total + 255) / 256;
+      herm_kx0_kernel<<<(unsigned)(blocks < 4096 ? blocks : 4096), 256, 0, stream>>>(X, aux, g, FS(), ST(), FS(), br);
     });
     if (rc) return rc;
     RkArgs a{};
@@ -387,78 +426,103 @@ struct mhd_problem {
     a.sol = sol;
     a.acc = acc;
     a.xn = (op == OP_LS_FIRST || op == OP_LS) ? sol : xs;
+    a.sp = dparams;
     a.fs = FS();
-    a.nu = (float)p.nu;
-    a.eta = (float)p.eta;
-    a.h = h;
-    a.dt = (float)p.dt;
+    a.stI = ST();
+    a.prodI = sz.rowbuf;
+    a.hI = FS();
+    a.hf = hf;
     a.ca = ca;
     a.cb = cb;
     a.op = op;
     const double n3 = (double)g.n * g.n * g.n;
     a.pscale = (float)(1.0 / (n3 * n3));
     const int bx = g.kx <= 256 ? (g.kx + 31) / 32 * 32 : 256;
-    const dim3 grid((g.kx + bx - 1) / bx, g.k2, g.k2);
+    const dim3 grid((g.kx + bx - 1) / bx, g.k2, g.k2 * cap);
     return launch(KC_RKEPI, [&] {
       switch (op) {
-        case OP_RHS: rk_epilogue_kernel<OP_RHS><<<grid, bx, 0, stream>>>(a, g); break;
-        case OP_RK4_FIRST: rk_epilogue_kernel<OP_RK4_FIRST><<<grid, bx, 0, stream>>>(a, g); break;
-        case OP_RK4_MID: rk_epilogue_kernel<OP_RK4_MID><<<grid, bx, 0, stream>>>(a, g); break;
-        case OP_RK4_LAST: rk_epilogue_kernel<OP_RK4_LAST><<<grid, bx, 0, stream>>>(a, g); break;
-        case OP_LS_FIRST: rk_epilogue_kernel<OP_LS_FIRST><<<grid, bx, 0, stream>>>(a, g); break;
-        default: rk_epilogue_kernel<OP_LS><<<grid, bx, 0, stream>>>(a, g); break;
+        case OP_RHS: rk_epilogue_kernel<OP_RHS><<<grid, bx, 0, stream>>>(a, g, br); break;
+        case OP_RK4_FIRST: rk_epilogue_kernel<OP_RK4_FIRST><<<grid, bx, 0, stream>>>(a, g, br); break;
+        case OP_RK4_MID: rk_epilogue_kernel<OP_RK4_MID><<<grid, bx, 0, stream>>>(a, g, br); break;
+        case OP_RK4_LAST: rk_epilogue_kernel<OP_RK4_LAST><<<grid, bx, 0, stream>>>(a, g, br); break;
+        case OP_LS_FIRST: rk_epilogue_kernel<OP_LS_FIRST><<<grid, bx, 0, stream>>>(a, g, br); break;
+        default: rk_epilogue_kernel<OP_LS><<<grid, bx, 0, stream>>>(a, g, br); break;
       }
     });
   }
-  int epilogues(const float2* X, int op, float h, float ca, float cb) {
+  int rhs(const float2* X, int op, float hf, float ca, float cb, BatchRef br) {
     int rc;
-    if ((rc = z_forward(rowbuf, kSlots))) return rc;
-    return epilogue(X, op, h, ca, cb);
+    if ((rc = z_inverse(X, ST(), 6, br))) return rc;
+    if ((rc = y_inverse(6, br))) return rc;
+    if ((rc = x_fused(br))) return rc;
+    if ((rc = y_forward(kSlots, br))) return rc;
+    if ((rc = z_forward(rowbuf, sz.rowbuf, kSlots, br))) return rc;
+    return epilogue(X, op, hf, ca, cb, br);
   }
-  int rhs_passes(const float2* X) {
+  // One step of every active slot (launches only; see run_steps for graphs and clocks).
+  int issue_step() {
+    const BatchRef br = active_ref();
     int rc;
-    if ((rc = z_inverse(X, 6))) return rc;
-    if ((rc = y_inverse(6))) return rc;
-    if ((rc = x_fused())) return rc;
-    if ((rc = y_forward(kSlots))) return rc;
+    if (p.scheme == MHD_RK4) {
+      if ((rc = rhs(sol, OP_RK4_FIRST, 0.5f, 0.f, 0.f, br))) return rc;
+      if ((rc = rhs(xs, OP_RK4_MID, 0.5f, 0.f, 0.f, br))) return rc;
+      if ((rc = rhs(xs, OP_RK4_MID, 1.0f, 0.f, 0.f, br))) return rc;
+      return rhs(xs, OP_RK4_LAST, 0.f, 0.f, 0.f, br);
+    }
+    for (int i = 0; i < 5; ++i)
+      if ((rc = rhs(sol, i == 0 ? OP_LS_FIRST : OP_LS, 0.f, (float)kLsA[i], (float)kLsB[i], br))) return rc;
     return MHD_OK;
   }
-  int step_rk4() {
-    const float dtf = (float)p.dt;
-    const float half = dtf / 2.0f;
-    int rc;
-    if ((rc = rhs_passes(sol))) return rc;
-    if ((rc = epilogues(sol, OP_RK4_FIRST, half, 0.f, 0.f))) return rc;
-    if ((rc = rhs_passes(xs))) return rc;
-    if ((rc = epilogues(xs, OP_RK4_MID, half, 0.f, 0.f))) return rc;
-    if ((rc = rhs_passes(xs))) return rc;
-    if ((rc = epilogues(xs, OP_RK4_MID, dtf, 0.f, 0.f))) return rc;
-    if ((rc = rhs_passes(xs))) return rc;
-    if ((rc = epilogues(xs, OP_RK4_LAST, 0.f, 0.f, 0.f))) return rc;
+  int build_graph() {
+    if (graph) return MHD_OK;
+    cudaGraph_t gr = nullptr;
+    MHD_CUDA(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+    int rc = issue_step();
+    cudaError_t e = cudaStreamEndCapture(stream, &gr);
+    if (rc) { if (gr) cudaGraphDestroy(gr); return rc; }
+    if (e != cudaSuccess) return fail(MHD_ERR_CUDA, std::string("cudaStreamEndCapture: ") + cudaGetErrorString(e));
+    e = cudaGraphInstantiate(&graph, gr, 0);
+    cudaGraphDestroy(gr);
+    if (e != cudaSuccess) { graph = nullptr; return fail(MHD_ERR_CUDA, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(e)); }
     return MHD_OK;
   }
-  int step_lsrk4() {
+  void advance_clocks() {
+    for (int s : active) { t[s] += hparams[s].dt; stepc[s] += 1; }
+  }
+  int run_steps(int nsteps) {
     int rc;
-    for (int i = 0; i < 5; ++i) {
-      if ((rc = rhs_passes(sol))) return rc;
-      if ((rc = epilogues(sol, i == 0 ? OP_LS_FIRST : OP_LS, 0.f, (float)kLsA[i], (float)kLsB[i]))) return rc;
+    if ((rc = sync_lists())) return rc;
+    if (active.empty()) return MHD_OK;
+    if (!profiling && (rc = build_graph())) return rc;
+    for (int i = 0; i < nsteps; ++i) {
+      if (profiling) {
+        if ((rc = issue_step())) return rc;
+      } else {
+        MHD_CUDA(cudaGraphLaunch(graph, stream));
+      }
+      advance_clocks();
     }
     return MHD_OK;
   }
-  // One field: compact (src, field slot) -> physical staging (normalised inverse).
-  int inverse_field(const float2* src) {
+  // One field of one slot: compact (src) -> physical staging, normalised inverse.
+  int inverse_field(const float2* src, long long sI, int slot) {
     int rc;
-    if ((rc = z_inverse(src, 1))) return rc;
-    if ((rc = y_inverse(1))) return rc;
-    return launch(KC_OTHER, [&] { ops->x_c2r(rowbuf, phys, g, SLK(), (float)(1.0 / ((double)g.n * g.n * g.n)), stream); });
+    const BatchRef br = slot_ref(slot);
+    if ((rc = z_inverse(src, sI, 1, br))) return rc;
+    if ((rc = y_inverse(1, br))) return rc;
+    float2* rb = rowbuf + slot * sz.rowbuf;
+    return launch(KC_OTHER, [&] { ops->x_c2r(rb, phys, g, SLK(), (float)(1.0 / ((double)g.n * g.n * g.n)), stream); });
   }
-  // One field: physical staging -> compact dst (unnormalised forward).
-  int forward_field(float2* dst) {
+  // One field of one slot: physical staging -> compact (dst + slot*dI), unnormalised forward.
+  int forward_field(float2* dst, long long dI, int slot) {
     int rc;
-    if ((rc = launch(KC_OTHER, [&] { ops->x_r2c(phys, rowbuf, g, SLK(), stream); }))) return rc;
-    if ((rc = y_forward(1))) return rc;
-    return z_forward(dst, 1);
+    const BatchRef br = slot_ref(slot);
+    float2* rb = rowbuf + slot * sz.rowbuf;
+    if ((rc = launch(KC_OTHER, [&] { ops->x_r2c(phys, rb, g, SLK(), stream); }))) return rc;
+    if ((rc = y_forward(1, br))) return rc;
+    return z_forward(dst, dI, 1, br);
   }
+  bool valid_slot(int s) const { return s >= 0 && s < cap && used[s]; }
 };
 
 namespace {
@@ -470,6 +534,13 @@ int check_handle(mhd_handle h) {
   return MHD_OK;
 }
 
+int check_slot(mhd_handle h, int slot) {
+  int rc = check_handle(h);
+  if (rc) return rc;
+  if (!h->valid_slot(slot)) return fail(MHD_ERR_INVALID, "slot " + std::to_string(slot) + " is not active");
+  return h->sync_lists();
+}
+
 int validate(const mhd_params* p) {
   if (!p) return fail(MHD_ERR_INVALID, "null params");
   if (!supported(p->n)) return fail(MHD_ERR_INVALID, "unsupported grid size n=" + std::to_string(p->n) + " (supported: 16,32,48,64,96,128,256,512)");
@@ -479,6 +550,75 @@ int validate(const mhd_params* p) {
   if (!std::isfinite(p->dt)) return fail(MHD_ERR_INVALID, "dt must be finite");
   if (p->scheme != MHD_RK4 && p->scheme != MHD_LSRK4) return fail(MHD_ERR_INVALID, "scheme must be MHD_RK4 or MHD_LSRK4");
   if (p->precision != MHD_PREC_FP32) return fail(MHD_ERR_INVALID, "only MHD_PREC_FP32 is available");
+  return MHD_OK;
+}
+
+int create_class(const mhd_params* params, int cap, mhd_handle* out) {
+  g_err.clear();
+  if (!out) return fail(MHD_ERR_INVALID, "null output handle");
+  *out = nullptr;
+  int rc = validate(params);
+  if (rc) return rc;
+  if (cap < 1 || cap > 4096) return fail(MHD_ERR_INVALID, "capacity must be 1..4096");
+  {
+    const Geom g0 = make_geom(params->n, params->L);
+    if ((long long)g0.k2 * cap > 65535) return fail(MHD_ERR_INVALID, "capacity too large for this grid size");
+  }
+  std::unique_ptr<mhd_problem> h(new (std::nothrow) mhd_problem());
+  if (!h) return fail(MHD_ERR_OOM, "host allocation failed");
+  h->p = *params;
+  h->cap = cap;
+  h->device = params->device;
+  MHD_CUDA(cudaSetDevice(h->device));
+  h->g = make_geom(params->n, params->L);
+  h->sz = sizes_of(h->g);
+  h->ops.reset(make_ops(params->n));
+  if (!h->ops) return fail(MHD_ERR_INVALID, "no plan for n");
+  if ((rc = h->ops->setup(h->g))) return rc;
+  MHD_CUDA(cudaStreamCreateWithFlags(&h->own_stream, cudaStreamNonBlocking));
+  h->stream = h->own_stream;
+  const Sizes& s = h->sz;
+  const size_t c = (size_t)cap;
+  MHD_CUDA(cudaMalloc(&h->sol, c * s.state * sizeof(float2)));
+  MHD_CUDA(cudaMalloc(&h->xs, c * s.state * sizeof(float2)));
+  MHD_CUDA(cudaMalloc(&h->acc, c * s.state * sizeof(float2)));
+  MHD_CUDA(cudaMalloc(&h->aux, c * s.fs * sizeof(float2)));
+  MHD_CUDA(cudaMalloc(&h->colbuf, c * s.colbuf * sizeof(float2)));
+  MHD_CUDA(cudaMalloc(&h->rowbuf, c * s.rowbuf * sizeof(float2)));
+  MHD_CUDA(cudaMalloc(&h->ref, s.ref * sizeof(float2)));
+  MHD_CUDA(cudaMalloc(&h->phys, s.phys * sizeof(float)));
+  MHD_CUDA(cudaMalloc(&h->diag_partial, (size_t)s.diag_blocks * kDiagSlots * sizeof(double)));
+  MHD_CUDA(cudaMalloc(&h->diag_out, 16 * sizeof(double)));
+  MHD_CUDA(cudaMalloc(&h->maxabs, 16 * sizeof(unsigned int)));
+  MHD_CUDA(cudaMalloc(&h->dparams, c * sizeof(SlotParams)));
+  MHD_CUDA(cudaMalloc(&h->dlist, (2 * c + 2) * sizeof(int)));
+  MHD_CUDA(cudaMemsetAsync(h->sol, 0, c * s.state * sizeof(float2), h->stream));
+  MHD_CUDA(cudaMemsetAsync(h->xs, 0, c * s.state * sizeof(float2), h->stream));
+  MHD_CUDA(cudaMemsetAsync(h->acc, 0, c * s.state * sizeof(float2), h->stream));
+  h->hparams.assign(cap, SlotParams{0.f, 0.f, 0.f, 0.f});
+  h->used.assign(cap, 0);
+  h->t.assign(cap, 0.0);
+  h->stepc.assign(cap, 0);
+  h->list_dirty = true;
+  if ((rc = h->sync_lists())) return rc;
+  MHD_CUDA(cudaStreamSynchronize(h->stream));
+  *out = h.release();
+  return MHD_OK;
+}
+
+int add_slot(mhd_handle h, double nu, double eta, double dt, int* slot) {
+  if (!(nu >= 0) || !(eta >= 0) || !std::isfinite(dt)) return fail(MHD_ERR_INVALID, "nu, eta >= 0 and finite dt required");
+  int s = -1;
+  for (int i = 0; i < h->cap; ++i) if (!h->used[i]) { s = i; break; }
+  if (s < 0) return fail(MHD_ERR_STATE, "size class is full (capacity " + std::to_string(h->cap) + ")");
+  h->used[s] = 1;
+  h->active.push_back(s);
+  h->hparams[s] = SlotParams{(float)nu, (float)eta, (float)dt, 0.f};
+  h->t[s] = 0.0;
+  h->stepc[s] = 0;
+  h->list_dirty = true;
+  MHD_CUDA(cudaMemsetAsync(h->sol + s * h->sz.state, 0, h->sz.state * sizeof(float2), h->stream));
+  if (slot) *slot = s;
   return MHD_OK;
 }
 
@@ -500,46 +640,32 @@ int mhd_footprint_bytes(const mhd_params* params, long long* bytes) {
   int rc = validate(params);
   if (rc) return rc;
   if (!bytes) return fail(MHD_ERR_INVALID, "null output");
-  *bytes = footprint(make_geom(params->n, params->L));
+  *bytes = footprint(make_geom(params->n, params->L), 1);
+  return MHD_OK;
+}
+
+int mhd_slot_bytes(const mhd_params* params, long long* per_slot, long long* per_class) {
+  int rc = validate(params);
+  if (rc) return rc;
+  const Geom g = make_geom(params->n, params->L);
+  if (per_slot) *per_slot = slot_bytes(g);
+  if (per_class) *per_class = class_bytes(g);
   return MHD_OK;
 }
 
 int mhd_create(const mhd_params* params, mhd_handle* out) {
-  g_err.clear();
-  if (!out) return fail(MHD_ERR_INVALID, "null output handle");
-  *out = nullptr;
-  int rc = validate(params);
+  int rc = create_class(params, 1, out);
   if (rc) return rc;
-  std::unique_ptr<mhd_problem> h(new (std::nothrow) mhd_problem());
-  if (!h) return fail(MHD_ERR_OOM, "host allocation failed");
-  h->p = *params;
-  h->device = params->device;
-  MHD_CUDA(cudaSetDevice(h->device));
-  h->g = make_geom(params->n, params->L);
-  h->sz = sizes_of(h->g);
-  h->ops.reset(make_ops(params->n));
-  if (!h->ops) return fail(MHD_ERR_INVALID, "no plan for n");
-  if ((rc = h->ops->setup(h->g))) return rc;
-  MHD_CUDA(cudaStreamCreateWithFlags(&h->own_stream, cudaStreamNonBlocking));
-  h->stream = h->own_stream;
-  const Sizes& s = h->sz;
-  MHD_CUDA(cudaMalloc(&h->sol, s.state * sizeof(float2)));
-  MHD_CUDA(cudaMalloc(&h->xs, s.state * sizeof(float2)));
-  MHD_CUDA(cudaMalloc(&h->acc, s.state * sizeof(float2)));
-  MHD_CUDA(cudaMalloc(&h->aux, s.fs * sizeof(float2)));
-  MHD_CUDA(cudaMalloc(&h->colbuf, s.colbuf * sizeof(float2)));
-  MHD_CUDA(cudaMalloc(&h->rowbuf, s.rowbuf * sizeof(float2)));
-  MHD_CUDA(cudaMalloc(&h->ref, s.ref * sizeof(float2)));
-  MHD_CUDA(cudaMalloc(&h->phys, s.phys * sizeof(float)));
-  MHD_CUDA(cudaMalloc(&h->diag_partial, (size_t)s.diag_blocks * kDiagSlots * sizeof(double)));
-  MHD_CUDA(cudaMalloc(&h->diag_out, 16 * sizeof(double)));
-  MHD_CUDA(cudaMalloc(&h->maxabs, 16 * sizeof(unsigned int)));
-  MHD_CUDA(cudaMemsetAsync(h->sol, 0, s.state * sizeof(float2), h->stream));
-  MHD_CUDA(cudaMemsetAsync(h->xs, 0, s.state * sizeof(float2), h->stream));
-  MHD_CUDA(cudaMemsetAsync(h->acc, 0, s.state * sizeof(float2), h->stream));
-  MHD_CUDA(cudaStreamSynchronize(h->stream));
-  *out = h.release();
-  return MHD_OK;
+  if ((rc = add_slot(*out, params->nu, params->eta, params->dt, nullptr))) {
+    delete *out;
+    *out = nullptr;
+    return rc;
+  }
+  return (*out)->sync_lists();
+}
+
+int mhd_batch_create(const mhd_params* params, int capacity, mhd_handle* out) {
+  return create_class(params, capacity, out);
 }
 
 int mhd_destroy(mhd_handle h) {
@@ -550,99 +676,107 @@ int mhd_destroy(mhd_handle h) {
   return MHD_OK;
 }
 
-int mhd_set_state(mhd_handle h, const float* sol) {
+int mhd_batch_add(mhd_handle h, double nu, double eta, double dt, int* slot) {
   int rc = check_handle(h);
+  if (rc) return rc;
+  return add_slot(h, nu, eta, dt, slot);
+}
+
+int mhd_batch_remove(mhd_handle h, int slot) {
+  int rc = check_handle(h);
+  if (rc) return rc;
+  if (!h->valid_slot(slot)) return fail(MHD_ERR_INVALID, "slot " + std::to_string(slot) + " is not active");
+  h->used[slot] = 0;
+  for (size_t i = 0; i < h->active.size(); ++i)
+    if (h->active[i] == slot) { h->active.erase(h->active.begin() + i); break; }
+  h->list_dirty = true;
+  return MHD_OK;
+}
+
+int mhd_batch_info(mhd_handle h, int* capacity, int* active) {
+  if (!h) return fail(MHD_ERR_INVALID, "null handle");
+  if (capacity) *capacity = h->cap;
+  if (active) *active = (int)h->active.size();
+  return MHD_OK;
+}
+
+int mhd_slot_set_state(mhd_handle h, int slot, const float* sol) {
+  int rc = check_slot(h, slot);
   if (rc) return rc;
   if (!sol) return fail(MHD_ERR_INVALID, "null sol");
   MHD_CUDA(cudaMemcpyAsync(h->ref, sol, h->sz.ref * sizeof(float2), cudaMemcpyHostToDevice, h->stream));
-  if ((rc = h->launch(KC_OTHER, [&] { gather_state_kernel<<<1216, 256, 0, h->stream>>>(h->ref, h->sol, h->g, 6); }))) return rc;
+  float2* dst = h->sol + slot * h->sz.state;
+  if ((rc = h->launch(KC_OTHER, [&] { gather_state_kernel<<<1216, 256, 0, h->stream>>>(h->ref, dst, h->g, 6); }))) return rc;
   MHD_CUDA(cudaStreamSynchronize(h->stream));
   return MHD_OK;
 }
 
-int mhd_get_state(mhd_handle h, float* sol) {
-  int rc = check_handle(h);
+int mhd_slot_get_state(mhd_handle h, int slot, float* sol) {
+  int rc = check_slot(h, slot);
   if (rc) return rc;
   if (!sol) return fail(MHD_ERR_INVALID, "null sol");
-  if ((rc = h->launch(KC_OTHER, [&] { scatter_state_kernel<<<1216, 256, 0, h->stream>>>(h->sol, h->ref, h->g, 6); }))) return rc;
+  const float2* src = h->sol + slot * h->sz.state;
+  if ((rc = h->launch(KC_OTHER, [&] { scatter_state_kernel<<<1216, 256, 0, h->stream>>>(src, h->ref, h->g, 6); }))) return rc;
   MHD_CUDA(cudaMemcpyAsync(sol, h->ref, h->sz.ref * sizeof(float2), cudaMemcpyDeviceToHost, h->stream));
   MHD_CUDA(cudaStreamSynchronize(h->stream));
   return MHD_OK;
 }
 
-int mhd_set_physical(mhd_handle h, int field, const float* phys) {
-  int rc = check_handle(h);
+int mhd_slot_set_physical(mhd_handle h, int slot, int field, const float* phys) {
+  int rc = check_slot(h, slot);
   if (rc) return rc;
   if (field < 0 || field > 5) return fail(MHD_ERR_INVALID, "field must be 0..5 (ux uy uz bx by bz)");
   if (!phys) return fail(MHD_ERR_INVALID, "null field array");
   MHD_CUDA(cudaMemcpyAsync(h->phys, phys, h->sz.phys * sizeof(float), cudaMemcpyHostToDevice, h->stream));
-  if ((rc = h->forward_field(h->sol + field * h->sz.fs))) return rc;
+  if ((rc = h->forward_field(h->sol + field * h->sz.fs, h->sz.state, slot))) return rc;
   MHD_CUDA(cudaStreamSynchronize(h->stream));
   return MHD_OK;
 }
 
-int mhd_get_physical(mhd_handle h, int field, float* phys) {
-  int rc = check_handle(h);
+int mhd_slot_get_physical(mhd_handle h, int slot, int field, float* phys) {
+  int rc = check_slot(h, slot);
   if (rc) return rc;
   if (field < 0 || field > 5) return fail(MHD_ERR_INVALID, "field must be 0..5 (ux uy uz bx by bz)");
   if (!phys) return fail(MHD_ERR_INVALID, "null field array");
-  if ((rc = h->inverse_field(h->sol + field * h->sz.fs))) return rc;
+  if ((rc = h->inverse_field(h->sol + field * h->sz.fs, h->sz.state, slot))) return rc;
   MHD_CUDA(cudaMemcpyAsync(phys, h->phys, h->sz.phys * sizeof(float), cudaMemcpyDeviceToHost, h->stream));
   MHD_CUDA(cudaStreamSynchronize(h->stream));
   return MHD_OK;
 }
 
-int mhd_step(mhd_handle h, int nsteps) {
-  int rc = check_handle(h);
-  if (rc) return rc;
-  if (nsteps < 0) return fail(MHD_ERR_INVALID, "nsteps must be >= 0");
-  for (int i = 0; i < nsteps; ++i) {
-    rc = h->p.scheme == MHD_RK4 ? h->step_rk4() : h->step_lsrk4();
-    if (rc) return rc;
-    h->t += h->p.dt;
-    h->step += 1;
+int mhd_slot_get_clock(mhd_handle h, int slot, double* t, long long* step, double* dt) {
+  if (!h) return fail(MHD_ERR_INVALID, "null handle");
+  if (!h->valid_slot(slot)) return fail(MHD_ERR_INVALID, "slot " + std::to_string(slot) + " is not active");
+  if (t) *t = h->t[slot];
+  if (step) *step = h->stepc[slot];
+  if (dt) *dt = h->hparams[slot].dt;
+  return MHD_OK;
+}
+
+int mhd_slot_set_clock(mhd_handle h, int slot, double t, long long step, double dt) {
+  if (!h) return fail(MHD_ERR_INVALID, "null handle");
+  if (!h->valid_slot(slot)) return fail(MHD_ERR_INVALID, "slot " + std::to_string(slot) + " is not active");
+  if (!std::isfinite(t) || !std::isfinite(dt)) return fail(MHD_ERR_INVALID, "t and dt must be finite");
+  h->t[slot] = t;
+  h->stepc[slot] = step;
+  if ((float)dt != h->hparams[slot].dt) {
+    h->hparams[slot].dt = (float)dt;
+    h->list_dirty = true;
   }
   return MHD_OK;
 }
 
-int mhd_compute_rhs(mhd_handle h, float* rhs_out) {
-  int rc = check_handle(h);
-  if (rc) return rc;
-  if (!rhs_out) return fail(MHD_ERR_INVALID, "null output");
-  if ((rc = h->rhs_passes(h->sol))) return rc;
-  if ((rc = h->epilogues(h->sol, OP_RHS, 0.f, 0.f, 0.f))) return rc;
-  if ((rc = h->launch(KC_OTHER, [&] { scatter_state_kernel<<<1216, 256, 0, h->stream>>>(h->acc, h->ref, h->g, 6); }))) return rc;
-  MHD_CUDA(cudaMemcpyAsync(rhs_out, h->ref, h->sz.ref * sizeof(float2), cudaMemcpyDeviceToHost, h->stream));
-  MHD_CUDA(cudaStreamSynchronize(h->stream));
-  return MHD_OK;
-}
-
-int mhd_get_clock(mhd_handle h, double* t, long long* step, double* dt) {
-  if (!h) return fail(MHD_ERR_INVALID, "null handle");
-  if (t) *t = h->t;
-  if (step) *step = h->step;
-  if (dt) *dt = h->p.dt;
-  return MHD_OK;
-}
-
-int mhd_set_clock(mhd_handle h, double t, long long step, double dt) {
-  if (!h) return fail(MHD_ERR_INVALID, "null handle");
-  if (!std::isfinite(t) || !std::isfinite(dt)) return fail(MHD_ERR_INVALID, "t and dt must be finite");
-  h->t = t;
-  h->step = step;
-  h->p.dt = dt;
-  return MHD_OK;
-}
-
-int mhd_diagnostics(mhd_handle h, double* out, int nout) {
-  int rc = check_handle(h);
+int mhd_slot_diagnostics(mhd_handle h, int slot, double* out, int nout) {
+  int rc = check_slot(h, slot);
   if (rc) return rc;
   if (!out || nout < 8) return fail(MHD_ERR_INVALID, "diagnostics needs an output array of >= 8 doubles");
   const Sizes& s = h->sz;
-  if ((rc = h->launch(KC_OTHER, [&] { diag_partial_kernel<<<s.diag_blocks, kDiagThreads, 0, h->stream>>>(h->sol, h->g, h->diag_partial); }))) return rc;
+  const float2* st = h->sol + slot * s.state;
+  float2* aux = h->aux + slot * s.fs;
+  if ((rc = h->launch(KC_OTHER, [&] { diag_partial_kernel<<<s.diag_blocks, kDiagThreads, 0, h->stream>>>(st, h->g, h->diag_partial); }))) return rc;
   if ((rc = h->launch(KC_OTHER, [&] { diag_final_kernel<<<1, kDiagThreads, 0, h->stream>>>(h->diag_partial, s.diag_blocks, h->diag_out); }))) return rc;
-  if ((rc = h->launch(KC_OTHER, [&] { divb_spectrum_kernel<<<1216, 256, 0, h->stream>>>(h->sol, h->aux, h->g); }))) return rc;
-  if ((rc = h->inverse_field(h->aux))) return rc;
+  if ((rc = h->launch(KC_OTHER, [&] { divb_spectrum_kernel<<<1216, 256, 0, h->stream>>>(st, aux, h->g); }))) return rc;
+  if ((rc = h->inverse_field(h->aux, s.fs, slot))) return rc;
   MHD_CUDA(cudaMemsetAsync(h->maxabs, 0, sizeof(unsigned int), h->stream));
   if ((rc = h->launch(KC_OTHER, [&] { maxabs_kernel<<<1216, 256, 0, h->stream>>>(h->phys, s.phys, h->maxabs); }))) return rc;
   double d[kDiagSlots];
@@ -662,8 +796,35 @@ int mhd_diagnostics(mhd_handle h, double* out, int nout) {
   out[4] = d[4];
   out[5] = (double)mxf;
   out[6] = d[5];
-  out[7] = h->t;
+  out[7] = h->t[slot];
   if (d[5] > 0 || !std::isfinite(out[0]) || !std::isfinite(out[1])) return fail(MHD_ERR_NONFINITE, "detected NaN! Quit the simulation right now.");
+  return MHD_OK;
+}
+
+// ---- single-problem API (slot 0)
+int mhd_set_state(mhd_handle h, const float* sol) { return mhd_slot_set_state(h, 0, sol); }
+int mhd_get_state(mhd_handle h, float* sol) { return mhd_slot_get_state(h, 0, sol); }
+int mhd_set_physical(mhd_handle h, int field, const float* phys) { return mhd_slot_set_physical(h, 0, field, phys); }
+int mhd_get_physical(mhd_handle h, int field, float* phys) { return mhd_slot_get_physical(h, 0, field, phys); }
+int mhd_get_clock(mhd_handle h, double* t, long long* step, double* dt) { return mhd_slot_get_clock(h, 0, t, step, dt); }
+int mhd_set_clock(mhd_handle h, double t, long long step, double dt) { return mhd_slot_set_clock(h, 0, t, step, dt); }
+int mhd_diagnostics(mhd_handle h, double* out, int nout) { return mhd_slot_diagnostics(h, 0, out, nout); }
+
+int mhd_step(mhd_handle h, int nsteps) {
+  int rc = check_handle(h);
+  if (rc) return rc;
+  if (nsteps < 0) return fail(MHD_ERR_INVALID, "nsteps must be >= 0");
+  return h->run_steps(nsteps);
+}
+
+int mhd_compute_rhs(mhd_handle h, float* rhs_out) {
+  int rc = check_slot(h, 0);
+  if (rc) return rc;
+  if (!rhs_out) return fail(MHD_ERR_INVALID, "null output");
+  if ((rc = h->rhs(h->sol, OP_RHS, 0.f, 0.f, 0.f, h->slot_ref(0)))) return rc;
+  if ((rc = h->launch(KC_OTHER, [&] { scatter_state_kernel<<<1216, 256, 0, h->stream>>>(h->acc, h->ref, h->g, 6); }))) return rc;
+  MHD_CUDA(cudaMemcpyAsync(rhs_out, h->ref, h->sz.ref * sizeof(float2), cudaMemcpyDeviceToHost, h->stream));
+  MHD_CUDA(cudaStreamSynchronize(h->stream));
   return MHD_OK;
 }
 
@@ -684,7 +845,7 @@ void* mhd_get_stream(mhd_handle h) { return h ? (void*)h->stream : nullptr; }
 
 int mhd_memory_bytes(mhd_handle h, long long* bytes) {
   if (!h || !bytes) return fail(MHD_ERR_INVALID, "null argument");
-  *bytes = footprint(h->g);
+  *bytes = footprint(h->g, h->cap);
   return MHD_OK;
 }
 
@@ -730,6 +891,7 @@ int mhd_kernel_class_count(void) { return KC_COUNT; }
 int mhd_kernel_class_bytes(mhd_handle h, int cls, double* bytes) {
   if (!h || !bytes) return fail(MHD_ERR_INVALID, "null argument");
   const double n = h->g.n, kx = h->g.kx, k2 = h->g.k2, c = 8.0;
+  const double inst = (double)(h->active.empty() ? 1 : h->active.size());
   const double state_field = k2 * k2 * kx * c;
   double b = 0;
   // state arrays (6 fields each) one epilogue launch touches, averaged over the scheme's stages
@@ -744,7 +906,7 @@ int mhd_kernel_class_bytes(mhd_handle h, int cls, double* bytes) {
     case KC_HERM: b = 2 * 6 * k2 * k2 * c; break;
     default: b = 0;
   }
-  *bytes = b;
+  *bytes = b * inst;
   return MHD_OK;
 }
 
@@ -752,11 +914,13 @@ int mhd_step_timed(mhd_handle h, int nsteps, double* ms_per_step) {
   int rc = check_handle(h);
   if (rc) return rc;
   if (nsteps < 1 || !ms_per_step) return fail(MHD_ERR_INVALID, "nsteps >= 1 and a non-null output are required");
+  if ((rc = h->sync_lists())) return rc;
+  if (!h->profiling && (rc = h->build_graph())) return rc;
   std::vector<cudaEvent_t> ev(nsteps + 1);
   for (auto& e : ev) MHD_CUDA(cudaEventCreate(&e));
   cudaEventRecord(ev[0], h->stream);
   for (int i = 0; i < nsteps && rc == MHD_OK; ++i) {
-    rc = mhd_step(h, 1);
+    rc = h->run_steps(1);
     cudaEventRecord(ev[i + 1], h->stream);
   }
   cudaError_t e = cudaEventSynchronize(ev[nsteps]);
@@ -775,11 +939,13 @@ int mhd_time_steps(mhd_handle h, int nsteps, double* ms) {
   int rc = check_handle(h);
   if (rc) return rc;
   if (!ms) return fail(MHD_ERR_INVALID, "null output");
+  if ((rc = h->sync_lists())) return rc;
+  if (!h->profiling && (rc = h->build_graph())) return rc;
   cudaEvent_t a, b;
   MHD_CUDA(cudaEventCreate(&a));
   MHD_CUDA(cudaEventCreate(&b));
   cudaEventRecord(a, h->stream);
-  rc = mhd_step(h, nsteps);
+  rc = h->run_steps(nsteps);
   cudaEventRecord(b, h->stream);
   cudaError_t e = cudaEventSynchronize(b);
   float f = 0.f;
@@ -789,6 +955,102 @@ int mhd_time_steps(mhd_handle h, int nsteps, double* ms) {
   if (rc) return rc;
   if (e != cudaSuccess) return fail(MHD_ERR_CUDA, std::string("cudaEventSynchronize: ") + cudaGetErrorString(e));
   *ms = f;
+  return MHD_OK;
+}
+
+}  // extern "C"
+
+// ------------------------------------------------------------------------------------------
+// Ensembles: several size classes stepped concurrently.  One step of every class is captured
+// into a single CUDA graph: the classes fork onto their own streams and join on the first one,
+// so small boxes run alongside large ones instead of one class after another.
+// ------------------------------------------------------------------------------------------
+struct mhd_ensemble_s {
+  std::vector<mhd_handle> hs;
+  cudaGraphExec_t graph = nullptr;
+  std::vector<cudaEvent_t> evs;
+  ~mhd_ensemble_s() {
+    if (graph) cudaGraphExecDestroy(graph);
+    for (auto e : evs) cudaEventDestroy(e);
+  }
+};
+
+extern "C" {
+
+int mhd_ensemble_create(mhd_handle* hs, int nh, mhd_ensemble* out) {
+  if (!out || !hs || nh < 1) return fail(MHD_ERR_INVALID, "need >= 1 handles and an output");
+  *out = nullptr;
+  for (int i = 0; i < nh; ++i) {
+    if (!hs[i]) return fail(MHD_ERR_INVALID, "null handle in ensemble");
+    if (hs[i]->device != hs[0]->device) return fail(MHD_ERR_INVALID, "ensemble members must share a device");
+    for (int j = 0; j < i; ++j) if (hs[j] == hs[i]) return fail(MHD_ERR_INVALID, "duplicate handle in ensemble");
+  }
+  std::unique_ptr<mhd_ensemble_s> e(new (std::nothrow) mhd_ensemble_s());
+  if (!e) return fail(MHD_ERR_OOM, "host allocation failed");
+  e->hs.assign(hs, hs + nh);
+  *out = e.release();
+  return MHD_OK;
+}
+
+int mhd_ensemble_destroy(mhd_ensemble e) {
+  if (!e) return MHD_OK;
+  delete e;
+  return MHD_OK;
+}
+
+int mhd_ensemble_step(mhd_ensemble e, int nsteps) {
+  if (!e) return fail(MHD_ERR_INVALID, "null ensemble");
+  if (nsteps < 0) return fail(MHD_ERR_INVALID, "nsteps must be >= 0");
+  mhd_handle h0 = e->hs[0];
+  int rc = check_handle(h0);
+  if (rc) return rc;
+  for (auto h : e->hs) {
+    if ((rc = h->sync_lists())) return rc;
+    if (h->profiling) return fail(MHD_ERR_STATE, "ensemble steps do not run with per-kernel profiling enabled");
+  }
+  // the lists are uploaded on each member's stream: order them before the graph's first node
+  for (size_t i = 1; i < e->hs.size(); ++i) {
+    cudaEvent_t ev;
+    MHD_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+    cudaEventRecord(ev, e->hs[i]->stream);
+    cudaStreamWaitEvent(h0->stream, ev, 0);
+    cudaEventDestroy(ev);
+  }
+  if (!e->graph) {
+    const size_t m = e->hs.size();
+    e->evs.resize(m + 1);
+    for (auto& ev : e->evs) MHD_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+    cudaGraph_t gr = nullptr;
+    MHD_CUDA(cudaStreamBeginCapture(h0->stream, cudaStreamCaptureModeThreadLocal));
+    cudaEventRecord(e->evs[m], h0->stream);
+    for (size_t i = 0; i < m && rc == MHD_OK; ++i) {
+      mhd_handle h = e->hs[i];
+      if (i > 0) cudaStreamWaitEvent(h->stream, e->evs[m], 0);
+      rc = h->issue_step();
+      if (i > 0) {
+        cudaEventRecord(e->evs[i], h->stream);
+        cudaStreamWaitEvent(h0->stream, e->evs[i], 0);
+      }
+    }
+    cudaError_t err = cudaStreamEndCapture(h0->stream, &gr);
+    if (rc) { if (gr) cudaGraphDestroy(gr); return rc; }
+    if (err != cudaSuccess) return fail(MHD_ERR_CUDA, std::string("ensemble capture: ") + cudaGetErrorString(err));
+    err = cudaGraphInstantiate(&e->graph, gr, 0);
+    cudaGraphDestroy(gr);
+    if (err != cudaSuccess) { e->graph = nullptr; return fail(MHD_ERR_CUDA, std::string("ensemble instantiate: ") + cudaGetErrorString(err)); }
+  }
+  for (int s = 0; s < nsteps; ++s) {
+    MHD_CUDA(cudaGraphLaunch(e->graph, h0->stream));
+    for (auto h : e->hs) h->advance_clocks();
+  }
+  // later work on any member's own stream follows the ensemble's steps
+  for (size_t i = 1; i < e->hs.size(); ++i) {
+    cudaEvent_t ev;
+    MHD_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+    cudaEventRecord(ev, h0->stream);
+    cudaStreamWaitEvent(e->hs[i]->stream, ev, 0);
+    cudaEventDestroy(ev);
+  }
   return MHD_OK;
 }
 

@@ -49,11 +49,24 @@ struct RowSync {
   }
 };
 
+// Batched work: the kernels walk the active instances list[0..*count) of a size class; an
+// instance's buffers sit at slot * (slot stride) inside pools shared by the class.  Reading the
+// count from device memory lets membership change between steps without new launches.
+struct BatchRef {
+  const int* list;   // active slots
+  const int* count;  // number of active slots
+};
+
+struct SlotParams {
+  float nu, eta, dt, pad;
+};
+
 struct ColArgs {
   const float2* src;
   float2* dst;
   long long sF, sO, sR;  // source strides (complex elements): field/slot, outer, row
   long long dF, dO, dR;  // destination strides
+  long long sI, dI;      // source / destination slot strides (instances of a size class)
 };
 
 // ------------------------------------------------------------------------------------------
@@ -97,12 +110,13 @@ __device__ __forceinline__ void col_prefetch(float2* buf, const float2* src, lon
 
 template <class P0, int TX, int DIR, bool PIN, bool POUT>
 __global__ void __launch_bounds__(TX * P0::G, TX * P0::G <= 256 ? 2 : 1)
-    col_pass_kernel(ColArgs a, Geom geo, ColWork w, const float2* __restrict__ tw) {
+    col_pass_kernel(ColArgs a, Geom geo, ColWork w, BatchRef br, const float2* __restrict__ tw) {
   using P = Unpadded<P0>;
   extern __shared__ float2 smem[];
   constexpr int G = P::G, V = P::V, N = P::N, NT = TX * P0::G;
   const int tx = threadIdx.x % TX, g = threadIdx.x / TX;
-  const int total = w.tiles_x * w.outer * w.nf;
+  const int per = w.tiles_x * w.outer * w.nf;  // tiles of one instance
+  const int total = *br.count * per;
   // Kept-output bookkeeping (loop invariant): output element e of slot d has frequency
   // k = g + G*d + LF*e; it is kept for e < e_lo[d] (k < Kp) or e >= e_hi[d] (k >= n - Kn),
   // and its kept index is k (first range) or k - (n - K2) (second range).
@@ -116,11 +130,12 @@ __global__ void __launch_bounds__(TX * P0::G, TX * P0::G <= 256 ? 2 : 1)
   const int dR = (int)a.dR;  // row offsets inside one buffer fit 32 bits for n <= 512
   const int shift = (N - geo.k2) * dR;
   auto tile_src = [&](int t, int& col0) {
-    const int tx_t = t % w.tiles_x;
-    const int r = t / w.tiles_x;
+    const int inst = t / per, rem = t - inst * per;
+    const int tx_t = rem % w.tiles_x;
+    const int r = rem / w.tiles_x;
     const int o = r % w.outer, f = r / w.outer;
     col0 = tx_t * TX;
-    return a.src + f * a.sF + (long long)o * a.sO;
+    return a.src + br.list[inst] * a.sI + f * a.sF + (long long)o * a.sO;
   };
   int t = blockIdx.x;
   if (t < total) {
@@ -140,8 +155,9 @@ __global__ void __launch_bounds__(TX * P0::G, TX * P0::G <= 256 ? 2 : 1)
     cp_async_commit();
     cp_async_wait<1>();
     __syncthreads();
-    const int tx_t = t % w.tiles_x;
-    const int r = t / w.tiles_x;
+    const int inst = t / per, rem = t - inst * per;
+    const int tx_t = rem % w.tiles_x;
+    const int r = rem / w.tiles_x;
     const int o = r % w.outer, f = r / w.outer;
     const int kxg = tx_t * TX + tx;
     float2 v[1][V];
@@ -152,7 +168,7 @@ __global__ void __launch_bounds__(TX * P0::G, TX * P0::G <= 256 ? 2 : 1)
     __syncthreads();  // cur is now free: reuse it as the exchange buffer
     fft_run<P, DIR, 1, 0, TX>(v, cur, tx, g, tw, BlockSync{});
     if (kxg < geo.kx) {
-      float2* dst = a.dst + f * a.dF + (long long)o * a.dO + kxg;
+      float2* dst = a.dst + br.list[inst] * a.dI + f * a.dF + (long long)o * a.dO + kxg;
 #pragma unroll
       for (int d = 0; d < P::DF; ++d) {
         const int base = (g + G * d) * dR;
@@ -242,9 +258,9 @@ struct XCfg {
 };
 
 template <class P, int GROUPS>
-__global__ void __launch_bounds__(GROUPS * XCfg<P>::TPG, (P::V > 8 ? 2 : 4)) x_fused_kernel(float2* buf, Geom geo, long long rowstride,
-                                                                             long long slot, const float2* __restrict__ tw,
-                                                                             const float2* __restrict__ twr) {
+__global__ void __launch_bounds__(GROUPS * XCfg<P>::TPG, (P::V > 8 ? 2 : 4))
+    x_fused_kernel(float2* pool, Geom geo, long long rowstride, long long slot, long long istride, BatchRef br,
+                   const float2* __restrict__ tw, const float2* __restrict__ twr) {
   using PR = typename Reverse<P>::type;
   using XC = XCfg<P>;
   constexpr int G = P::G, V = P::V, N = P::N, RPG = XC::RPG, TPG = XC::TPG, TS = XC::TS;
@@ -257,15 +273,22 @@ __global__ void __launch_bounds__(GROUPS * XCfg<P>::TPG, (P::V > 8 ? 2 : 4)) x_f
   float2* gs = smem + grp * XC::group_words(kxp);
   float2* sb = gs + 2 * sw + rr * TS;
   const RowSync<G> sync{1 + grp};
-  const long long ngroups = (long long)N * N / RPG;
+  constexpr int GPI = N * N / RPG;  // row groups per instance
+  const long long ngroups = (long long)(*br.count) * GPI;
   const int chunks_row = 3 * kxp;  // 16-byte chunks of the six contiguous field rows (slot == kxp)
+  // first row of row group q, inside its instance's rowbuf
+  auto group_rows = [&](long long q) {
+    const int inst = (int)(q / GPI);
+    return pool + br.list[inst] * istride + (q - (long long)inst * GPI) * RPG * rowstride;
+  };
 
   // rows q*RPG .. q*RPG+RPG-1 -> dst (each row's six fields contiguous)
   auto prefetch = [&](long long q, float2* dst) {
+    const float2* src = group_rows(q);
     for (int c = gt; c < RPG * chunks_row; c += TPG) {
       const int r = RPG == 1 ? 0 : c / chunks_row;
       const int cc = RPG == 1 ? c : c - r * chunks_row;
-      cp_async16(dst + r * 6 * kxp + 2 * cc, buf + (q * RPG + r) * rowstride + 2 * cc);
+      cp_async16(dst + r * 6 * kxp + 2 * cc, src + r * rowstride + 2 * cc);
     }
   };
 
@@ -299,7 +322,7 @@ __global__ void __launch_bounds__(GROUPS * XCfg<P>::TPG, (P::V > 8 ? 2 : 4)) x_f
       w[2][i] = make_float2(by * bz - uy * uz, ux * by - bx * uy);
       w[3][i] = make_float2(ux * bz - bx * uz, uy * bz - by * uz);
     }
-    float2* rowp = buf + (q * RPG + rr) * rowstride;
+    float2* rowp = group_rows(q) + rr * rowstride;
 #pragma unroll
     for (int t = 0; t < 4; ++t) {
       fft_run<PR, -1, 1, TS, 1>(reinterpret_cast<float2(&)[1][V]>(w[t]), sb, 0, g, twr, sync);
@@ -396,20 +419,30 @@ enum StageOp : int {
 // projection removes).  Induction: R_b = i k x E - eta k^2 X_b with E = (Ayz, -Axz, Axy) = u x B.
 // ------------------------------------------------------------------------------------------
 struct RkArgs {
-  const float2* prod;   // 8 compact planes
-  const float2* X;      // stage state (6 fields)
-  const float2* H;      // Hermitian part of X on the kx = 0 plane, [f][kz'][ky'] (diffusion operand)
+  const float2* prod;   // 8 compact planes (slot stride prodI)
+  const float2* X;      // stage state (6 fields, slot stride stI)
+  const float2* H;      // Hermitian part of X on the kx = 0 plane, [f][kz'][ky'] (slot stride hI)
   float2* sol;          // RK4 step-start state
   float2* acc;          // RK4 accumulator / LSRK4 du / OP_RHS output
   float2* xn;           // RK4 next stage state / LSRK4 u
+  const SlotParams* sp; // per-slot nu, eta, dt
   long long fs;         // compact field stride (complex elements)
-  float nu, eta, h, dt, ca, cb;
+  long long stI, prodI, hI;
+  float hf;             // RK4 stage fraction of dt (1/2 or 1)
+  float ca, cb;         // LSRK4 coefficients of the stage
   float pscale;         // 1/n^6: the column and row passes are unnormalised in both directions
   int op;
 };
 
+struct RkSlot {
+  float2* sol;
+  float2* acc;
+  float2* xn;
+  float h, dt, ca, cb;
+};
+
 template <int OP>
-__device__ __forceinline__ void rk_apply(const RkArgs& a, long long o, float2 x, float2 R) {
+__device__ __forceinline__ void rk_apply(const RkSlot& a, long long o, float2 x, float2 R) {
   if constexpr (OP == OP_RHS) {
     a.acc[o] = R;
   } else if constexpr (OP == OP_RK4_FIRST) {
@@ -437,26 +470,35 @@ __device__ __forceinline__ void rk_apply(const RkArgs& a, long long o, float2 x,
 
 // grid (ceil(kx / blockDim.x), k2, k2): one thread per retained mode, no index division.
 template <int OP>
-__global__ void __launch_bounds__(256) rk_epilogue_kernel(RkArgs a, Geom geo) {
+__global__ void __launch_bounds__(256) rk_epilogue_kernel(RkArgs a, Geom geo, BatchRef br) {
   const int x = blockIdx.x * blockDim.x + threadIdx.x;
   if (x >= geo.kx) return;
-  const int jy = blockIdx.y, jz = blockIdx.z;
+  const int inst = blockIdx.z / geo.k2;
+  if (inst >= *br.count) return;
+  const int slot = br.list[inst];
+  const int jy = blockIdx.y, jz = blockIdx.z - inst * geo.k2;
   const long long fs = a.fs;
   const long long i = ((long long)jz * geo.k2 + jy) * geo.kxp + x;
+  const SlotParams sp = a.sp[slot];
+  const long long so = slot * a.stI;
+  RkSlot rs{a.sol + so, a.acc + so, a.xn + so, a.hf * sp.dt, sp.dt, a.ca, a.cb};
+  const float2* X = a.X + so;
+  const float2* prod = a.prod + slot * a.prodI;
   const float kxv = geo.kscale * (float)x;
   const float kyv = geo.kscale * (float)signed_of_kept(geo, jy);
   const float kzv = geo.kscale * (float)signed_of_kept(geo, jz);
   const float k2 = kxv * kxv + kyv * kyv + kzv * kzv;
   float2 p[8];
 #pragma unroll
-  for (int q = 0; q < 8; ++q) p[q] = cscale(__ldcs(a.prod + q * fs + i), a.pscale);
+  for (int q = 0; q < 8; ++q) p[q] = cscale(__ldcs(prod + q * fs + i), a.pscale);
   float2 xv[6], xd[6];
 #pragma unroll
-  for (int c = 0; c < 6; ++c) xv[c] = xd[c] = a.X[c * fs + i];
+  for (int c = 0; c < 6; ++c) xv[c] = xd[c] = X[c * fs + i];
   if (x == 0) {
     const long long p = (long long)jz * geo.k2 + jy, pl = (long long)geo.k2 * geo.k2;
+    const float2* H = a.H + slot * a.hI;
 #pragma unroll
-    for (int c = 0; c < 6; ++c) xd[c] = a.H[c * pl + p];
+    for (int c = 0; c < 6; ++c) xd[c] = H[c * pl + p];
   }
   const float2 dxz = p[0], dyz = p[1], txy = p[2], txz = p[3], tyz = p[4];
   const float2 axy = p[5], axz = p[6], ayz = p[7];
@@ -478,20 +520,26 @@ __global__ void __launch_bounds__(256) rk_epilogue_kernel(RkArgs a, Geom geo) {
   nl[3] = make_float2(-wx.y, wx.x);
   nl[4] = make_float2(-wy.y, wy.x);
   nl[5] = make_float2(-wz.y, wz.x);
-  const float du = -a.nu * k2, db = -a.eta * k2;
+  const float du = -sp.nu * k2, db = -sp.eta * k2;
 #pragma unroll
   for (int c = 0; c < 6; ++c) {
     const float dk = c < 3 ? du : db;
-    rk_apply<OP>(a, c * fs + i, xv[c], make_float2(nl[c].x + dk * xd[c].x, nl[c].y + dk * xd[c].y));
+    rk_apply<OP>(rs, c * fs + i, xv[c], make_float2(nl[c].x + dk * xd[c].x, nl[c].y + dk * xd[c].y));
   }
 }
 
 // Hermitian part of the kx = 0 plane of the six fields: H(k) = (X(k) + conj X(-k)) / 2, with
 // X(-k) = 0 when -k is in the alias band.  The reference's diffusion term is computed from the
 // re-transformed physical field, rfft(irfft(X)), which is exactly this on the kx = 0 plane.
-__global__ void herm_kx0_kernel(const float2* __restrict__ X, float2* __restrict__ H, Geom geo, long long fs) {
-  const int total = 6 * geo.k2 * geo.k2;
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
+__global__ void herm_kx0_kernel(const float2* __restrict__ Xpool, float2* __restrict__ Hpool, Geom geo, long long fs,
+                                long long stI, long long hI, BatchRef br) {
+  const int per = 6 * geo.k2 * geo.k2;
+  const int total = *br.count * per;
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < total; t += gridDim.x * blockDim.x) {
+    const int inst = t / per, i = t - inst * per;
+    const int slot = br.list[inst];
+    const float2* X = Xpool + slot * stI;
+    float2* H = Hpool + slot * hI;
     const int jy = i % geo.k2;
     const int r = i / geo.k2;
     const int jz = r % geo.k2, c = r / geo.k2;
