@@ -167,6 +167,19 @@ int mhd_time_steps(mhd_handle h, int nsteps, double* ms);
  * ms_per_step[0..nsteps) with each step's device milliseconds (synchronises at the end). */
 int mhd_step_timed(mhd_handle h, int nsteps, double* ms_per_step);
 
+/* Allocation-free spectral diagnostics (no counterpart in the reference).  For callers that may
+ * not allocate device memory (inside a graph capture, a stream callback, a real-time loop, or a
+ * host whose device memory belongs to another allocator): reads sol_dev, a device copy of
+ * prob.sol (complex64, column-major (n/2+1, n, n, 6), the mhd_set_state layout), and writes to
+ * out_dev[0..6) on the device: E_u, E_B, H_c (sums over the retained band times dV, like
+ * mhd_diagnostics), max|k.u_hat|, max|k.B_hat|, non-finite count.  Launches on `stream`
+ * (a cudaStream_t, NULL = default stream) and does not synchronise.  The only scratch is a
+ * static 58,368-byte device array inside the library (partial sums of at most 1216 blocks);
+ * n must be a supported size (16..512).  The first call on each device resolves that array's
+ * address with cudaGetSymbolAddress, so make it before any stream capture; calls that overlap
+ * on the GPU share the array and race. */
+int mhd_diagnostics_noalloc(const float* sol_dev, int n, double L, double* out_dev, void* stream);
+
 /* Last error message of the calling thread ("" if none). */
 const char* mhd_last_error(void);
 

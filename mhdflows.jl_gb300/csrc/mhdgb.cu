@@ -16,6 +16,7 @@
 #include <cstdio>
 #include <cstring>
 #include <memory>
+#include <mutex>
 #include <new>
 #include <string>
 #include <vector>
@@ -1055,3 +1056,127 @@ int mhd_ensemble_step(mhd_ensemble e, int nsteps) {
 }
 
 }  // extern "C"
+
+// ------------------------------------------------------------------------------------------
+// Allocation-free diagnostics.
+//
+// Some callers cannot call cudaMalloc: code running inside a CUDA-graph capture or another
+// library's stream callback, real-time loops that must not block on the allocator, and hosts
+// whose memory is owned by a pool they do not control (a Julia or Python array library that
+// hands out device pointers but not allocation rights).  mhd_diagnostics_noalloc serves them:
+// it reads a caller-owned device copy of prob.sol and writes six doubles to caller-owned device
+// memory, and the only scratch it uses is the fixed array below, compiled into the library.
+// ------------------------------------------------------------------------------------------
+namespace {
+
+// Per-block partial sums of the reduction: at most kNoAllocBlocks blocks x kDiagSlots doubles
+// (1216 x 6 x 8 B = 58,368 bytes).  Every GPU that loads the library holds it until the process
+// exits.  Each call overwrites the partials it uses before reading them, so nothing has to be
+// zeroed between calls, but all calls share this one array: calls whose kernels overlap on the
+// GPU (two streams, or two host threads) race on it and must be serialised by the caller.
+constexpr int kNoAllocBlocks = 1216;
+static __device__ __align__(256) double g_noalloc_partials[kNoAllocBlocks * kDiagSlots];
+
+// Device address of g_noalloc_partials on each device, looked up once per device.
+std::mutex g_noalloc_mtx;
+double* g_noalloc_ptr[256] = {nullptr};
+
+// Partial sums over a reference-layout half spectrum sol[f][kz][ky][kx] (nkr = n/2+1 fastest),
+// restricted to the retained band, with the weights and sums of diag_partial_kernel.
+__global__ void __launch_bounds__(kDiagThreads) diag_partial_ref_kernel(const float2* __restrict__ sol, Geom geo,
+                                                                        double* partial) {
+  const int nkr = geo.n / 2 + 1;
+  const long long plane = (long long)geo.n * geo.n * nkr;  // one field
+  double acc[kDiagSlots] = {0, 0, 0, 0, 0, 0};
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < plane; i += (long long)gridDim.x * blockDim.x) {
+    const int x = (int)(i % nkr);
+    if (x >= geo.kx) continue;
+    const long long r = i / nkr;
+    const int fy = (int)(r % geo.n);
+    const int fz = (int)(r / geo.n);
+    const int jy = kept_of_freq(geo, fy), jz = kept_of_freq(geo, fz);
+    if (jy < 0 || jz < 0) continue;
+    const double w = x == 0 ? 1.0 : 2.0;
+    const double kx = (double)geo.kscale * x;
+    const double ky = (double)geo.kscale * signed_of_kept(geo, jy);
+    const double kz = (double)geo.kscale * signed_of_kept(geo, jz);
+    double2 ku = make_double2(0, 0), kb = make_double2(0, 0);
+    double eu = 0, eb = 0, hc = 0;
+    bool bad = false;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      const float2 u = sol[c * plane + i], b = sol[(c + 3) * plane + i];
+      bad |= !isfinite(u.x) || !isfinite(u.y) || !isfinite(b.x) || !isfinite(b.y);
+      eu += (double)u.x * u.x + (double)u.y * u.y;
+      eb += (double)b.x * b.x + (double)b.y * b.y;
+      hc += (double)u.x * b.x + (double)u.y * b.y;
+      const double kc = c == 0 ? kx : (c == 1 ? ky : kz);
+      ku.x += kc * u.x; ku.y += kc * u.y;
+      kb.x += kc * b.x; kb.y += kc * b.y;
+    }
+    acc[0] += w * eu;
+    acc[1] += w * eb;
+    acc[2] += w * hc;
+    acc[3] = fmax(acc[3], sqrt(ku.x * ku.x + ku.y * ku.y));
+    acc[4] = fmax(acc[4], sqrt(kb.x * kb.x + kb.y * kb.y));
+    acc[5] += bad ? 1.0 : 0.0;
+  }
+  block_reduce_diag(acc, partial + (long long)blockIdx.x * kDiagSlots);
+}
+
+// Reduce the partials in block order and scale the three sums by dV / n^3 into out[0..6).
+__global__ void __launch_bounds__(kDiagThreads) diag_final_scaled_kernel(const double* __restrict__ partial, int nblocks,
+                                                                         double scale, double* out) {
+  __shared__ double res[kDiagSlots];
+  double acc[kDiagSlots] = {0, 0, 0, 0, 0, 0};
+  for (int b = threadIdx.x; b < nblocks; b += blockDim.x) {
+#pragma unroll
+    for (int s = 0; s < kDiagSlots; ++s) {
+      const double x = partial[b * kDiagSlots + s];
+      acc[s] = (s == 3 || s == 4) ? fmax(acc[s], x) : acc[s] + x;
+    }
+  }
+  block_reduce_diag(acc, res);
+  __syncthreads();
+  if (threadIdx.x < kDiagSlots) out[threadIdx.x] = threadIdx.x < 3 ? res[threadIdx.x] * scale : res[threadIdx.x];
+}
+
+}  // namespace
+
+extern "C" int mhd_diagnostics_noalloc(const float* sol_dev, int n, double L, double* out_dev, void* stream) {
+  if (!sol_dev || !out_dev) return fail(MHD_ERR_INVALID, "sol_dev and out_dev must be device pointers");
+  if (!supported(n)) {
+    return fail(MHD_ERR_INVALID, "n=" + std::to_string(n) + " is beyond what this entry point handles (n in 16,32,48,64,96,128,256,512)");
+  }
+  if (!(L > 0) || !std::isfinite(L)) return fail(MHD_ERR_INVALID, "box size L must be positive");
+  int dev = 0;
+  MHD_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 256) return fail(MHD_ERR_INVALID, "device ordinal out of range");
+  double* partials = nullptr;
+  {
+    std::lock_guard<std::mutex> lock(g_noalloc_mtx);
+    if (!g_noalloc_ptr[dev]) {
+      // first call on this device (the current one): resolve the scratch array's device address
+      void* p = nullptr;
+      cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_partials);
+      if (e != cudaSuccess) return fail(MHD_ERR_CUDA, std::string("cudaGetSymbolAddress(g_noalloc_partials): ") + cudaGetErrorString(e));
+      g_noalloc_ptr[dev] = static_cast<double*>(p);
+    }
+    partials = g_noalloc_ptr[dev];
+  }
+  const Geom g = make_geom(n, L);
+  const long long plane = (long long)n * n * (n / 2 + 1);
+  long long blocks = (plane + kDiagThreads - 1) / kDiagThreads;
+  if (blocks > kNoAllocBlocks) blocks = kNoAllocBlocks;  // grid-stride loop covers the rest
+  if (blocks < 1 || blocks > kNoAllocBlocks) return fail(MHD_ERR_INVALID, "reduction needs more partial sums than the scratch holds");
+  cudaStream_t s = (cudaStream_t)stream;
+  const double dx = L / n;
+  const double scale = dx * dx * dx / ((double)n * n * n);
+  diag_partial_ref_kernel<<<(unsigned)blocks, kDiagThreads, 0, s>>>(reinterpret_cast<const float2*>(sol_dev), g, partials);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return fail(MHD_ERR_CUDA, std::string("diag_partial_ref_kernel launch: ") + cudaGetErrorString(e));
+  diag_final_scaled_kernel<<<1, kDiagThreads, 0, s>>>(partials, (int)blocks, scale, out_dev);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return fail(MHD_ERR_CUDA, std::string("diag_final_scaled_kernel launch: ") + cudaGetErrorString(e));
+  return MHD_OK;
+}
