@@ -97,3 +97,17 @@ def test_product_does_not_import_oracle():
             if f.endswith((".py", ".cu", ".cuh", ".h", ".jl")):
                 text = open(os.path.join(dirpath, f)).read()
                 assert not re.search(r"^\s*(from|import)\s+oracle", text, re.M), f
+
+
+def test_package_initial_conditions_match_oracle(pkg, mo):
+    from importlib import import_module
+
+    ic = import_module("mhdflows_gb300.ic")
+    for n in (16, 32, 48):
+        a = ic.random_spectrum_state(n, 12)
+        b = mo.random_spectrum_state(mo.Grid(n, dtype=np.float32), 12)
+        assert np.array_equal(a, b)
+    assert ic.kept_counts(96) == mo.kept_counts(96)
+    g = mo.Grid(16, dtype=np.float32)
+    for x, y in zip(ic.taylor_green_fields(16), mo.taylor_green(g)):
+        assert np.allclose(x, y, atol=1e-6)
