@@ -129,37 +129,47 @@ __global__ void __launch_bounds__(TX * P0::G, TX * P0::G <= 256 ? 2 : 1)
   }
   const int dR = (int)a.dR;  // row offsets inside one buffer fit 32 bits for n <= 512
   const int shift = (N - geo.k2) * dR;
-  auto tile_src = [&](int t, int& col0) {
-    const int inst = t / per, rem = t - inst * per;
-    const int tx_t = rem % w.tiles_x;
-    const int r = rem / w.tiles_x;
-    const int o = r % w.outer, f = r / w.outer;
-    col0 = tx_t * TX;
-    return a.src + br.list[inst] * a.sI + f * a.sF + (long long)o * a.sO;
+  // Tile index t = tx_t + tiles_x*(o + outer*(f + nf*inst)).  The grid-stride walk advances it
+  // by gridDim.x with a carrying mixed-radix add, so divisions happen once per CTA.
+  struct Cur { int tx, o, f, inst; };
+  auto decompose = [&](int t) {
+    Cur c;
+    c.tx = t % w.tiles_x;
+    int r = t / w.tiles_x;
+    c.o = r % w.outer;
+    r /= w.outer;
+    c.f = r % w.nf;
+    c.inst = r / w.nf;
+    return c;
+  };
+  const Cur gstep = decompose(gridDim.x);
+  auto advance = [&](Cur c) {
+    int carry;
+    c.tx += gstep.tx; carry = c.tx >= w.tiles_x; if (carry) c.tx -= w.tiles_x;
+    c.o += gstep.o + carry; carry = c.o >= w.outer; if (carry) c.o -= w.outer;
+    c.f += gstep.f + carry; carry = c.f >= w.nf; if (carry) c.f -= w.nf;
+    c.inst += gstep.inst + carry;
+    return c;
+  };
+  auto tile_src = [&](const Cur& c) {
+    return a.src + br.list[c.inst] * a.sI + c.f * a.sF + (long long)c.o * a.sO;
   };
   int t = blockIdx.x;
-  if (t < total) {
-    int c0;
-    const float2* s0 = tile_src(t, c0);
-    col_prefetch<TX, NT, N, PIN>(smem, s0, a.sR, w.rows_in, c0, geo);
-  }
+  Cur cur_t = decompose(t);
+  if (t < total) col_prefetch<TX, NT, N, PIN>(smem, tile_src(cur_t), a.sR, w.rows_in, cur_t.tx * TX, geo);
   cp_async_commit();
   for (int it = 0; t < total; t += gridDim.x, ++it) {
     float2* cur = smem + (it & 1) * (N * TX);
     const int tn = t + gridDim.x;
-    if (tn < total) {
-      int c1;
-      const float2* s1 = tile_src(tn, c1);
-      col_prefetch<TX, NT, N, PIN>(smem + ((it + 1) & 1) * (N * TX), s1, a.sR, w.rows_in, c1, geo);
-    }
+    const Cur nxt = advance(cur_t);
+    if (tn < total)
+      col_prefetch<TX, NT, N, PIN>(smem + ((it + 1) & 1) * (N * TX), tile_src(nxt), a.sR, w.rows_in, nxt.tx * TX, geo);
     cp_async_commit();
     cp_async_wait<1>();
     __syncthreads();
-    const int inst = t / per, rem = t - inst * per;
-    const int tx_t = rem % w.tiles_x;
-    const int r = rem / w.tiles_x;
-    const int o = r % w.outer, f = r / w.outer;
-    const int kxg = tx_t * TX + tx;
+    const int inst = cur_t.inst, f = cur_t.f, o = cur_t.o;
+    const int kxg = cur_t.tx * TX + tx;
+    cur_t = nxt;
     float2 v[1][V];
 #pragma unroll
     for (int d = 0; d < P::DI; ++d)
@@ -326,17 +336,41 @@ __global__ void __launch_bounds__(GROUPS * XCfg<P>::TPG, (P::V > 8 ? 2 : 4))
 #pragma unroll
     for (int t = 0; t < 4; ++t) {
       fft_run<PR, -1, 1, TS, 1>(reinterpret_cast<float2(&)[1][V]>(w[t]), sb, 0, g, twr, sync);
-      sync();
-#pragma unroll
-      for (int d = 0; d < PR::DF; ++d)
+      if constexpr (G <= 32 && PR::DF == 1 && PR::LF == G) {
+        // Output element e of lane g is Z[g + G e]; its mirror Z[N - k] sits in lane (G - g) % G
+        // of the same row at element RF-1-e (element (RF - e) % RF of lane 0 itself for g = 0).
+        const int src = (threadIdx.x & 31) - g + ((G - g) % G);
 #pragma unroll
         for (int e = 0; e < PR::RF; ++e) {
-          const int k = g + G * d + PR::LF * e;
-          if (k < kx || k > N - kx) sb[k] = w[t][d * PR::RF + e];
+          if (e * G >= kx) continue;  // uniform across the warp: every lane shuffles or none does
+          const float2 m = w[t][PR::RF - 1 - e];
+          float2 zm;
+          zm.x = __shfl_sync(0xffffffffu, m.x, src);
+          zm.y = __shfl_sync(0xffffffffu, m.y, src);
+          if (g == 0) zm = w[t][(PR::RF - e) % PR::RF];
+          const int k = g + G * e;
+          if (k < kx) {
+            const float2 z = w[t][e];
+            const float2 zc = cconj(zm);
+            const float2 sm = cadd(z, zc), df = csub(z, zc);
+            rowp[(2 * t) * slot + k] = make_float2(0.5f * sm.x, 0.5f * sm.y);
+            rowp[(2 * t + 1) * slot + k] = make_float2(0.5f * df.y, -0.5f * df.x);
+          }
         }
-      sync();
-      store_split_pair(sb, N, kx, g, G, rowp + (2 * t) * slot, rowp + (2 * t + 1) * slot);
-      sync();
+        sync();  // the next transform reuses sb
+      } else {
+        sync();
+#pragma unroll
+        for (int d = 0; d < PR::DF; ++d)
+#pragma unroll
+          for (int e = 0; e < PR::RF; ++e) {
+            const int k = g + G * d + PR::LF * e;
+            if (k < kx || k > N - kx) sb[k] = w[t][d * PR::RF + e];
+          }
+        sync();
+        store_split_pair(sb, N, kx, g, G, rowp + (2 * t) * slot, rowp + (2 * t + 1) * slot);
+        sync();
+      }
     }
   }
   cp_async_wait<0>();
