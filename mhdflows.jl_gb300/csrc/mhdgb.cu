@@ -49,14 +49,14 @@ int fail(int code, const std::string& msg) {
 // ------------------------------------------------------------------------------------------
 template <int N>
 struct Cfg;
-template <> struct Cfg<16>  { using C = Plan<16, 4, 4, 4>;       using R = Plan<16, 4, 4, 4>;       static constexpr int TX = 16, ROWS = 32; };
-template <> struct Cfg<32>  { using C = Plan<32, 4, 8, 4>;       using R = Plan<32, 4, 8, 4>;       static constexpr int TX = 16, ROWS = 32; };
-template <> struct Cfg<48>  { using C = Plan<48, 4, 12, 4>;      using R = Plan<48, 4, 12, 4>;      static constexpr int TX = 16, ROWS = 32; };
-template <> struct Cfg<64>  { using C = Plan<64, 8, 8, 8>;       using R = Plan<64, 8, 8, 8>;       static constexpr int TX = 16, ROWS = 16; };
-template <> struct Cfg<96>  { using C = Plan<96, 8, 12, 4, 2>;   using R = Plan<96, 8, 12, 4, 2>;   static constexpr int TX = 16, ROWS = 16; };
-template <> struct Cfg<128> { using C = Plan<128, 8, 16, 8>;     using R = Plan<128, 16, 8, 4, 4>;  static constexpr int TX = 16, ROWS = 8; };
-template <> struct Cfg<256> { using C = Plan<256, 16, 16, 16>;   using R = Plan<256, 32, 8, 8, 4>;  static constexpr int TX = 16, ROWS = 4; };
-template <> struct Cfg<512> { using C = Plan<512, 32, 16, 8, 4>; using R = Plan<512, 64, 8, 8, 8>;  static constexpr int TX = 16, ROWS = 2; };
+template <> struct Cfg<16>  { using C = Plan<16, 4, 4, 4>;       using R = Plan<16, 4, 4, 4>;       static constexpr int COLMINB = 2; static constexpr int TX = 16, ROWS = 32; };
+template <> struct Cfg<32>  { using C = Plan<32, 4, 8, 4>;       using R = Plan<32, 4, 8, 4>;       static constexpr int COLMINB = 2; static constexpr int TX = 16, ROWS = 32; };
+template <> struct Cfg<48>  { using C = Plan<48, 4, 12, 4>;      using R = Plan<48, 4, 12, 4>;      static constexpr int COLMINB = 2; static constexpr int TX = 16, ROWS = 32; };
+template <> struct Cfg<64>  { using C = Plan<64, 8, 8, 8>;       using R = Plan<64, 8, 8, 8>;       static constexpr int COLMINB = 2; static constexpr int TX = 16, ROWS = 16; };
+template <> struct Cfg<96>  { using C = Plan<96, 8, 12, 4, 2>;   using R = Plan<96, 8, 12, 4, 2>;   static constexpr int COLMINB = 2; static constexpr int TX = 16, ROWS = 16; };
+template <> struct Cfg<128> { using C = Plan<128, 8, 16, 8>;     using R = Plan<128, 16, 8, 4, 4>;  static constexpr int COLMINB = 2; static constexpr int TX = 16, ROWS = 8; };
+template <> struct Cfg<256> { using C = Plan<256, 16, 16, 16>;   using R = Plan<256, 32, 8, 8, 4>;  static constexpr int COLMINB = 3; static constexpr int TX = 16, ROWS = 4; };
+template <> struct Cfg<512> { using C = Plan<512, 32, 16, 8, 4>; using R = Plan<512, 64, 8, 8, 8>;  static constexpr int COLMINB = 1; static constexpr int TX = 16, ROWS = 2; };
 
 constexpr int kSlots = 8;
 
@@ -118,6 +118,7 @@ struct Ops : OpsBase {
   using RR = typename Reverse<R>::type;
   using XC = XCfg<R>;
   static constexpr int TX = Cfg<N>::TX;
+  static constexpr int MINB = Cfg<N>::COLMINB;
   static constexpr int GROUPS = XC::TPG >= 64 ? 2 : 4;  // x row groups per CTA (128 threads)
   static constexpr size_t kColSmem = sizeof(float2) * 2 * N * TX;
   static constexpr size_t kRowSmem = sizeof(float2) * RowCfg<R>::TS;
@@ -145,13 +146,13 @@ struct Ops : OpsBase {
     twR = tw_all + tc.size();
     twRR = twR + tr.size();
     x_smem = sizeof(float2) * (size_t)GROUPS * XC::group_words(g.kxp);
-    if ((rc = set_smem(col_pass_kernel<C, TX, +1, true, false>, kColSmem))) return rc;
-    if ((rc = set_smem(col_pass_kernel<C, TX, -1, false, true>, kColSmem))) return rc;
+    if ((rc = set_smem(col_pass_kernel<C, TX, +1, true, false, MINB>, kColSmem))) return rc;
+    if ((rc = set_smem(col_pass_kernel<C, TX, -1, false, true, MINB>, kColSmem))) return rc;
     if ((rc = set_smem(x_fused_kernel<R, GROUPS>, x_smem))) return rc;
     if ((rc = set_smem(x_c2r_kernel<R, Cfg<N>::ROWS>, kRowSmem * Cfg<N>::ROWS))) return rc;
     if ((rc = set_smem(x_r2c_kernel<R, Cfg<N>::ROWS>, kRowSmem * Cfg<N>::ROWS))) return rc;
-    if ((rc = resident_ctas(col_pass_kernel<C, TX, +1, true, false>, TX * C::G, kColSmem, &col_inv_ctas))) return rc;
-    if ((rc = resident_ctas(col_pass_kernel<C, TX, -1, false, true>, TX * C::G, kColSmem, &col_fwd_ctas))) return rc;
+    if ((rc = resident_ctas(col_pass_kernel<C, TX, +1, true, false, MINB>, TX * C::G, kColSmem, &col_inv_ctas))) return rc;
+    if ((rc = resident_ctas(col_pass_kernel<C, TX, -1, false, true, MINB>, TX * C::G, kColSmem, &col_fwd_ctas))) return rc;
     if ((rc = resident_ctas(x_fused_kernel<R, GROUPS>, GROUPS * XC::TPG, x_smem, &x_ctas))) return rc;
     return MHD_OK;
   }
@@ -159,13 +160,13 @@ struct Ops : OpsBase {
     ColWork w{(g.kx + TX - 1) / TX, outer, nf, g.k2};
     const long long total = (long long)cap * w.tiles_x * w.outer * w.nf;
     const int grid = (int)(total < col_inv_ctas ? total : col_inv_ctas);
-    col_pass_kernel<C, TX, +1, true, false><<<grid, TX * C::G, kColSmem, s>>>(a, g, w, br, twC);
+    col_pass_kernel<C, TX, +1, true, false, MINB><<<grid, TX * C::G, kColSmem, s>>>(a, g, w, br, twC);
   }
   void col_fwd(const ColArgs& a, const Geom& g, int outer, int nf, BatchRef br, int cap, cudaStream_t s) override {
     ColWork w{(g.kx + TX - 1) / TX, outer, nf, N};
     const long long total = (long long)cap * w.tiles_x * w.outer * w.nf;
     const int grid = (int)(total < col_fwd_ctas ? total : col_fwd_ctas);
-    col_pass_kernel<C, TX, -1, false, true><<<grid, TX * C::G, kColSmem, s>>>(a, g, w, br, twC);
+    col_pass_kernel<C, TX, -1, false, true, MINB><<<grid, TX * C::G, kColSmem, s>>>(a, g, w, br, twC);
   }
   void x_fused(float2* pool, const Geom& g, long long rowstride, long long slot, long long istride, BatchRef br, int cap,
                cudaStream_t s) override {

@@ -108,8 +108,8 @@ __device__ __forceinline__ void col_prefetch(float2* buf, const float2* src, lon
   }
 }
 
-template <class P0, int TX, int DIR, bool PIN, bool POUT>
-__global__ void __launch_bounds__(TX * P0::G, TX * P0::G <= 256 ? 2 : 1)
+template <class P0, int TX, int DIR, bool PIN, bool POUT, int MINB>
+__global__ void __launch_bounds__(TX * P0::G, MINB)
     col_pass_kernel(ColArgs a, Geom geo, ColWork w, BatchRef br, const float2* __restrict__ tw) {
   using P = Unpadded<P0>;
   extern __shared__ float2 smem[];
@@ -318,7 +318,7 @@ __global__ void __launch_bounds__(GROUPS * XCfg<P>::TPG, (P::V > 8 ? 2 : 4))
     for (int t = 0; t < 3; ++t) load_herm_pair<P>(v[t], rin + (2 * t) * kxp, rin + (2 * t + 1) * kxp, kx, g);
 #pragma unroll
     for (int t = 0; t < 3; ++t) {
-      fft_run<P, +1, 1, TS, 1>(reinterpret_cast<float2(&)[1][V]>(v[t]), sb, 0, g, tw, sync);
+      fft_run<P, +1, 1, TS, 1, RowSync<G>, true>(reinterpret_cast<float2(&)[1][V]>(v[t]), sb, 0, g, tw, sync);
       sync();
     }
     float2 w[4][V];
@@ -335,30 +335,8 @@ __global__ void __launch_bounds__(GROUPS * XCfg<P>::TPG, (P::V > 8 ? 2 : 4))
     float2* rowp = group_rows(q) + rr * rowstride;
 #pragma unroll
     for (int t = 0; t < 4; ++t) {
-      fft_run<PR, -1, 1, TS, 1>(reinterpret_cast<float2(&)[1][V]>(w[t]), sb, 0, g, twr, sync);
-      if constexpr (G <= 32 && PR::DF == 1 && PR::LF == G) {
-        // Output element e of lane g is Z[g + G e]; its mirror Z[N - k] sits in lane (G - g) % G
-        // of the same row at element RF-1-e (element (RF - e) % RF of lane 0 itself for g = 0).
-        const int src = (threadIdx.x & 31) - g + ((G - g) % G);
-#pragma unroll
-        for (int e = 0; e < PR::RF; ++e) {
-          if (e * G >= kx) continue;  // uniform across the warp: every lane shuffles or none does
-          const float2 m = w[t][PR::RF - 1 - e];
-          float2 zm;
-          zm.x = __shfl_sync(0xffffffffu, m.x, src);
-          zm.y = __shfl_sync(0xffffffffu, m.y, src);
-          if (g == 0) zm = w[t][(PR::RF - e) % PR::RF];
-          const int k = g + G * e;
-          if (k < kx) {
-            const float2 z = w[t][e];
-            const float2 zc = cconj(zm);
-            const float2 sm = cadd(z, zc), df = csub(z, zc);
-            rowp[(2 * t) * slot + k] = make_float2(0.5f * sm.x, 0.5f * sm.y);
-            rowp[(2 * t + 1) * slot + k] = make_float2(0.5f * df.y, -0.5f * df.x);
-          }
-        }
-        sync();  // the next transform reuses sb
-      } else {
+      fft_run<PR, -1, 1, TS, 1, RowSync<G>, true>(reinterpret_cast<float2(&)[1][V]>(w[t]), sb, 0, g, twr, sync);
+      {
         sync();
 #pragma unroll
         for (int d = 0; d < PR::DF; ++d)
