@@ -288,11 +288,7 @@ struct PlanTw {
 // SYNC() must be a barrier over every thread that shares buf.  tw is the plan's PlanTw table.
 // Input: v[t][d*R0 + n0] = x[l1 + LI*n0] with l1 = g + G*d.
 // Output: v[t][d*RF + e] = X[lF + LF*e] with lF = g + G*d.
-// TWREC: derive the stage twiddles of one label as powers of a single table entry
-// (W^{n1 b} = (W^b)^{n1}; W^{n2 (k0 + R0 k1)} = W^{n2 k0} (W^{n2 R0})^{k1}) instead of one table
-// load each: two loads per stage, the rest FMA work.  Used where the L1 pipe, not the FMA pipe,
-// bounds the kernel; the recurrence (at most R-1 products) keeps twiddles within a few ulp.
-template <class P, int DIR, int NT, int TS, int STR, class SyncF, bool TWREC = false>
+template <class P, int DIR, int NT, int TS, int STR, class SyncF>
 __device__ __forceinline__ void fft_run(float2 (&v)[NT][P::V], float2* buf, int off, int g,
                                         const float2* __restrict__ tw, SyncF SYNC) {
   constexpr int V = P::V, G = P::G, R0 = P::R0, R1 = P::R1, R2 = P::R2;
@@ -314,19 +310,10 @@ __device__ __forceinline__ void fft_run(float2 (&v)[NT][P::V], float2* buf, int 
   for (int d = 0; d < V / R1; ++d) {
     const int l2 = g + G * d;
     const int k0 = l2 % R0, n2 = l2 / R0;
-    float2 wb = make_float2(1.f, 0.f), wc = wb;
-    if (TWREC && R1 > 1) wb = ldtw(tw, 1 * R0 + k0);  // W_{R0R1}^{k0}
 #pragma unroll
     for (int n1 = 0; n1 < R1; ++n1) {
       float2 w = make_float2(1.f, 0.f);
-      if (n1 != 0) {  // W_{R0R1}^{n1 k0}
-        if (TWREC) {
-          wc = (n1 == 1) ? wb : make_float2(wc.x * wb.x - wc.y * wb.y, wc.x * wb.y + wc.y * wb.x);
-          w = wc;
-        } else {
-          w = ldtw(tw, n1 * R0 + k0);
-        }
-      }
+      if (n1 != 0) w = ldtw(tw, n1 * R0 + k0);  // W_{R0R1}^{n1 k0}
 #pragma unroll
       for (int t = 0; t < NT; ++t) {
         float2 a = buf[t * TS + (k0 * P::E1S + n1 * R2 + n2) * STR + off];
@@ -345,21 +332,10 @@ __device__ __forceinline__ void fft_run(float2 (&v)[NT][P::V], float2* buf, int 
     for (int d = 0; d < V / R1; ++d) {
       const int l2 = g + G * d;
       const int k0 = l2 % R0, n2 = l2 / R0;
-      float2 w0 = make_float2(1.f, 0.f), ws = w0, wc = w0;
-      if (TWREC) {
-        w0 = ldtw(tw, PlanTw<P>::T2 + l2);                       // W_N^{n2 k0}
-        ws = ldtw(tw, PlanTw<P>::T2 + (R0 * R2) + R0 * n2);      // W_N^{n2 R0}
-      }
 #pragma unroll
       for (int k1 = 0; k1 < R1; ++k1) {
         const int l3 = k0 + R0 * k1;
-        float2 w;
-        if (TWREC) {
-          wc = (k1 == 0) ? w0 : make_float2(wc.x * ws.x - wc.y * ws.y, wc.x * ws.y + wc.y * ws.x);
-          w = wc;
-        } else {
-          w = ldtw(tw, PlanTw<P>::T2 + k1 * (R0 * R2) + l2);  // W_N^{n2 l3}
-        }
+        const float2 w = ldtw(tw, PlanTw<P>::T2 + k1 * (R0 * R2) + l2);  // W_N^{n2 l3}
 #pragma unroll
         for (int t = 0; t < NT; ++t) {
           const float2 a = cmul_cs<DIR>(v[t][d * R1 + k1], w.x, w.y);

@@ -318,7 +318,7 @@ __global__ void __launch_bounds__(GROUPS * XCfg<P>::TPG, (P::V > 8 ? 2 : 4))
     for (int t = 0; t < 3; ++t) load_herm_pair<P>(v[t], rin + (2 * t) * kxp, rin + (2 * t + 1) * kxp, kx, g);
 #pragma unroll
     for (int t = 0; t < 3; ++t) {
-      fft_run<P, +1, 1, TS, 1, RowSync<G>, true>(reinterpret_cast<float2(&)[1][V]>(v[t]), sb, 0, g, tw, sync);
+      fft_run<P, +1, 1, TS, 1>(reinterpret_cast<float2(&)[1][V]>(v[t]), sb, 0, g, tw, sync);
       sync();
     }
     float2 w[4][V];
@@ -335,7 +335,7 @@ __global__ void __launch_bounds__(GROUPS * XCfg<P>::TPG, (P::V > 8 ? 2 : 4))
     float2* rowp = group_rows(q) + rr * rowstride;
 #pragma unroll
     for (int t = 0; t < 4; ++t) {
-      fft_run<PR, -1, 1, TS, 1, RowSync<G>, true>(reinterpret_cast<float2(&)[1][V]>(w[t]), sb, 0, g, twr, sync);
+      fft_run<PR, -1, 1, TS, 1>(reinterpret_cast<float2(&)[1][V]>(w[t]), sb, 0, g, twr, sync);
       {
         sync();
 #pragma unroll
