@@ -107,6 +107,14 @@ int mhd_set_clock(mhd_handle h, double t, long long step, double dt);
  * nout >= 8. Returns MHD_ERR_NONFINITE (after filling out) if the state holds NaN/Inf. */
 int mhd_diagnostics(mhd_handle h, double* out, int nout);
 
+/* getCFL! of TimeIntegrator! (src/integrator.jl:54-58, 158-198) on the device.  While enabled,
+ * every step ends with dt = min(coef * dx / vmax, t_diff), vmax = max of |u_i| and |B_i| over
+ * the physical fields of the step's last stage (the fields the reference's getCFL! reads from
+ * vars), t_diff = coef * dx^2 / max(nu, eta); the clock t then advances on the device and no
+ * step synchronises with the host.  Enabling primes vmax from the current state.  Applies to
+ * every slot of the handle. */
+int mhd_set_cfl(mhd_handle h, int enable, double coef);
+
 /* Wait for all work of the handle. */
 int mhd_synchronize(mhd_handle h);
 

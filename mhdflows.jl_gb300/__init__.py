@@ -29,7 +29,7 @@ from ._lib import MHDError, MHD_LSRK4, MHD_RK4
 __all__ = [
     "GPU", "CPU", "Problem", "SetUpProblemIC", "stepforward", "updatevars", "ProbDiagnostic",
     "Diagnostics", "TimeIntegrator", "MHDError", "kept_modes", "supported_sizes", "footprint_bytes",
-    "Batch", "Ensemble", "slot_bytes",
+    "Batch", "Ensemble", "slot_bytes", "Diagnostic",
 ]
 
 FIELDS = ("ux", "uy", "uz", "bx", "by", "bz")
@@ -339,21 +339,50 @@ def ProbDiagnostic(prob: Problem):
     return r3(d.E_u), r3(d.E_B)
 
 
-def TimeIntegrator(prob: Problem, t0: float, N0: int, *, usr_dt: float = 0.0, diags=(), loop_number=100):
-    """Stepping part of TimeIntegrator! (src/integrator.jl:104-113): runs while N0 >= step and
-    t0 >= t, i.e. N0+1 steps from step 0, like the reference.  A fixed ``usr_dt`` is required
-    (the CFL path is not part of this drop-in).  Returns zone updates per second."""
+class Diagnostic:
+    """Diagnostic{T,N} (src/DiagnosticWrapper.jl:14-105): ``calc(prob)`` evaluated every ``freq``
+    steps by ``increment``; ``data``, ``t`` and ``steps`` hold the samples."""
+
+    def __init__(self, calc, prob, freq: int = 1):
+        self.calc, self.prob, self.freq = calc, prob, int(freq)
+        self.data, self.t, self.steps = [], [], []
+
+    def update(self):
+        self.data.append(self.calc(self.prob))
+        self.t.append(self.prob.clock.t)
+        self.steps.append(self.prob.clock.step)
+
+    def increment(self):
+        if self.prob.clock.step % self.freq == 0:
+            self.update()
+
+    __call__ = increment
+
+
+def TimeIntegrator(prob: Problem, t0: float, N0: int, *, usr_dt: float = 0.0, CFL_Coef: float = 0.25,
+                   diags=()):
+    """Stepping part of TimeIntegrator! (src/integrator.jl:31-156): runs while N0 >= step and
+    t0 >= t, i.e. N0+1 steps from step 0 like the reference.  With usr_dt > 0 the step is fixed;
+    with usr_dt = 0 getCFL! runs on the device before every step (dt = min(CFL_Coef dx / vmax,
+    t_diff), src/integrator.jl:158-198) without host synchronisation.  Diagnostics are
+    incremented after every step (increment!(diags), src/integrator.jl:116).  Returns the zone
+    updates per second, the reference's own throughput figure (src/integrator.jl:150-153)."""
     import time
 
-    if usr_dt <= 0:
-        raise MHDError(_lib.MHD_ERR_INVALID, "TimeIntegrator on this path needs a fixed usr_dt > 0")
-    prob.clock.dt = usr_dt
+    if usr_dt > 0:
+        _lib.check(prob._lib.mhd_set_cfl(prob._h, 0, CFL_Coef))
+        prob.clock.dt = usr_dt
+    else:
+        _lib.check(prob._lib.mhd_set_cfl(prob._h, 1, CFL_Coef))
     prob.clock.step = 0
     start = time.perf_counter()
-    while N0 >= prob.clock.step and t0 >= prob.clock.t:
-        stepforward(prob)
-        for d in diags:
-            d(prob)
+    if math.isinf(t0) and not diags:
+        stepforward(prob, N0 + 1)  # no stopping time to test: one call, no host round trips
+    else:
+        while N0 >= prob.clock.step and t0 >= prob.clock.t:
+            stepforward(prob)
+            for d in diags:
+                d.increment()
     prob.synchronize()
     el = time.perf_counter() - start
     return prob.clock.step * prob.n ** 3 / el if el > 0 else float("inf")

@@ -90,6 +90,7 @@ _SIGS = {
     "mhd_ensemble_create": (C.c_int, [C.POINTER(C.c_void_p), C.c_int, C.POINTER(C.c_void_p)]),
     "mhd_ensemble_step": (C.c_int, [C.c_void_p, C.c_int]),
     "mhd_ensemble_destroy": (C.c_int, [C.c_void_p]),
+    "mhd_set_cfl": (C.c_int, [C.c_void_p, C.c_int, C.c_double]),
     "mhd_diagnostics_noalloc": (C.c_int, [C.c_void_p, C.c_int, C.c_double, C.c_void_p, C.c_void_p]),
     "mhd_last_error": (C.c_char_p, []),
 }

@@ -68,7 +68,7 @@ struct OpsBase {
   virtual void col_inv(const ColArgs& a, const Geom& g, int outer, int nf, BatchRef br, int cap, cudaStream_t s) = 0;
   virtual void col_fwd(const ColArgs& a, const Geom& g, int outer, int nf, BatchRef br, int cap, cudaStream_t s) = 0;
   virtual void x_fused(float2* pool, const Geom& g, long long rowstride, long long slot, long long istride, BatchRef br,
-                       int cap, cudaStream_t s) = 0;
+                       int cap, unsigned int* vmax, cudaStream_t s) = 0;
   virtual void x_c2r(const float2* src, float* dst, const Geom& g, long long srow, float scale, cudaStream_t s) = 0;
   virtual void x_r2c(const float* src, float2* dst, const Geom& g, long long drow, cudaStream_t s) = 0;
 };
@@ -169,11 +169,11 @@ struct Ops : OpsBase {
     col_pass_kernel<C, TX, -1, false, true, MINB><<<grid, TX * C::G, kColSmem, s>>>(a, g, w, br, twC);
   }
   void x_fused(float2* pool, const Geom& g, long long rowstride, long long slot, long long istride, BatchRef br, int cap,
-               cudaStream_t s) override {
+               unsigned int* vmax, cudaStream_t s) override {
     const long long groups = (long long)cap * N * N / XC::RPG;
     const long long need = (groups + GROUPS - 1) / GROUPS;
     const int grid = (int)(need < x_ctas ? need : x_ctas);
-    x_fused_kernel<R, GROUPS><<<grid, GROUPS * XC::TPG, x_smem, s>>>(pool, g, rowstride, slot, istride, br, twR, twRR);
+    x_fused_kernel<R, GROUPS><<<grid, GROUPS * XC::TPG, x_smem, s>>>(pool, g, rowstride, slot, istride, br, twR, twRR, vmax);
   }
   void x_c2r(const float2* src, float* dst, const Geom& g, long long srow, float scale, cudaStream_t s) override {
     constexpr int ROWS = Cfg<N>::ROWS;
@@ -298,7 +298,13 @@ struct mhd_problem {
   unsigned int* maxabs = nullptr;
   // work lists
   SlotParams* dparams = nullptr;
-  int* dlist = nullptr;   // active slots, then the identity list (cap each), then counts
+  int* dlist = nullptr;
+  // on-device CFL: per-slot maxima of |u|, |B| (float bits) and device clock
+  unsigned int* dvmax = nullptr;
+  double* dtime = nullptr;
+  bool cfl = false;
+  double cfl_coef = 0.3;
+  int graph_version = 0;   // active slots, then the identity list (cap each), then counts
   std::vector<SlotParams> hparams;
   std::vector<char> used;
   std::vector<int> active;
@@ -325,10 +331,11 @@ struct mhd_problem {
     recs.clear();
     for (auto e : pool) cudaEventDestroy(e);
     pool.clear();
-    void* ptrs[] = {sol, xs, acc, aux, colbuf, rowbuf, ref, phys, diag_partial, diag_out, maxabs, dparams, dlist};
+    void* ptrs[] = {sol, xs, acc, aux, colbuf, rowbuf, ref, phys, diag_partial, diag_out, maxabs, dparams, dlist, dvmax, dtime};
     for (void* q : ptrs) if (q) cudaFree(q);
     sol = xs = acc = aux = colbuf = rowbuf = ref = nullptr;
     phys = nullptr; diag_partial = nullptr; diag_out = nullptr; maxabs = nullptr; dparams = nullptr; dlist = nullptr;
+    dvmax = nullptr; dtime = nullptr;
     if (own_stream) cudaStreamDestroy(own_stream);
     own_stream = nullptr;
   }
@@ -400,9 +407,9 @@ struct mhd_problem {
     ColArgs a{colbuf, rowbuf, (long long)g.kxp, AZ(), SLK(), (long long)g.kxp, BZ(), SLK(), sz.colbuf, sz.rowbuf};
     return launch(KC_YINV, [&] { ops->col_inv(a, g, g.n, nf, br, cap, stream); });
   }
-  int x_fused(BatchRef br) {
+  int x_fused(BatchRef br, unsigned int* vmax) {
     // the six field rows of a physical row are contiguous (slot stride == kxp)
-    return launch(KC_XFUSED, [&] { ops->x_fused(rowbuf, g, SLK(), g.kxp, sz.rowbuf, br, cap, stream); });
+    return launch(KC_XFUSED, [&] { ops->x_fused(rowbuf, g, SLK(), g.kxp, sz.rowbuf, br, cap, vmax, stream); });
   }
   int y_forward(int nf, BatchRef br) {
     ColArgs a{rowbuf, colbuf, (long long)g.kxp, BZ(), SLK(), (long long)g.kxp, AZ(), SLK(), sz.rowbuf, sz.colbuf};
@@ -452,11 +459,12 @@ struct mhd_problem {
       }
     });
   }
-  int rhs(const float2* X, int op, float hf, float ca, float cb, BatchRef br) {
+  // record: the stage whose physical fields getCFL! reads (the last one of a step)
+  int rhs(const float2* X, int op, float hf, float ca, float cb, BatchRef br, bool record = false) {
     int rc;
     if ((rc = z_inverse(X, ST(), 6, br))) return rc;
     if ((rc = y_inverse(6, br))) return rc;
-    if ((rc = x_fused(br))) return rc;
+    if ((rc = x_fused(br, (record && cfl) ? dvmax : nullptr))) return rc;
     if ((rc = y_forward(kSlots, br))) return rc;
     if ((rc = z_forward(rowbuf, sz.rowbuf, kSlots, br))) return rc;
     return epilogue(X, op, hf, ca, cb, br);
@@ -469,10 +477,30 @@ struct mhd_problem {
       if ((rc = rhs(sol, OP_RK4_FIRST, 0.5f, 0.f, 0.f, br))) return rc;
       if ((rc = rhs(xs, OP_RK4_MID, 0.5f, 0.f, 0.f, br))) return rc;
       if ((rc = rhs(xs, OP_RK4_MID, 1.0f, 0.f, 0.f, br))) return rc;
-      return rhs(xs, OP_RK4_LAST, 0.f, 0.f, 0.f, br);
+      if ((rc = rhs(xs, OP_RK4_LAST, 0.f, 0.f, 0.f, br, true))) return rc;
+    } else {
+      for (int i = 0; i < 5; ++i)
+        if ((rc = rhs(sol, i == 0 ? OP_LS_FIRST : OP_LS, 0.f, (float)kLsA[i], (float)kLsB[i], br, i == 4))) return rc;
     }
-    for (int i = 0; i < 5; ++i)
-      if ((rc = rhs(sol, i == 0 ? OP_LS_FIRST : OP_LS, 0.f, (float)kLsA[i], (float)kLsB[i], br))) return rc;
+    if (cfl) return cfl_update(1);
+    return MHD_OK;
+  }
+  int cfl_update(int advance) {
+    const float coef_dx = (float)(cfl_coef * p.L / g.n);
+    return launch(KC_OTHER, [&] {
+      cfl_update_kernel<<<(cap + 127) / 128, 128, 0, stream>>>(active_ref(), dparams, dvmax, dtime, coef_dx, advance);
+    });
+  }
+  // maxima of the current state's physical fields (the first CFL step's vars)
+  int cfl_prime() {
+    int rc;
+    MHD_CUDA(cudaMemsetAsync(dvmax, 0, 2 * (size_t)cap * sizeof(unsigned int), stream));
+    for (int s : active)
+      for (int f = 0; f < 6; ++f) {
+        if ((rc = inverse_field(sol + f * sz.fs, sz.state, s))) return rc;
+        unsigned int* out = dvmax + 2 * s + (f < 3 ? 0 : 1);
+        if ((rc = launch(KC_OTHER, [&] { maxabs_into_kernel<<<1216, 256, 0, stream>>>(phys, sz.phys, out); }))) return rc;
+      }
     return MHD_OK;
   }
   int build_graph() {
@@ -489,7 +517,15 @@ struct mhd_problem {
     return MHD_OK;
   }
   void advance_clocks() {
-    for (int s : active) { t[s] += hparams[s].dt; stepc[s] += 1; }
+    for (int s : active) {
+      if (!cfl) t[s] += hparams[s].dt;  // with the on-device CFL the clock lives on the device
+      stepc[s] += 1;
+    }
+  }
+  void invalidate_graph() {
+    if (graph) cudaGraphExecDestroy(graph);
+    graph = nullptr;
+    ++graph_version;
   }
   int run_steps(int nsteps) {
     int rc;
@@ -594,6 +630,10 @@ int create_class(const mhd_params* params, int cap, mhd_handle* out) {
   MHD_CUDA(cudaMalloc(&h->maxabs, 16 * sizeof(unsigned int)));
   MHD_CUDA(cudaMalloc(&h->dparams, c * sizeof(SlotParams)));
   MHD_CUDA(cudaMalloc(&h->dlist, (2 * c + 2) * sizeof(int)));
+  MHD_CUDA(cudaMalloc(&h->dvmax, 2 * c * sizeof(unsigned int)));
+  MHD_CUDA(cudaMalloc(&h->dtime, c * sizeof(double)));
+  MHD_CUDA(cudaMemsetAsync(h->dvmax, 0, 2 * c * sizeof(unsigned int), h->stream));
+  MHD_CUDA(cudaMemsetAsync(h->dtime, 0, c * sizeof(double), h->stream));
   MHD_CUDA(cudaMemsetAsync(h->sol, 0, c * s.state * sizeof(float2), h->stream));
   MHD_CUDA(cudaMemsetAsync(h->xs, 0, c * s.state * sizeof(float2), h->stream));
   MHD_CUDA(cudaMemsetAsync(h->acc, 0, c * s.state * sizeof(float2), h->stream));
@@ -615,7 +655,9 @@ int add_slot(mhd_handle h, double nu, double eta, double dt, int* slot) {
   if (s < 0) return fail(MHD_ERR_STATE, "size class is full (capacity " + std::to_string(h->cap) + ")");
   h->used[s] = 1;
   h->active.push_back(s);
-  h->hparams[s] = SlotParams{(float)nu, (float)eta, (float)dt, 0.f};
+  const double dl = h->p.L / h->g.n, vi = nu > eta ? nu : eta;
+  h->hparams[s] = SlotParams{(float)nu, (float)eta, (float)dt, vi > 0 ? (float)(h->cfl_coef * dl * dl / vi) : 0.f};
+  if (h->cfl) MHD_CUDA(cudaMemsetAsync(h->dtime + s, 0, sizeof(double), h->stream));
   h->t[s] = 0.0;
   h->stepc[s] = 0;
   h->list_dirty = true;
@@ -749,6 +791,15 @@ int mhd_slot_get_physical(mhd_handle h, int slot, int field, float* phys) {
 int mhd_slot_get_clock(mhd_handle h, int slot, double* t, long long* step, double* dt) {
   if (!h) return fail(MHD_ERR_INVALID, "null handle");
   if (!h->valid_slot(slot)) return fail(MHD_ERR_INVALID, "slot " + std::to_string(slot) + " is not active");
+  if (h->cfl) {  // dt and t are advanced on the device
+    int rc = check_handle(h);
+    if (rc) return rc;
+    SlotParams sp;
+    MHD_CUDA(cudaMemcpyAsync(&h->t[slot], h->dtime + slot, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    MHD_CUDA(cudaMemcpyAsync(&sp, h->dparams + slot, sizeof(SlotParams), cudaMemcpyDeviceToHost, h->stream));
+    MHD_CUDA(cudaStreamSynchronize(h->stream));
+    h->hparams[slot].dt = sp.dt;
+  }
   if (t) *t = h->t[slot];
   if (step) *step = h->stepc[slot];
   if (dt) *dt = h->hparams[slot].dt;
@@ -765,6 +816,47 @@ int mhd_slot_set_clock(mhd_handle h, int slot, double t, long long step, double 
     h->hparams[slot].dt = (float)dt;
     h->list_dirty = true;
   }
+  if (h->cfl) {
+    int rc = check_handle(h);
+    if (rc) return rc;
+    MHD_CUDA(cudaMemcpyAsync(h->dtime + slot, &h->t[slot], sizeof(double), cudaMemcpyHostToDevice, h->stream));
+    MHD_CUDA(cudaStreamSynchronize(h->stream));
+  }
+  return MHD_OK;
+}
+
+int mhd_set_cfl(mhd_handle h, int enable, double coef) {
+  int rc = check_handle(h);
+  if (rc) return rc;
+  if (enable && !(coef > 0 && std::isfinite(coef))) return fail(MHD_ERR_INVALID, "CFL coefficient must be positive");
+  if ((rc = h->sync_lists())) return rc;
+  MHD_CUDA(cudaStreamSynchronize(h->stream));
+  if (enable) {
+    h->cfl_coef = coef;
+    const double dl = h->p.L / h->g.n;
+    for (int s = 0; s < h->cap; ++s) {
+      const double vi = h->hparams[s].nu > h->hparams[s].eta ? h->hparams[s].nu : h->hparams[s].eta;
+      h->hparams[s].tdiff = vi > 0 ? (float)(coef * dl * dl / vi) : 0.f;
+    }
+    h->list_dirty = true;
+    if ((rc = h->sync_lists())) return rc;
+    MHD_CUDA(cudaMemcpyAsync(h->dtime, h->t.data(), h->cap * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+    h->cfl = true;
+    if ((rc = h->cfl_prime())) { h->cfl = false; return rc; }
+    if ((rc = h->cfl_update(0))) { h->cfl = false; return rc; }
+    std::vector<SlotParams> dev(h->cap);
+    MHD_CUDA(cudaMemcpyAsync(dev.data(), h->dparams, h->cap * sizeof(SlotParams), cudaMemcpyDeviceToHost, h->stream));
+    MHD_CUDA(cudaStreamSynchronize(h->stream));
+    for (int s = 0; s < h->cap; ++s) h->hparams[s].dt = dev[s].dt;
+  } else if (h->cfl) {
+    std::vector<SlotParams> dev(h->cap);
+    MHD_CUDA(cudaMemcpyAsync(h->t.data(), h->dtime, h->cap * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    MHD_CUDA(cudaMemcpyAsync(dev.data(), h->dparams, h->cap * sizeof(SlotParams), cudaMemcpyDeviceToHost, h->stream));
+    MHD_CUDA(cudaStreamSynchronize(h->stream));
+    for (int s = 0; s < h->cap; ++s) h->hparams[s].dt = dev[s].dt;
+    h->cfl = false;
+  }
+  h->invalidate_graph();
   return MHD_OK;
 }
 
@@ -969,6 +1061,7 @@ int mhd_time_steps(mhd_handle h, int nsteps, double* ms) {
 // ------------------------------------------------------------------------------------------
 struct mhd_ensemble_s {
   std::vector<mhd_handle> hs;
+  std::vector<int> versions;
   cudaGraphExec_t graph = nullptr;
   std::vector<cudaEvent_t> evs;
   ~mhd_ensemble_s() {
@@ -1017,6 +1110,15 @@ int mhd_ensemble_step(mhd_ensemble e, int nsteps) {
     cudaEventRecord(ev, e->hs[i]->stream);
     cudaStreamWaitEvent(h0->stream, ev, 0);
     cudaEventDestroy(ev);
+  }
+  {
+    std::vector<int> v;
+    for (auto h : e->hs) v.push_back(h->graph_version);
+    if (e->graph && v != e->versions) {  // a member changed what one of its steps launches
+      cudaGraphExecDestroy(e->graph);
+      e->graph = nullptr;
+    }
+    e->versions = v;
   }
   if (!e->graph) {
     const size_t m = e->hs.size();

@@ -58,7 +58,8 @@ struct BatchRef {
 };
 
 struct SlotParams {
-  float nu, eta, dt, pad;
+  float nu, eta, dt;
+  float tdiff;  // diffusive time-step limit of the on-device CFL (0: none)
 };
 
 struct ColArgs {
@@ -270,7 +271,7 @@ struct XCfg {
 template <class P, int GROUPS>
 __global__ void __launch_bounds__(GROUPS * XCfg<P>::TPG, (P::V > 8 ? 2 : 4))
     x_fused_kernel(float2* pool, Geom geo, long long rowstride, long long slot, long long istride, BatchRef br,
-                   const float2* __restrict__ tw, const float2* __restrict__ twr) {
+                   const float2* __restrict__ tw, const float2* __restrict__ twr, unsigned int* vmax) {
   using PR = typename Reverse<P>::type;
   using XC = XCfg<P>;
   constexpr int G = P::G, V = P::V, N = P::N, RPG = XC::RPG, TPG = XC::TPG, TS = XC::TS;
@@ -331,6 +332,27 @@ __global__ void __launch_bounds__(GROUPS * XCfg<P>::TPG, (P::V > 8 ? 2 : 4))
       w[1][i] = make_float2(bx * by - ux * uy, bx * bz - ux * uz);
       w[2][i] = make_float2(by * bz - uy * uz, ux * by - bx * uy);
       w[3][i] = make_float2(ux * bz - bx * uz, uy * bz - by * uz);
+    }
+    if (vmax) {
+      // max |u_i| and max |B_i| over the physical fields (getCFL! on the last stage's fields);
+      // non-negative floats order like their bit patterns, NaN above +inf
+      float mu = 0.f, mb = 0.f;
+#pragma unroll
+      for (int i = 0; i < V; ++i) {
+        mu = fmaxf(mu, fmaxf(fabsf(v[0][i].x), fmaxf(fabsf(v[0][i].y), fabsf(v[1][i].x))));
+        mb = fmaxf(mb, fmaxf(fabsf(v[1][i].y), fmaxf(fabsf(v[2][i].x), fabsf(v[2][i].y))));
+      }
+      unsigned int bu = __float_as_uint(mu), bb = __float_as_uint(mb);
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        bu = max(bu, __shfl_xor_sync(0xffffffffu, bu, o));
+        bb = max(bb, __shfl_xor_sync(0xffffffffu, bb, o));
+      }
+      if ((threadIdx.x & 31) == 0) {
+        const int inst = (int)(q / GPI);
+        atomicMax(vmax + 2 * br.list[inst], bu);
+        atomicMax(vmax + 2 * br.list[inst] + 1, bb);
+      }
     }
     float2* rowp = group_rows(q) + rr * rowstride;
 #pragma unroll
@@ -563,6 +585,39 @@ __global__ void herm_kx0_kernel(const float2* __restrict__ Xpool, float2* __rest
     if (py >= 0 && pz >= 0) xp = X[base + ((long long)pz * geo.k2 + py) * geo.kxp];
     H[i] = make_float2(0.5f * (xk.x + xp.x), 0.5f * (xk.y - xp.y));
   }
+}
+
+// On-device getCFL! (src/integrator.jl:158-198 of MHDFlows.jl) after a step of every active
+// slot: t += dt of the step just taken; next dt = min(coef * dx / max(|u|max, |B|max), tdiff)
+// from the maxima x_fused recorded on the step's last stage; the maxima are cleared for the next
+// step.  A slot with no finite positive maximum keeps its dt.
+__global__ void cfl_update_kernel(BatchRef br, SlotParams* sp, unsigned int* vmax, double* t, float coef_dx,
+                                  int advance) {
+  const int n = *br.count;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const int s = br.list[i];
+    SlotParams p = sp[s];
+    if (advance) t[s] += (double)p.dt;
+    const float vm = fmaxf(__uint_as_float(vmax[2 * s]), __uint_as_float(vmax[2 * s + 1]));
+    if (vm > 0.f && isfinite(vm)) {
+      float dt = coef_dx / vm;
+      if (p.tdiff > 0.f) dt = fminf(dt, p.tdiff);
+      p.dt = dt;
+      sp[s] = p;
+    }
+    vmax[2 * s] = 0u;
+    vmax[2 * s + 1] = 0u;
+  }
+}
+
+// max |field| of one physical field into vmax[which] (initial fields before the first CFL step).
+__global__ void maxabs_into_kernel(const float* __restrict__ a, long long n, unsigned int* out) {
+  unsigned int m = 0;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    m = max(m, __float_as_uint(fabsf(a[i])));
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_down_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0) atomicMax(out, m);
 }
 
 // ------------------------------------------------------------------------------------------
