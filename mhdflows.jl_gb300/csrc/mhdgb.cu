@@ -487,8 +487,10 @@ struct mhd_problem {
   }
   int cfl_update(int advance) {
     const float coef_dx = (float)(cfl_coef * p.L / g.n);
+    const float vscale = (float)(1.0 / ((double)g.n * g.n * g.n));
     return launch(KC_OTHER, [&] {
-      cfl_update_kernel<<<(cap + 127) / 128, 128, 0, stream>>>(active_ref(), dparams, dvmax, dtime, coef_dx, advance);
+      cfl_update_kernel<<<(cap + 127) / 128, 128, 0, stream>>>(active_ref(), dparams, dvmax, dtime, coef_dx, vscale,
+                                                              advance);
     });
   }
   // maxima of the current state's physical fields (the first CFL step's vars)
@@ -497,7 +499,7 @@ struct mhd_problem {
     MHD_CUDA(cudaMemsetAsync(dvmax, 0, 2 * (size_t)cap * sizeof(unsigned int), stream));
     for (int s : active)
       for (int f = 0; f < 6; ++f) {
-        if ((rc = inverse_field(sol + f * sz.fs, sz.state, s))) return rc;
+        if ((rc = inverse_field(sol + f * sz.fs, sz.state, s, 1.0f))) return rc;  // raw units, like x_fused
         unsigned int* out = dvmax + 2 * s + (f < 3 ? 0 : 1);
         if ((rc = launch(KC_OTHER, [&] { maxabs_into_kernel<<<1216, 256, 0, stream>>>(phys, sz.phys, out); }))) return rc;
       }
@@ -543,13 +545,15 @@ struct mhd_problem {
     return MHD_OK;
   }
   // One field of one slot: compact (src) -> physical staging, normalised inverse.
-  int inverse_field(const float2* src, long long sI, int slot) {
+  // scale < 0: the normalised inverse (1/n^3)
+  int inverse_field(const float2* src, long long sI, int slot, float scale = -1.f) {
     int rc;
     const BatchRef br = slot_ref(slot);
     if ((rc = z_inverse(src, sI, 1, br))) return rc;
     if ((rc = y_inverse(1, br))) return rc;
     float2* rb = rowbuf + slot * sz.rowbuf;
-    return launch(KC_OTHER, [&] { ops->x_c2r(rb, phys, g, SLK(), (float)(1.0 / ((double)g.n * g.n * g.n)), stream); });
+    const float sc = scale < 0.f ? (float)(1.0 / ((double)g.n * g.n * g.n)) : scale;
+    return launch(KC_OTHER, [&] { ops->x_c2r(rb, phys, g, SLK(), sc, stream); });
   }
   // One field of one slot: physical staging -> compact (dst + slot*dI), unnormalised forward.
   int forward_field(float2* dst, long long dI, int slot) {

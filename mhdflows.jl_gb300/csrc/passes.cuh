@@ -591,14 +591,16 @@ __global__ void herm_kx0_kernel(const float2* __restrict__ Xpool, float2* __rest
 // slot: t += dt of the step just taken; next dt = min(coef * dx / max(|u|max, |B|max), tdiff)
 // from the maxima x_fused recorded on the step's last stage; the maxima are cleared for the next
 // step.  A slot with no finite positive maximum keeps its dt.
+// vmax holds maxima of the unnormalised fields the passes work with (n^3 times the physical
+// values); vscale = 1/n^3 converts them.
 __global__ void cfl_update_kernel(BatchRef br, SlotParams* sp, unsigned int* vmax, double* t, float coef_dx,
-                                  int advance) {
+                                  float vscale, int advance) {
   const int n = *br.count;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     const int s = br.list[i];
     SlotParams p = sp[s];
     if (advance) t[s] += (double)p.dt;
-    const float vm = fmaxf(__uint_as_float(vmax[2 * s]), __uint_as_float(vmax[2 * s + 1]));
+    const float vm = vscale * fmaxf(__uint_as_float(vmax[2 * s]), __uint_as_float(vmax[2 * s + 1]));
     if (vm > 0.f && isfinite(vm)) {
       float dt = coef_dx / vm;
       if (p.tdiff > 0.f) dt = fminf(dt, p.tdiff);
