@@ -133,6 +133,7 @@ struct Ops : OpsBase {
 
   int setup(const Geom& g) override {
     int rc = MHD_OK;
+    if (g.kx != kept_kx_of(N)) return fail(MHD_ERR_INVALID, "kept-mode count differs from the compiled row plan");
     std::vector<float2> tc, tr, trr;
     plan_twiddles<C>(tc);
     plan_twiddles<R>(tr);

@@ -204,27 +204,36 @@ __global__ void __launch_bounds__(TX * P0::G, MINB)
 // ------------------------------------------------------------------------------------------
 // x rows: Hermitian two-for-one helpers.
 // ------------------------------------------------------------------------------------------
-// Input of an inverse (c2r) transform of two half-spectrum rows f1, f2 with kx kept modes
+// Kept rfft-axis modes of the 2/3 rule for n points, as a compile-time constant (the same double
+// arithmetic as FourierFlows' getaliasedwavenumbers with aliased fraction 1/3: floor(n/3 + tiny)).
+__host__ __device__ constexpr int kept_kx_of(int n) { return (int)((1.0 - 1.0 / 3.0) / 2.0 * n); }
+
+// Input of an inverse (c2r) transform of two half-spectrum rows f1, f2 with KX kept modes
 // (plain loads: the rows may live in global or in shared memory):
 // z[n] = F1[n] + i F2[n] with F[n-n] = conj(F[n]); the kx = 0 imaginary parts are dropped,
-// which is what a c2r transform does with a non-Hermitian kx = 0 plane.
-template <class P>
+// which is what a c2r transform does with a non-Hermitian kx = 0 plane.  Elements whose index
+// lies in the alias band for every lane are compile-time zeros, so the first stage of the
+// transform is pruned by constant folding.
+template <class P, int KX>
 __device__ __forceinline__ void load_herm_pair(float2 (&v)[P::V], const float2* __restrict__ f1,
-                                               const float2* __restrict__ f2, int kx, int g) {
+                                               const float2* __restrict__ f2, int g) {
 #pragma unroll
   for (int d = 0; d < P::DI; ++d)
 #pragma unroll
     for (int n0 = 0; n0 < P::R0; ++n0) {
-      const int n = g + P::G * d + P::LI * n0;
+      const int nmin = P::G * d + P::LI * n0;  // element index of lane 0
       float2 z = make_float2(0.f, 0.f);
-      if (n < kx) {
-        float2 a = f1[n], b = f2[n];
-        if (n == 0) { a.y = 0.f; b.y = 0.f; }
-        z = make_float2(a.x - b.y, a.y + b.x);
-      } else if (n > P::N - kx) {
-        const int m = P::N - n;
-        float2 a = f1[m], b = f2[m];
-        z = make_float2(a.x + b.y, b.x - a.y);
+      if (nmin < KX || nmin + P::G - 1 > P::N - KX) {  // some lane holds a kept mode
+        const int n = g + nmin;
+        if (n < KX) {
+          float2 a = f1[n], b = f2[n];
+          if (n == 0) { a.y = 0.f; b.y = 0.f; }
+          z = make_float2(a.x - b.y, a.y + b.x);
+        } else if (n > P::N - KX) {
+          const int m = P::N - n;
+          float2 a = f1[m], b = f2[m];
+          z = make_float2(a.x + b.y, b.x - a.y);
+        }
       }
       v[d * P::R0 + n0] = z;
     }
@@ -240,6 +249,38 @@ __device__ __forceinline__ void store_split_pair(const float2* sb, int n, int kx
     const float2 s = cadd(z, zc), df = csub(z, zc);
     outa[k] = make_float2(0.5f * s.x, 0.5f * s.y);
     outb[k] = make_float2(0.5f * df.y, -0.5f * df.x);
+  }
+}
+
+// The same split straight from the registers of a forward transform whose G lanes sit in one
+// warp (G <= 32, lanes rowbase .. rowbase+G-1).  With the output layout of fft_run,
+// register (m % DF)*RF + m / DF of lane g holds Z[g + G m], and Z[N - g - G m] sits in lane
+// (G - g) % G at index V-1-m (g > 0) or in lane 0 itself at index (V-m) % V (g = 0): one
+// shuffle per needed output, no shared memory.  Outputs of every lane past the kept band are
+// never read, so the last stage of the transform is pruned as dead code.
+template <class P, int KX>
+__device__ __forceinline__ void store_split_shfl(const float2 (&v)[P::V], int g, int rowbase, float2* outa,
+                                                 float2* outb) {
+  constexpr int G = P::G, V = P::V, DF = P::DF, RF = P::RF;
+  static_assert(G <= 32, "the shuffle split needs the row inside one warp");
+  const int partner = rowbase + (G - g) % G;
+#pragma unroll
+  for (int m = 0; m < V; ++m) {
+    if (G * m >= KX) break;  // no lane holds a kept output from here on (compile-time)
+    const float2 z = v[(m % DF) * RF + m / DF];
+    const int mp = V - 1 - m, m0 = (V - m) % V;
+    const float2 pz = v[(mp % DF) * RF + mp / DF];
+    float2 p;
+    p.x = __shfl_sync(0xffffffffu, pz.x, partner);
+    p.y = __shfl_sync(0xffffffffu, pz.y, partner);
+    if (g == 0) p = v[(m0 % DF) * RF + m0 / DF];
+    const int k = g + G * m;
+    if (k < KX) {
+      const float2 zc = cconj(p);
+      const float2 s = cadd(z, zc), df = csub(z, zc);
+      outa[k] = make_float2(0.5f * s.x, 0.5f * s.y);
+      outb[k] = make_float2(0.5f * df.y, -0.5f * df.x);
+    }
   }
 }
 
@@ -275,8 +316,9 @@ __global__ void __launch_bounds__(GROUPS * XCfg<P>::TPG, (P::V > 8 ? 2 : 4))
   using PR = typename Reverse<P>::type;
   using XC = XCfg<P>;
   constexpr int G = P::G, V = P::V, N = P::N, RPG = XC::RPG, TPG = XC::TPG, TS = XC::TS;
+  constexpr int KX = kept_kx_of(N);  // the host checks geo.kx == KX
   extern __shared__ float2 smem[];
-  const int kxp = geo.kxp, kx = geo.kx;
+  const int kxp = geo.kxp;
   const int grp = threadIdx.x / TPG;
   const int gt = threadIdx.x % TPG;          // thread within group
   const int rr = gt / G, g = gt % G;         // row within group, lane within row
@@ -316,22 +358,11 @@ __global__ void __launch_bounds__(GROUPS * XCfg<P>::TPG, (P::V > 8 ? 2 : 4))
     const float2* rin = cur + rr * 6 * kxp;
     float2 v[3][V];
 #pragma unroll
-    for (int t = 0; t < 3; ++t) load_herm_pair<P>(v[t], rin + (2 * t) * kxp, rin + (2 * t + 1) * kxp, kx, g);
+    for (int t = 0; t < 3; ++t) load_herm_pair<P, KX>(v[t], rin + (2 * t) * kxp, rin + (2 * t + 1) * kxp, g);
 #pragma unroll
     for (int t = 0; t < 3; ++t) {
       fft_run<P, +1, 1, TS, 1>(reinterpret_cast<float2(&)[1][V]>(v[t]), sb, 0, g, tw, sync);
       sync();
-    }
-    float2 w[4][V];
-#pragma unroll
-    for (int i = 0; i < V; ++i) {
-      const float ux = v[0][i].x, uy = v[0][i].y, uz = v[1][i].x;
-      const float bx = v[1][i].y, by = v[2][i].x, bz = v[2][i].y;
-      const float tzz = bz * bz - uz * uz;
-      w[0][i] = make_float2((bx * bx - ux * ux) - tzz, (by * by - uy * uy) - tzz);
-      w[1][i] = make_float2(bx * by - ux * uy, bx * bz - ux * uz);
-      w[2][i] = make_float2(by * bz - uy * uz, ux * by - bx * uy);
-      w[3][i] = make_float2(ux * bz - bx * uz, uy * bz - by * uz);
     }
     if (vmax) {
       // max |u_i| and max |B_i| over the physical fields (getCFL! on the last stage's fields);
@@ -355,20 +386,43 @@ __global__ void __launch_bounds__(GROUPS * XCfg<P>::TPG, (P::V > 8 ? 2 : 4))
       }
     }
     float2* rowp = group_rows(q) + rr * rowstride;
+    // one product pair at a time: the six fields stay live, the pair is formed just before its
+    // forward transform (fewer live registers than all eight products at once)
 #pragma unroll
     for (int t = 0; t < 4; ++t) {
-      fft_run<PR, -1, 1, TS, 1>(reinterpret_cast<float2(&)[1][V]>(w[t]), sb, 0, g, twr, sync);
-      {
+      float2 w[1][V];
+#pragma unroll
+      for (int i = 0; i < V; ++i) {
+        const float ux = v[0][i].x, uy = v[0][i].y, uz = v[1][i].x;
+        const float bx = v[1][i].y, by = v[2][i].x, bz = v[2][i].y;
+        if (t == 0) {
+          const float tzz = bz * bz - uz * uz;
+          w[0][i] = make_float2((bx * bx - ux * ux) - tzz, (by * by - uy * uy) - tzz);
+        } else if (t == 1) {
+          w[0][i] = make_float2(bx * by - ux * uy, bx * bz - ux * uz);
+        } else if (t == 2) {
+          w[0][i] = make_float2(by * bz - uy * uz, ux * by - bx * uy);
+        } else {
+          w[0][i] = make_float2(ux * bz - bx * uz, uy * bz - by * uz);
+        }
+      }
+      fft_run<PR, -1, 1, TS, 1>(w, sb, 0, g, twr, sync);
+      float2* oa = rowp + (2 * t) * slot;
+      float2* ob = rowp + (2 * t + 1) * slot;
+      if constexpr (G <= 32) {
+        store_split_shfl<PR, KX>(w[0], g, (threadIdx.x & 31) - g, oa, ob);
+        sync();  // the next transform's first exchange overwrites sb
+      } else {
         sync();
 #pragma unroll
         for (int d = 0; d < PR::DF; ++d)
 #pragma unroll
           for (int e = 0; e < PR::RF; ++e) {
             const int k = g + G * d + PR::LF * e;
-            if (k < kx || k > N - kx) sb[k] = w[t][d * PR::RF + e];
+            if (k < KX || k > N - KX) sb[k] = w[0][d * PR::RF + e];
           }
         sync();
-        store_split_pair(sb, N, kx, g, G, rowp + (2 * t) * slot, rowp + (2 * t + 1) * slot);
+        store_split_pair(sb, N, KX, g, G, oa, ob);
         sync();
       }
     }
@@ -387,7 +441,7 @@ __global__ void __launch_bounds__(ROWS * P::G) x_c2r_kernel(const float2* src, f
   const int r = threadIdx.x / G, g = threadIdx.x % G;
   const long long q = (long long)blockIdx.x * ROWS + r;
   float2 v[1][V];
-  load_herm_pair<P>(v[0], src + (2 * q) * srow, src + (2 * q + 1) * srow, geo.kx, g);
+  load_herm_pair<P, kept_kx_of(P::N)>(v[0], src + (2 * q) * srow, src + (2 * q + 1) * srow, g);
   fft_run<P, +1, 1, TS, 1>(v, smem + r * TS, 0, g, tw, RowSync<G>{1 + r});
   float* da = dst + (2 * q) * N;
   float* db = dst + (2 * q + 1) * N;
