@@ -186,6 +186,7 @@ def run_ensemble(args):
             slot = b.add(v, v, dt)
             b.set_state(slot, x)
             boxes.append((n, v, dt, seed, x))
+        pkg.autotune(b)
         batches.append(b)
     ens = pkg.Ensemble(batches)
     K = args.steps
@@ -272,6 +273,8 @@ def run_gpu(args, rank, world, local, dist: Dist):
     chk = pkg._lib.check
     prob.set_sol(s0.T)
     stream = lib.mhd_get_stream(h)
+    # kernel variants: the autotuner's choice for this device and size (timed once, then cached)
+    variants = pkg.autotune(prob)
 
     # warm-up
     pkg.stepforward(prob, args.warmup)
@@ -360,19 +363,20 @@ def run_gpu(args, rank, world, local, dist: Dist):
         s2 = initial_state(n2)
         p2 = pkg.Problem(pkg.GPU(local), nx=n2, Lx=2 * math.pi, nu=5e-4, eta=5e-4, dt=2.5e-4, stepper="RK4")
         p2.set_sol(s2.T)
+        variants2 = pkg.autotune(p2)
         pkg.stepforward(p2, 3)
         p2.synchronize()
         ms2 = C.c_double()
         chk(lib.mhd_time_steps(p2.handle, 10, C.byref(ms2)))
         secondary = {"n": n2, "ms_per_step": round(ms2.value / 10, 3),
-                     "grid_pt_steps_per_s": n2 ** 3 / (ms2.value / 10 / 1e3)}
+                     "grid_pt_steps_per_s": n2 ** 3 / (ms2.value / 10 / 1e3), "variants": variants2}
         p2.close()
     prob.close()
     return {
         "value": value, "ms_per_step": ms_per_step, "p50_ms": p50, "p99_ms": p99, "launches": launches,
         "clocks": clocks, "top": top, "achieved": achieved, "bytes": b.value, "peak": peak, "peak_kind": peak_kind,
         "kernels": kernels, "e2e": e2e_value, "e2e_bytes": nbytes, "e2e_steps": ke, "finite": finite,
-        "secondary": secondary, "prof_ms": prof_ms,
+        "secondary": secondary, "prof_ms": prof_ms, "variants": variants,
     }
 
 
@@ -478,6 +482,7 @@ def main():
                          "window": "CUDA events around every launch over K steps right after the timed region",
                          "window_ms_per_step": r["prof_ms"]},
             "kernels": r["kernels"],
+            "variants": r["variants"],
             "cpu_baseline": cpu,
             "baseline_note": "vs_baseline = per-GPU value / (256^3 / 0.271 s), the reference README's RTX 3080 MHD RK4 256^3 figure",
         }

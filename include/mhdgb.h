@@ -175,6 +175,25 @@ int mhd_time_steps(mhd_handle h, int nsteps, double* ms);
  * ms_per_step[0..nsteps) with each step's device milliseconds (synchronises at the end). */
 int mhd_step_timed(mhd_handle h, int nsteps, double* ms_per_step);
 
+/* Autotuner (no counterpart in the reference, whose FFTs are FFTW / cuFFT plans made with
+ * MEASURE).  Each FFT pass class (z_inverse, y_inverse, x_fused, y_forward, z_forward: classes
+ * 0..4 of mhd_kernel_class_name) has a default kernel configuration and, for some grid sizes,
+ * further candidates (radix plans, kx columns per tile, transforms per exchange round, occupancy
+ * bounds).  mhd_autotune times every candidate that fits on the device on the handle's own
+ * scratch buffers (the state is not touched; at least one slot must be active) and selects the
+ * fastest of each class.  The result is kept for the process and appended to a tuning file
+ * ($MHDGB_TUNE_CACHE, else $XDG_CACHE_HOME/mhdgb/tune.txt, else $HOME/.cache/mhdgb/tune.txt;
+ * MHDGB_TUNE_CACHE="" disables the file), keyed by device name, SM count and n; handles created
+ * later for the same key start from it.  Without MHD_TUNE_FORCE a known result is applied
+ * without timing.  Every variant computes the same transforms; results agree to FP32 rounding. */
+#define MHD_TUNE_FORCE 1     /* time the candidates even if a result is known */
+#define MHD_TUNE_NO_FILE 2   /* do not append to the tuning file */
+int mhd_autotune(mhd_handle h, int flags);
+int mhd_variant_count(mhd_handle h, int cls, int* count);
+/* name of variant idx of class cls (idx < 0: the selected one) into buf[0..len) */
+int mhd_variant_name(mhd_handle h, int cls, int idx, char* buf, int len);
+int mhd_select_variant(mhd_handle h, int cls, int idx);
+
 /* Allocation-free spectral diagnostics (no counterpart in the reference).  For callers that may
  * not allocate device memory (inside a graph capture, a stream callback, a real-time loop, or a
  * host whose device memory belongs to another allocator): reads sol_dev, a device copy of

@@ -29,7 +29,8 @@ from ._lib import MHDError, MHD_LSRK4, MHD_RK4
 __all__ = [
     "GPU", "CPU", "Problem", "SetUpProblemIC", "stepforward", "updatevars", "ProbDiagnostic",
     "Diagnostics", "TimeIntegrator", "MHDError", "kept_modes", "supported_sizes", "footprint_bytes",
-    "Batch", "Ensemble", "slot_bytes", "Diagnostic",
+    "Batch", "Ensemble", "slot_bytes", "Diagnostic", "autotune", "variants", "select_variant",
+    "TUNED_CLASSES",
 ]
 
 FIELDS = ("ux", "uy", "uz", "bx", "by", "bz")
@@ -530,3 +531,42 @@ class Ensemble:
             self.close()
         except Exception:
             pass
+
+
+# ---- autotuner (FFT pass kernel variants) --------------------------------------------------
+TUNED_CLASSES = ("z_inverse", "y_inverse", "x_fused", "y_forward", "z_forward")
+
+
+def autotune(obj, force: bool = False, persist: bool = True):
+    """Time the kernel variants of each FFT pass on ``obj`` (a Problem or Batch) and keep the
+    fastest; returns the selected variant names.  A result already known for this device and
+    grid size is applied without timing unless ``force``."""
+    lib = _lib.load()
+    flags = (_lib.MHD_TUNE_FORCE if force else 0) | (0 if persist else _lib.MHD_TUNE_NO_FILE)
+    _lib.check(lib.mhd_autotune(obj.handle, flags))
+    return {c: v[0] for c, v in variants(obj).items()}
+
+
+def variants(obj):
+    """{class: (selected variant name, [all variant names])} of a Problem or Batch."""
+    lib = _lib.load()
+    out = {}
+    buf = C.create_string_buffer(256)
+    for i, cname in enumerate(TUNED_CLASSES):
+        cnt = C.c_int()
+        _lib.check(lib.mhd_variant_count(obj.handle, i, C.byref(cnt)))
+        names = []
+        for j in range(cnt.value):
+            _lib.check(lib.mhd_variant_name(obj.handle, i, j, buf, 256))
+            names.append(buf.value.decode())
+        _lib.check(lib.mhd_variant_name(obj.handle, i, -1, buf, 256))
+        out[cname] = (buf.value.decode(), names)
+    return out
+
+
+def select_variant(obj, cls, idx: int):
+    """Select variant ``idx`` of FFT pass class ``cls`` (index or name in TUNED_CLASSES)."""
+    lib = _lib.load()
+    ci = TUNED_CLASSES.index(cls) if isinstance(cls, str) else int(cls)
+    _lib.check(lib.mhd_select_variant(obj.handle, ci, int(idx)))
+

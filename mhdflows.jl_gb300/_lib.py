@@ -22,6 +22,8 @@ MHD_ERR_STATE = 5
 MHD_RK4 = 0
 MHD_LSRK4 = 1
 MHD_PREC_FP32 = 0
+MHD_TUNE_FORCE = 1
+MHD_TUNE_NO_FILE = 2
 
 
 class MHDError(RuntimeError):
@@ -92,6 +94,10 @@ _SIGS = {
     "mhd_ensemble_destroy": (C.c_int, [C.c_void_p]),
     "mhd_set_cfl": (C.c_int, [C.c_void_p, C.c_int, C.c_double]),
     "mhd_diagnostics_noalloc": (C.c_int, [C.c_void_p, C.c_int, C.c_double, C.c_void_p, C.c_void_p]),
+    "mhd_autotune": (C.c_int, [C.c_void_p, C.c_int]),
+    "mhd_variant_count": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_int)]),
+    "mhd_variant_name": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_char_p, C.c_int]),
+    "mhd_select_variant": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),
     "mhd_last_error": (C.c_char_p, []),
 }
 

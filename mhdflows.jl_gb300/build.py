@@ -1,10 +1,13 @@
 """Build the in-tree CUDA library ``lib/libmhdgb.so`` for sm_103a with nvcc.
 
-One translation unit, one ``-gencode``: a build takes well under a minute.  The library is
-rebuilt when any source under ``csrc/`` or ``include/`` is newer than it.
+The sources are a few translation units (the C ABI and step orchestration, and one unit per
+group of grid sizes holding that size's FFT pass kernels); they compile in parallel, one
+``-gencode``, and link into one shared library.  The library is rebuilt when any source under
+``csrc/`` or ``include/`` is newer than it.
 """
 from __future__ import annotations
 
+import concurrent.futures as cf
 import os
 import shutil
 import subprocess
@@ -17,7 +20,7 @@ LIB_DIR = os.path.join(PKG_DIR, "lib")
 LIB_PATH = os.path.join(LIB_DIR, "libmhdgb.so")
 
 ARCH_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a"]
-NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-O2", "-shared"]
+NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-O2"]
 
 
 def _sources():
@@ -43,20 +46,40 @@ def needs_build() -> bool:
     return any(os.path.getmtime(s) > t for s in _sources())
 
 
+def _units():
+    return sorted(os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith(".cu"))
+
+
 def build(force: bool = False, verbose: bool = False) -> str:
-    """Compile csrc/mhdgb.cu into lib/libmhdgb.so (sm_103a) and return its path."""
+    """Compile csrc/*.cu into lib/libmhdgb.so (sm_103a) and return its path."""
     if not force and not needs_build():
         return LIB_PATH
     os.makedirs(LIB_DIR, exist_ok=True)
+    obj_dir = os.path.join(LIB_DIR, "obj")
+    os.makedirs(obj_dir, exist_ok=True)
+    nvcc = _nvcc()
+
+    def compile_unit(src):
+        obj = os.path.join(obj_dir, os.path.basename(src)[:-3] + ".o")
+        cmd = [nvcc, *ARCH_FLAGS, *NVCC_FLAGS, "-I", INCLUDE, "-c", "-o", obj, src]
+        if verbose:
+            cmd.insert(1, "-Xptxas=-v")
+        res = subprocess.run(cmd, capture_output=True, text=True)
+        return obj, cmd, res
+
+    objs = []
+    with cf.ThreadPoolExecutor(max_workers=min(8, os.cpu_count() or 1)) as ex:
+        for obj, cmd, res in ex.map(compile_unit, _units()):
+            if res.returncode != 0:
+                raise RuntimeError("nvcc failed:\n" + " ".join(cmd) + "\n" + res.stdout + res.stderr)
+            if verbose:
+                print(res.stdout + res.stderr)
+            objs.append(obj)
     tmp = LIB_PATH + ".tmp"
-    cmd = [_nvcc(), *ARCH_FLAGS, *NVCC_FLAGS, "-I", INCLUDE, "-o", tmp, os.path.join(CSRC, "mhdgb.cu")]
-    if verbose:
-        cmd.insert(1, "-Xptxas=-v")
+    cmd = [nvcc, *ARCH_FLAGS, "-shared", "-o", tmp, *objs]
     res = subprocess.run(cmd, capture_output=True, text=True)
     if res.returncode != 0:
-        raise RuntimeError("nvcc failed:\n" + " ".join(cmd) + "\n" + res.stdout + res.stderr)
-    if verbose:
-        print(res.stdout + res.stderr)
+        raise RuntimeError("nvcc link failed:\n" + " ".join(cmd) + "\n" + res.stdout + res.stderr)
     os.replace(tmp, LIB_PATH)
     return LIB_PATH
 

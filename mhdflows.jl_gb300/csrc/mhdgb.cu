@@ -12,9 +12,14 @@
 // ever read: dealias! zeroes the alias band of the stage state before every RHS evaluation.
 #include <cuda_runtime.h>
 
+#include <sys/stat.h>
+
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
+#include <map>
 #include <memory>
 #include <mutex>
 #include <new>
@@ -22,7 +27,8 @@
 #include <vector>
 
 #include "../../include/mhdgb.h"
-#include "passes.cuh"
+#include "ops.cuh"
+#include "step_kernels.cuh"
 
 using namespace mhdgb;
 
@@ -44,160 +50,18 @@ int fail(int code, const std::string& msg) {
     }                                                                                    \
   } while (0)
 
-// ------------------------------------------------------------------------------------------
-// Per-size plans: column passes (y, z) and x rows.
-// ------------------------------------------------------------------------------------------
-template <int N>
-struct Cfg;
-template <> struct Cfg<16>  { using C = Plan<16, 4, 4, 4>;       using R = Plan<16, 4, 4, 4>;       static constexpr int COLMINB = 2; static constexpr int TX = 16, ROWS = 32; };
-template <> struct Cfg<32>  { using C = Plan<32, 4, 8, 4>;       using R = Plan<32, 4, 8, 4>;       static constexpr int COLMINB = 2; static constexpr int TX = 16, ROWS = 32; };
-template <> struct Cfg<48>  { using C = Plan<48, 4, 12, 4>;      using R = Plan<48, 4, 12, 4>;      static constexpr int COLMINB = 2; static constexpr int TX = 16, ROWS = 32; };
-template <> struct Cfg<64>  { using C = Plan<64, 8, 8, 8>;       using R = Plan<64, 8, 8, 8>;       static constexpr int COLMINB = 2; static constexpr int TX = 16, ROWS = 16; };
-template <> struct Cfg<96>  { using C = Plan<96, 8, 12, 4, 2>;   using R = Plan<96, 8, 12, 4, 2>;   static constexpr int COLMINB = 2; static constexpr int TX = 16, ROWS = 16; };
-template <> struct Cfg<128> { using C = Plan<128, 8, 16, 8>;     using R = Plan<128, 16, 8, 4, 4>;  static constexpr int COLMINB = 2; static constexpr int TX = 16, ROWS = 8; };
-template <> struct Cfg<256> { using C = Plan<256, 16, 16, 16>;   using R = Plan<256, 32, 8, 8, 4>;  static constexpr int COLMINB = 3; static constexpr int TX = 16, ROWS = 4; };
-template <> struct Cfg<512> { using C = Plan<512, 32, 16, 8, 4>; using R = Plan<512, 64, 8, 8, 8>;  static constexpr int COLMINB = 1; static constexpr int TX = 16, ROWS = 2; };
-
 constexpr int kSlots = 8;
-
-struct OpsBase {
-  virtual ~OpsBase() {}
-  virtual int setup(const Geom& g) = 0;
-  // cap: upper bound of the active instances (the grid covers cap instances; the kernels read
-  // the actual count from the BatchRef)
-  virtual void col_inv(const ColArgs& a, const Geom& g, int outer, int nf, BatchRef br, int cap, cudaStream_t s) = 0;
-  virtual void col_fwd(const ColArgs& a, const Geom& g, int outer, int nf, BatchRef br, int cap, cudaStream_t s) = 0;
-  virtual void x_fused(float2* pool, const Geom& g, long long rowstride, long long slot, long long istride, BatchRef br,
-                       int cap, unsigned int* vmax, cudaStream_t s) = 0;
-  virtual void x_c2r(const float2* src, float* dst, const Geom& g, long long srow, float scale, cudaStream_t s) = 0;
-  virtual void x_r2c(const float* src, float2* dst, const Geom& g, long long drow, cudaStream_t s) = 0;
-};
-
-// Host construction of a plan's stage-twiddle table (PlanTw layout), in double precision.
-template <class P>
-void plan_twiddles(std::vector<float2>& out) {
-  constexpr int N = P::N, R0 = P::R0, R1 = P::R1, R2 = P::R2;
-  out.assign(PlanTw<P>::SIZE, make_float2(1.f, 0.f));
-  auto w = [](long long j) {
-    const double ang = 2.0 * M_PI * (double)(j % N) / (double)N;
-    return make_float2((float)std::cos(ang), (float)std::sin(ang));
-  };
-  for (int n1 = 0; n1 < R1; ++n1)
-    for (int k0 = 0; k0 < R0; ++k0) out[n1 * R0 + k0] = w((long long)((n1 * k0) % (R0 * R1)) * R2);
-  if (R2 > 1)
-    for (int k1 = 0; k1 < R1; ++k1)
-      for (int n2 = 0; n2 < R2; ++n2)
-        for (int k0 = 0; k0 < R0; ++k0) out[R0 * R1 + k1 * (R0 * R2) + k0 + R0 * n2] = w((long long)n2 * (k0 + R0 * k1));
-}
-
-template <class K>
-int set_smem(K kernel, size_t bytes) {
-  if (bytes > 48 * 1024) {
-    cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
-    if (e != cudaSuccess) return fail(MHD_ERR_CUDA, std::string("cudaFuncSetAttribute: ") + cudaGetErrorString(e));
-  }
-  return MHD_OK;
-}
-
-// Resident CTAs of a kernel on the whole device (persistent grid size).
-template <class K>
-int resident_ctas(K kernel, int threads, size_t smem, int* out) {
-  int dev = 0, sms = 0, per = 0;
-  cudaGetDevice(&dev);
-  cudaError_t e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, threads, smem);
-  if (e != cudaSuccess) return fail(MHD_ERR_CUDA, std::string("occupancy query: ") + cudaGetErrorString(e));
-  *out = (per < 1 ? 1 : per) * sms;
-  return MHD_OK;
-}
-
-template <int N>
-struct Ops : OpsBase {
-  using C = typename Cfg<N>::C;
-  using R = typename Cfg<N>::R;
-  using RR = typename Reverse<R>::type;
-  using XC = XCfg<R>;
-  static constexpr int TX = Cfg<N>::TX;
-  static constexpr int MINB = Cfg<N>::COLMINB;
-  static constexpr int GROUPS = XC::TPG >= 64 ? 2 : 4;  // x row groups per CTA (128 threads)
-  static constexpr size_t kColSmem = sizeof(float2) * 2 * N * TX;
-  static constexpr size_t kRowSmem = sizeof(float2) * RowCfg<R>::TS;
-  size_t x_smem = 0;
-  int col_inv_ctas = 0, col_fwd_ctas = 0, x_ctas = 0;
-  float2* tw_all = nullptr;
-  const float2 *twC = nullptr, *twR = nullptr, *twRR = nullptr;
-
-  ~Ops() override {
-    if (tw_all) cudaFree(tw_all);
-  }
-
-  int setup(const Geom& g) override {
-    int rc = MHD_OK;
-    if (g.kx != kept_kx_of(N)) return fail(MHD_ERR_INVALID, "kept-mode count differs from the compiled row plan");
-    std::vector<float2> tc, tr, trr;
-    plan_twiddles<C>(tc);
-    plan_twiddles<R>(tr);
-    plan_twiddles<RR>(trr);
-    std::vector<float2> all(tc);
-    all.insert(all.end(), tr.begin(), tr.end());
-    all.insert(all.end(), trr.begin(), trr.end());
-    MHD_CUDA(cudaMalloc(&tw_all, all.size() * sizeof(float2)));
-    MHD_CUDA(cudaMemcpy(tw_all, all.data(), all.size() * sizeof(float2), cudaMemcpyHostToDevice));
-    twC = tw_all;
-    twR = tw_all + tc.size();
-    twRR = twR + tr.size();
-    x_smem = sizeof(float2) * (size_t)GROUPS * XC::group_words(g.kxp);
-    if ((rc = set_smem(col_pass_kernel<C, TX, +1, true, false, MINB>, kColSmem))) return rc;
-    if ((rc = set_smem(col_pass_kernel<C, TX, -1, false, true, MINB>, kColSmem))) return rc;
-    if ((rc = set_smem(x_fused_kernel<R, GROUPS>, x_smem))) return rc;
-    if ((rc = set_smem(x_c2r_kernel<R, Cfg<N>::ROWS>, kRowSmem * Cfg<N>::ROWS))) return rc;
-    if ((rc = set_smem(x_r2c_kernel<R, Cfg<N>::ROWS>, kRowSmem * Cfg<N>::ROWS))) return rc;
-    if ((rc = resident_ctas(col_pass_kernel<C, TX, +1, true, false, MINB>, TX * C::G, kColSmem, &col_inv_ctas))) return rc;
-    if ((rc = resident_ctas(col_pass_kernel<C, TX, -1, false, true, MINB>, TX * C::G, kColSmem, &col_fwd_ctas))) return rc;
-    if ((rc = resident_ctas(x_fused_kernel<R, GROUPS>, GROUPS * XC::TPG, x_smem, &x_ctas))) return rc;
-    return MHD_OK;
-  }
-  void col_inv(const ColArgs& a, const Geom& g, int outer, int nf, BatchRef br, int cap, cudaStream_t s) override {
-    ColWork w{(g.kx + TX - 1) / TX, outer, nf, g.k2};
-    const long long total = (long long)cap * w.tiles_x * w.outer * w.nf;
-    const int grid = (int)(total < col_inv_ctas ? total : col_inv_ctas);
-    col_pass_kernel<C, TX, +1, true, false, MINB><<<grid, TX * C::G, kColSmem, s>>>(a, g, w, br, twC);
-  }
-  void col_fwd(const ColArgs& a, const Geom& g, int outer, int nf, BatchRef br, int cap, cudaStream_t s) override {
-    ColWork w{(g.kx + TX - 1) / TX, outer, nf, N};
-    const long long total = (long long)cap * w.tiles_x * w.outer * w.nf;
-    const int grid = (int)(total < col_fwd_ctas ? total : col_fwd_ctas);
-    col_pass_kernel<C, TX, -1, false, true, MINB><<<grid, TX * C::G, kColSmem, s>>>(a, g, w, br, twC);
-  }
-  void x_fused(float2* pool, const Geom& g, long long rowstride, long long slot, long long istride, BatchRef br, int cap,
-               unsigned int* vmax, cudaStream_t s) override {
-    const long long groups = (long long)cap * N * N / XC::RPG;
-    const long long need = (groups + GROUPS - 1) / GROUPS;
-    const int grid = (int)(need < x_ctas ? need : x_ctas);
-    x_fused_kernel<R, GROUPS><<<grid, GROUPS * XC::TPG, x_smem, s>>>(pool, g, rowstride, slot, istride, br, twR, twRR, vmax);
-  }
-  void x_c2r(const float2* src, float* dst, const Geom& g, long long srow, float scale, cudaStream_t s) override {
-    constexpr int ROWS = Cfg<N>::ROWS;
-    const long long pairs = (long long)N * N / 2;
-    x_c2r_kernel<R, ROWS><<<(unsigned)(pairs / ROWS), ROWS * R::G, kRowSmem * ROWS, s>>>(src, dst, g, srow, scale, twR);
-  }
-  void x_r2c(const float* src, float2* dst, const Geom& g, long long drow, cudaStream_t s) override {
-    constexpr int ROWS = Cfg<N>::ROWS;
-    const long long pairs = (long long)N * N / 2;
-    x_r2c_kernel<R, ROWS><<<(unsigned)(pairs / ROWS), ROWS * R::G, kRowSmem * ROWS, s>>>(src, dst, g, drow, twR);
-  }
-};
 
 OpsBase* make_ops(int n) {
   switch (n) {
-    case 16: return new Ops<16>();
-    case 32: return new Ops<32>();
-    case 48: return new Ops<48>();
-    case 64: return new Ops<64>();
-    case 96: return new Ops<96>();
-    case 128: return new Ops<128>();
-    case 256: return new Ops<256>();
-    case 512: return new Ops<512>();
+    case 16: return make_ops_16();
+    case 32: return make_ops_32();
+    case 48: return make_ops_48();
+    case 64: return make_ops_64();
+    case 96: return make_ops_96();
+    case 128: return make_ops_128();
+    case 256: return make_ops_256();
+    case 512: return make_ops_512();
     default: return nullptr;
   }
 }
@@ -226,8 +90,7 @@ Geom make_geom(int n, double L) {
   return g;
 }
 
-// Kernel classes for per-launch timing.
-enum KClass { KC_ZINV = 0, KC_YINV, KC_XFUSED, KC_YFWD, KC_ZFWD, KC_RKEPI, KC_HERM, KC_OTHER, KC_COUNT };
+// Kernel classes for per-launch timing (KClass of ops.cuh).
 const char* kClassNames[KC_COUNT] = {"z_inverse", "y_inverse", "x_fused", "y_forward", "z_forward", "rk_epilogue",
                                      "herm_kx0", "other"};
 
@@ -270,6 +133,99 @@ long long class_bytes(const Geom& g) {
   return s.ref * 8 + s.phys * 4 + 6LL * g.n * 8 + (long long)s.diag_blocks * kDiagSlots * 8 + 256;
 }
 long long footprint(const Geom& g, int cap) { return class_bytes(g) + (long long)cap * slot_bytes(g); }
+
+}  // namespace
+
+namespace mhdgb {
+int report_error(int code, const std::string& msg) { return fail(code, msg); }
+}  // namespace mhdgb
+
+namespace {
+
+// ------------------------------------------------------------------------------------------
+// Autotuner results: the selected variant name of each tuned kernel class, keyed by device
+// (name and SM count) and grid size.  Kept for the process and, unless disabled, in a text file
+// ($MHDGB_TUNE_CACHE, else $XDG_CACHE_HOME/mhdgb/tune.txt, else $HOME/.cache/mhdgb/tune.txt; an
+// empty $MHDGB_TUNE_CACHE turns the file off).  One line per entry:
+//   <device name>|<sm count>|<n>|<variant of z_inverse>|...|<variant of z_forward>
+// ------------------------------------------------------------------------------------------
+std::mutex g_tune_mtx;
+std::map<std::string, std::vector<std::string>> g_tuned;
+
+std::string tune_file() {
+  const char* e = std::getenv("MHDGB_TUNE_CACHE");
+  if (e) return std::string(e);
+  const char* x = std::getenv("XDG_CACHE_HOME");
+  if (x && *x) return std::string(x) + "/mhdgb/tune.txt";
+  const char* h = std::getenv("HOME");
+  if (h && *h) return std::string(h) + "/.cache/mhdgb/tune.txt";
+  return "";
+}
+
+std::string tune_key(int device, int n) {
+  cudaDeviceProp prop;
+  if (cudaGetDeviceProperties(&prop, device) != cudaSuccess) return "";
+  std::string name(prop.name);
+  for (auto& c : name) if (c == '|' || c == '\n') c = ' ';
+  return name + "|" + std::to_string(prop.multiProcessorCount) + "|" + std::to_string(n);
+}
+
+std::vector<std::string> split_bar(const std::string& line) {
+  std::vector<std::string> out;
+  size_t a = 0;
+  while (true) {
+    size_t b = line.find('|', a);
+    out.push_back(line.substr(a, b == std::string::npos ? std::string::npos : b - a));
+    if (b == std::string::npos) break;
+    a = b + 1;
+  }
+  return out;
+}
+
+// variant names of a key: the process cache, else the file
+bool tuned_lookup(const std::string& key, std::vector<std::string>* names) {
+  std::lock_guard<std::mutex> lock(g_tune_mtx);
+  auto it = g_tuned.find(key);
+  if (it != g_tuned.end()) { *names = it->second; return true; }
+  const std::string path = tune_file();
+  if (path.empty()) return false;
+  std::FILE* f = std::fopen(path.c_str(), "r");
+  if (!f) return false;
+  char buf[4096];
+  bool found = false;
+  while (std::fgets(buf, sizeof(buf), f)) {
+    std::string line(buf);
+    while (!line.empty() && (line.back() == '\n' || line.back() == '\r')) line.pop_back();
+    std::vector<std::string> parts = split_bar(line);
+    if (parts.size() != 3 + (size_t)kTunedClasses) continue;
+    if (parts[0] + "|" + parts[1] + "|" + parts[2] != key) continue;
+    names->assign(parts.begin() + 3, parts.end());
+    found = true;  // the last line of a key wins
+  }
+  std::fclose(f);
+  if (found) g_tuned[key] = *names;
+  return found;
+}
+
+void tuned_store(const std::string& key, const std::vector<std::string>& names, bool persist) {
+  std::lock_guard<std::mutex> lock(g_tune_mtx);
+  g_tuned[key] = names;
+  if (!persist) return;
+  const std::string path = tune_file();
+  if (path.empty()) return;
+  const size_t slash = path.rfind('/');
+  if (slash != std::string::npos && slash > 0) {  // create the directory chain, ignore failures
+    std::string dir = path.substr(0, slash);
+    for (size_t p = 1; p <= dir.size(); ++p)
+      if (p == dir.size() || dir[p] == '/') mkdir(dir.substr(0, p).c_str(), 0755);
+  }
+  std::FILE* f = std::fopen(path.c_str(), "a");
+  if (!f) return;
+  std::string line = key;
+  for (const auto& nm : names) line += "|" + nm;
+  std::fprintf(f, "%s\n", line.c_str());
+  std::fclose(f);
+}
 
 }  // namespace
 
@@ -402,11 +358,11 @@ struct mhd_problem {
   // compact fields (src + slot*sI, nf fields at stride FS) -> colbuf slots 0..nf-1
   int z_inverse(const float2* src, long long sI, int nf, BatchRef br) {
     ColArgs a{src, colbuf, FS(), (long long)g.kxp, (long long)g.k2 * g.kxp, (long long)g.kxp, SLK(), AZ(), sI, sz.colbuf};
-    return launch(KC_ZINV, [&] { ops->col_inv(a, g, g.k2, nf, br, cap, stream); });
+    return launch(KC_ZINV, [&] { ops->col(KC_ZINV, a, g, g.k2, nf, br, cap, stream); });
   }
   int y_inverse(int nf, BatchRef br) {
     ColArgs a{colbuf, rowbuf, (long long)g.kxp, AZ(), SLK(), (long long)g.kxp, BZ(), SLK(), sz.colbuf, sz.rowbuf};
-    return launch(KC_YINV, [&] { ops->col_inv(a, g, g.n, nf, br, cap, stream); });
+    return launch(KC_YINV, [&] { ops->col(KC_YINV, a, g, g.n, nf, br, cap, stream); });
   }
   int x_fused(BatchRef br, unsigned int* vmax) {
     // the six field rows of a physical row are contiguous (slot stride == kxp)
@@ -414,12 +370,12 @@ struct mhd_problem {
   }
   int y_forward(int nf, BatchRef br) {
     ColArgs a{rowbuf, colbuf, (long long)g.kxp, BZ(), SLK(), (long long)g.kxp, AZ(), SLK(), sz.rowbuf, sz.colbuf};
-    return launch(KC_YFWD, [&] { ops->col_fwd(a, g, g.n, nf, br, cap, stream); });
+    return launch(KC_YFWD, [&] { ops->col(KC_YFWD, a, g, g.n, nf, br, cap, stream); });
   }
   // colbuf slots -> compact planes (nf fields/products) at dst + slot*dI, pruned output
   int z_forward(float2* dst, long long dI, int nf, BatchRef br) {
     ColArgs a{colbuf, dst, (long long)g.kxp, SLK(), AZ(), FS(), (long long)g.kxp, (long long)g.k2 * g.kxp, sz.colbuf, dI};
-    return launch(KC_ZFWD, [&] { ops->col_fwd(a, g, g.k2, nf, br, cap, stream); });
+    return launch(KC_ZFWD, [&] { ops->col(KC_ZFWD, a, g, g.k2, nf, br, cap, stream); });
   }
   // Stage epilogue: RHS from the 8 compact product planes (in rowbuf) and the stage state X.
   int epilogue(const float2* X, int op, float hf, float ca, float cb, BatchRef br) {
@@ -504,6 +460,81 @@ struct mhd_problem {
         unsigned int* out = dvmax + 2 * s + (f < 3 ? 0 : 1);
         if ((rc = launch(KC_OTHER, [&] { maxabs_into_kernel<<<1216, 256, 0, stream>>>(phys, sz.phys, out); }))) return rc;
       }
+    return MHD_OK;
+  }
+  // ---- autotuner: each candidate is timed inside real right-hand-side evaluations (z_inverse ..
+  // z_forward, the kx = 0 Hermitian part and the epilogue in its RHS-only form, which writes
+  // only the scratch pass buffers and acc, never the state), with CUDA events around every
+  // launch.  Round r selects variant r of every class that has one (the others keep their
+  // current choice); the per-class time of a candidate is the best over two sweeps.
+  int tune_rounds(std::vector<std::vector<double>>& best) {
+    const BatchRef br = active_ref();
+    int maxv = 0;
+    for (int c = 0; c < kTunedClasses; ++c) maxv = std::max(maxv, ops->variant_count(c));
+    best.assign(kTunedClasses, std::vector<double>(maxv, 1e300));
+    int base[kTunedClasses];
+    std::memcpy(base, ops->sel, sizeof(base));
+    int rc = MHD_OK;
+    profiling = true;
+    for (int sweep = 0; sweep < 2 && rc == MHD_OK; ++sweep)
+      for (int r = 0; r < maxv && rc == MHD_OK; ++r) {
+        for (int c = 0; c < kTunedClasses; ++c) ops->sel[c] = ops->variant_ok(c, r) ? r : base[c];
+        // one evaluation to warm up, then three timed ones
+        for (int k = 0; k < 4 && rc == MHD_OK; ++k) {
+          if (k == 1) {
+            if ((rc = fold_records())) break;
+            for (int c = 0; c < KC_COUNT; ++c) { prof_launches[c] = 0; prof_ms[c] = 0; }
+          }
+          rc = rhs(sol, OP_RHS, 0.f, 0.f, 0.f, br);
+        }
+        if (rc == MHD_OK) rc = fold_records();
+        for (int c = 0; c < kTunedClasses && rc == MHD_OK; ++c)
+          if (ops->variant_ok(c, r) && prof_launches[c] > 0)
+            best[c][r] = std::min(best[c][r], prof_ms[c] / prof_launches[c]);
+      }
+    profiling = false;
+    for (auto& rec : recs) { pool.push_back(rec.a); pool.push_back(rec.b); }
+    recs.clear();
+    for (int c = 0; c < KC_COUNT; ++c) { prof_launches[c] = 0; prof_ms[c] = 0; }
+    std::memcpy(ops->sel, base, sizeof(base));
+    return rc;
+  }
+  std::vector<std::string> selected_names() const {
+    std::vector<std::string> v;
+    for (int c = 0; c < kTunedClasses; ++c) v.push_back(ops->variant_name(c, ops->sel[c]));
+    return v;
+  }
+  int apply_names(const std::vector<std::string>& names) {
+    if ((int)names.size() != kTunedClasses) return MHD_ERR_INVALID;
+    int saved[kTunedClasses];
+    std::memcpy(saved, ops->sel, sizeof(saved));
+    for (int c = 0; c < kTunedClasses; ++c)
+      if (ops->select_by_name(c, names[c]) != MHD_OK) {  // a stale entry: keep the defaults
+        std::memcpy(ops->sel, saved, sizeof(saved));
+        g_err.clear();
+        return MHD_ERR_INVALID;
+      }
+    invalidate_graph();
+    return MHD_OK;
+  }
+  int autotune(bool force, bool persist) {
+    if (profiling) return fail(MHD_ERR_STATE, "autotune does not run with per-kernel profiling enabled");
+    int rc;
+    if ((rc = sync_lists())) return rc;
+    const std::string key = tune_key(device, g.n);
+    std::vector<std::string> names;
+    if (!force && !key.empty() && tuned_lookup(key, &names) && apply_names(names) == MHD_OK) return MHD_OK;
+    if (active.empty()) return fail(MHD_ERR_STATE, "autotune needs at least one active slot");
+    std::vector<std::vector<double>> best;
+    if ((rc = tune_rounds(best))) return rc;
+    for (int c = 0; c < kTunedClasses; ++c) {
+      int pick = ops->sel[c];
+      for (int i = 0; i < (int)best[c].size(); ++i)
+        if (best[c][i] < best[c][pick]) pick = i;
+      ops->sel[c] = pick;
+    }
+    if (!key.empty()) tuned_store(key, selected_names(), persist);
+    invalidate_graph();
     return MHD_OK;
   }
   int build_graph() {
@@ -618,6 +649,13 @@ int create_class(const mhd_params* params, int cap, mhd_handle* out) {
   h->ops.reset(make_ops(params->n));
   if (!h->ops) return fail(MHD_ERR_INVALID, "no plan for n");
   if ((rc = h->ops->setup(h->g))) return rc;
+  {
+    // a selection the autotuner made earlier for this device and grid size (this process or the
+    // tuning file); the defaults otherwise
+    const std::string key = tune_key(h->device, h->g.n);
+    std::vector<std::string> names;
+    if (!key.empty() && tuned_lookup(key, &names)) h->apply_names(names);
+  }
   MHD_CUDA(cudaStreamCreateWithFlags(&h->own_stream, cudaStreamNonBlocking));
   h->stream = h->own_stream;
   const Sizes& s = h->sz;
@@ -1054,6 +1092,37 @@ int mhd_time_steps(mhd_handle h, int nsteps, double* ms) {
   if (rc) return rc;
   if (e != cudaSuccess) return fail(MHD_ERR_CUDA, std::string("cudaEventSynchronize: ") + cudaGetErrorString(e));
   *ms = f;
+  return MHD_OK;
+}
+
+int mhd_autotune(mhd_handle h, int flags) {
+  int rc = check_handle(h);
+  if (rc) return rc;
+  return h->autotune((flags & MHD_TUNE_FORCE) != 0, (flags & MHD_TUNE_NO_FILE) == 0);
+}
+
+int mhd_variant_count(mhd_handle h, int cls, int* count) {
+  if (!h || !count) return fail(MHD_ERR_INVALID, "null argument");
+  if (cls < 0 || cls >= kTunedClasses) return fail(MHD_ERR_INVALID, "class must be 0..4 (the FFT pass classes)");
+  *count = h->ops->variant_count(cls);
+  return MHD_OK;
+}
+
+int mhd_variant_name(mhd_handle h, int cls, int idx, char* buf, int len) {
+  if (!h || !buf || len < 1) return fail(MHD_ERR_INVALID, "null argument");
+  if (cls < 0 || cls >= kTunedClasses) return fail(MHD_ERR_INVALID, "class must be 0..4 (the FFT pass classes)");
+  if (idx < 0) idx = h->ops->sel[cls];
+  if (idx >= h->ops->variant_count(cls)) return fail(MHD_ERR_INVALID, "no such variant");
+  const std::string name = h->ops->variant_name(cls, idx);
+  std::snprintf(buf, (size_t)len, "%s", name.c_str());
+  return MHD_OK;
+}
+
+int mhd_select_variant(mhd_handle h, int cls, int idx) {
+  int rc = check_handle(h);
+  if (rc) return rc;
+  if ((rc = h->ops->select(cls, idx))) return rc;
+  h->invalidate_graph();
   return MHD_OK;
 }
 

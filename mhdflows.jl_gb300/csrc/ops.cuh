@@ -1,0 +1,183 @@
+// Per-grid-size pass kernels and their variants (sm_103a).
+//
+// Every grid size has a default configuration of each FFT pass.  For the sizes where the choice
+// matters there are further candidates (radix plans, kx columns per tile, transforms per
+// exchange round, occupancy bounds); mhd_autotune times them on the device and selects one per
+// kernel class.  Each grid size is compiled in its own translation unit (ops_*.cu) through the
+// make_ops_<n> factories below.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <map>
+#include <string>
+#include <vector>
+
+#include "passes.cuh"
+
+namespace mhdgb {
+
+// Kernel classes of one right-hand-side evaluation (also the per-launch profiling classes).
+enum KClass { KC_ZINV = 0, KC_YINV, KC_XFUSED, KC_YFWD, KC_ZFWD, KC_RKEPI, KC_HERM, KC_OTHER, KC_COUNT };
+constexpr int kTunedClasses = 5;  // z_inverse .. z_forward
+
+// Error reporting of the library (defined with the C ABI): stores the message, returns code.
+int report_error(int code, const std::string& msg);
+
+using XFn = void (*)(float2*, Geom, long long, long long, long long, BatchRef, const float2*, const float2*,
+                     unsigned int*);
+using ColFn = void (*)(ColArgs, Geom, ColWork, BatchRef, const float2*);
+using C2RFn = void (*)(const float2*, float*, Geom, long long, float, const float2*);
+using R2CFn = void (*)(const float*, float2*, Geom, long long, const float2*);
+
+struct XVariant {
+  std::string name;
+  XFn fn = nullptr;
+  int threads = 0, rpg = 1, groups = 1;
+  int (*group_words)(int) = nullptr;  // shared-memory words of one row group for a padded row length
+  size_t tw = 0, twr = 0;             // offsets of the plan's twiddles and of its reverse's
+  size_t smem = 0;
+  int ctas = 0;                       // resident CTAs on the device (0: does not fit)
+};
+
+struct ColVariant {
+  std::string name;
+  ColFn inv = nullptr, fwd = nullptr;
+  int threads = 0, tx = 0;
+  size_t tw = 0;
+  size_t smem = 0;
+  int ctas_inv = 0, ctas_fwd = 0;
+};
+
+class OpsBase {
+ public:
+  virtual ~OpsBase();
+  int setup(const Geom& g);
+  // cap: upper bound of the active instances (the grid covers cap instances; the kernels read
+  // the actual count from the BatchRef)
+  void col(int cls, const ColArgs& a, const Geom& g, int outer, int nf, BatchRef br, int cap, cudaStream_t s) const;
+  void x_fused(float2* pool, const Geom& g, long long rowstride, long long slot, long long istride, BatchRef br,
+               int cap, unsigned int* vmax, cudaStream_t s) const;
+  void x_c2r(const float2* src, float* dst, const Geom& g, long long srow, float scale, cudaStream_t s) const;
+  void x_r2c(const float* src, float2* dst, const Geom& g, long long drow, cudaStream_t s) const;
+
+  int n = 0;
+  std::vector<XVariant> xv;
+  std::vector<ColVariant> cv;
+  int sel[kTunedClasses] = {0, 0, 0, 0, 0};  // selected variant of each tuned class
+  int variant_count(int cls) const;
+  bool variant_ok(int cls, int i) const;
+  std::string variant_name(int cls, int i) const;
+  int select(int cls, int i);                 // MHD_OK or MHD_ERR_INVALID
+  int select_by_name(int cls, const std::string& name);
+
+ protected:
+  // plain row transforms (staging of set_physical / get_physical / diagnostics)
+  C2RFn c2r = nullptr;
+  R2CFn r2c = nullptr;
+  int rows = 1, row_threads = 0;
+  size_t row_smem = 0, row_tw = 0;
+  std::vector<float2> tw_host;
+  std::map<std::string, size_t> tw_index;
+  float2* tw_dev = nullptr;
+};
+
+// Host construction of a plan's stage-twiddle table (PlanTw layout of fft_core.cuh), double
+// precision rounded to FP32.
+template <class P>
+void plan_twiddles(std::vector<float2>& out) {
+  constexpr int N = P::N, R0 = P::R0, R1 = P::R1, R2 = P::R2;
+  out.assign(PlanTw<P>::SIZE, make_float2(1.f, 0.f));
+  auto w = [](long long j) {
+    const double ang = 2.0 * 3.14159265358979323846 * (double)(j % N) / (double)N;
+    return make_float2((float)std::cos(ang), (float)std::sin(ang));
+  };
+  for (int n1 = 0; n1 < R1; ++n1)
+    for (int k0 = 0; k0 < R0; ++k0) out[n1 * R0 + k0] = w((long long)((n1 * k0) % (R0 * R1)) * R2);
+  if (R2 > 1)
+    for (int k1 = 0; k1 < R1; ++k1)
+      for (int n2 = 0; n2 < R2; ++n2)
+        for (int k0 = 0; k0 < R0; ++k0) out[R0 * R1 + k1 * (R0 * R2) + k0 + R0 * n2] = w((long long)n2 * (k0 + R0 * k1));
+}
+
+template <class P>
+std::string plan_name() {
+  std::string s = std::to_string(P::R0) + "x" + std::to_string(P::R1);
+  if (P::R2 > 1) s += "x" + std::to_string(P::R2);
+  return s + "/g" + std::to_string(P::G);
+}
+
+// Builder of one grid size's variant lists (used by the ops_*.cu translation units).
+template <int N>
+class Ops : public OpsBase {
+ public:
+  Ops() { n = N; }
+
+  template <class P>
+  size_t twiddles() {
+    const std::string key = plan_name<P>();
+    auto it = tw_index.find(key);
+    if (it != tw_index.end()) return it->second;
+    std::vector<float2> t;
+    plan_twiddles<P>(t);
+    const size_t off = tw_host.size();
+    tw_host.insert(tw_host.end(), t.begin(), t.end());
+    tw_index[key] = off;
+    return off;
+  }
+
+  // x rows: plan R (inverse; the forward uses its reverse), GROUPS row groups per CTA, NTI / NTF
+  // transforms per exchange round, MINB CTAs per SM.
+  template <class R, int GROUPS, int NTI, int NTF, int MINB>
+  void add_x() {
+    constexpr int NTS = NTI > NTF ? NTI : NTF;
+    using XC = XCfg<R, NTS>;
+    XVariant v;
+    v.name = "x:" + plan_name<R>() + "/nt" + std::to_string(NTI) + std::to_string(NTF) + "/c" +
+             std::to_string(GROUPS) + "/b" + std::to_string(MINB);
+    v.fn = x_fused_kernel<R, GROUPS, NTI, NTF, MINB>;
+    v.threads = GROUPS * XC::TPG;
+    v.rpg = XC::RPG;
+    v.groups = GROUPS;
+    v.group_words = &XC::group_words;
+    v.tw = twiddles<R>();
+    v.twr = twiddles<typename Reverse<R>::type>();
+    xv.push_back(v);
+  }
+
+  // column passes (y and z): plan C, TX kx columns per tile, MINB CTAs per SM
+  template <class C, int TX, int MINB>
+  void add_col() {
+    ColVariant c;
+    c.name = "col:" + plan_name<C>() + "/tx" + std::to_string(TX) + "/b" + std::to_string(MINB);
+    c.inv = col_pass_kernel<C, TX, +1, true, false, MINB>;
+    c.fwd = col_pass_kernel<C, TX, -1, false, true, MINB>;
+    c.threads = TX * C::G;
+    c.tx = TX;
+    c.smem = sizeof(float2) * 2 * (size_t)N * TX;
+    c.tw = twiddles<C>();
+    cv.push_back(c);
+  }
+
+  // plain row c2r / r2c kernels, ROWS row pairs per CTA
+  template <class R, int ROWS>
+  void set_rows() {
+    c2r = x_c2r_kernel<R, ROWS>;
+    r2c = x_r2c_kernel<R, ROWS>;
+    rows = ROWS;
+    row_threads = ROWS * R::G;
+    row_smem = sizeof(float2) * (size_t)RowCfg<R>::TS * ROWS;
+    row_tw = twiddles<R>();
+  }
+};
+
+OpsBase* make_ops_16();
+OpsBase* make_ops_32();
+OpsBase* make_ops_48();
+OpsBase* make_ops_64();
+OpsBase* make_ops_96();
+OpsBase* make_ops_128();
+OpsBase* make_ops_256();
+OpsBase* make_ops_512();
+
+}  // namespace mhdgb

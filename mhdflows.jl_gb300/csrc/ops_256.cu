@@ -1,0 +1,20 @@
+// Pass kernels of the 256^3 grid: default configuration first, then autotuner candidates.
+#include "ops.cuh"
+
+namespace mhdgb {
+
+OpsBase* make_ops_256() {
+  auto* o = new Ops<256>();
+  o->add_col<Plan<256, 16, 16, 16>, 16, 3>();
+  o->add_col<Plan<256, 16, 16, 16>, 8, 4>();
+  o->add_col<Plan<256, 32, 8, 8, 4>, 8, 3>();
+  o->add_col<Plan<256, 32, 8, 8, 4>, 16, 2>();
+  o->add_x<Plan<256, 32, 8, 8, 4>, 4, 1, 1, 4>();
+  o->add_x<Plan<256, 32, 8, 8, 4>, 4, 3, 1, 3>();
+  o->add_x<Plan<256, 32, 8, 8, 4>, 4, 3, 2, 3>();
+  o->add_x<Plan<256, 16, 16, 16>, 4, 1, 1, 2>();
+  o->set_rows<Plan<256, 32, 8, 8, 4>, 4>();
+  return o;
+}
+
+}  // namespace mhdgb

@@ -1,0 +1,18 @@
+// Pass kernels of the 512^3 grid: default configuration first, then autotuner candidates.
+#include "ops.cuh"
+
+namespace mhdgb {
+
+OpsBase* make_ops_512() {
+  auto* o = new Ops<512>();
+  o->add_col<Plan<512, 32, 16, 8, 4>, 16, 1>();
+  o->add_col<Plan<512, 32, 16, 8, 4>, 8, 2>();
+  o->add_col<Plan<512, 64, 8, 8, 8>, 8, 1>();
+  o->add_x<Plan<512, 64, 8, 8, 8>, 2, 1, 1, 4>();
+  o->add_x<Plan<512, 32, 16, 8, 4>, 4, 1, 1, 2>();
+  o->add_x<Plan<512, 32, 8, 8, 8>, 4, 1, 1, 2>();
+  o->set_rows<Plan<512, 64, 8, 8, 8>, 2>();
+  return o;
+}
+
+}  // namespace mhdgb

@@ -1,0 +1,136 @@
+// Set-up, launch and selection of the pass-kernel variants of one grid size.
+#include <string>
+
+#include "../../include/mhdgb.h"
+#include "ops.cuh"
+
+namespace mhdgb {
+
+OpsBase::~OpsBase() {
+  if (tw_dev) cudaFree(tw_dev);
+}
+
+namespace {
+
+int set_smem(const void* fn, size_t bytes) {
+  if (bytes <= 48 * 1024) return MHD_OK;
+  cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  if (e != cudaSuccess) return report_error(MHD_ERR_CUDA, std::string("cudaFuncSetAttribute: ") + cudaGetErrorString(e));
+  return MHD_OK;
+}
+
+// Resident CTAs of a kernel on the whole device (persistent grid size); 0 when it does not fit.
+int resident_ctas(const void* fn, int threads, size_t smem, int sms, int* out) {
+  int per = 0;
+  cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fn, threads, smem);
+  if (e != cudaSuccess) return report_error(MHD_ERR_CUDA, std::string("occupancy query: ") + cudaGetErrorString(e));
+  *out = per * sms;
+  return MHD_OK;
+}
+
+bool is_col(int cls) { return cls == KC_ZINV || cls == KC_YINV || cls == KC_YFWD || cls == KC_ZFWD; }
+bool is_inv(int cls) { return cls == KC_ZINV || cls == KC_YINV; }
+
+}  // namespace
+
+int OpsBase::setup(const Geom& g) {
+  if (g.kx != kept_kx_of(n) || g.kp != kept_kx_of(n) || g.kn != kept_kn_of(n))
+    return report_error(MHD_ERR_INVALID, "kept-mode counts differ from the compiled pass plans");
+  int rc = MHD_OK, dev = 0, sms = 0, smem_max = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&smem_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  if (e != cudaSuccess) return report_error(MHD_ERR_CUDA, std::string("device query: ") + cudaGetErrorString(e));
+  e = cudaMalloc(&tw_dev, tw_host.size() * sizeof(float2));
+  if (e != cudaSuccess) return report_error(MHD_ERR_OOM, std::string("twiddle tables: ") + cudaGetErrorString(e));
+  e = cudaMemcpy(tw_dev, tw_host.data(), tw_host.size() * sizeof(float2), cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) return report_error(MHD_ERR_CUDA, std::string("twiddle upload: ") + cudaGetErrorString(e));
+  for (auto& x : xv) {
+    x.smem = sizeof(float2) * (size_t)x.groups * x.group_words(g.kxp);
+    x.ctas = 0;
+    if ((int)x.smem > smem_max) continue;
+    if ((rc = set_smem((const void*)x.fn, x.smem))) return rc;
+    if ((rc = resident_ctas((const void*)x.fn, x.threads, x.smem, sms, &x.ctas))) return rc;
+  }
+  for (auto& c : cv) {
+    c.ctas_inv = c.ctas_fwd = 0;
+    if ((int)c.smem > smem_max) continue;
+    if ((rc = set_smem((const void*)c.inv, c.smem))) return rc;
+    if ((rc = set_smem((const void*)c.fwd, c.smem))) return rc;
+    if ((rc = resident_ctas((const void*)c.inv, c.threads, c.smem, sms, &c.ctas_inv))) return rc;
+    if ((rc = resident_ctas((const void*)c.fwd, c.threads, c.smem, sms, &c.ctas_fwd))) return rc;
+  }
+  if ((rc = set_smem((const void*)c2r, row_smem))) return rc;
+  if ((rc = set_smem((const void*)r2c, row_smem))) return rc;
+  // the default of each class is its first variant that fits on this device
+  for (int cls = 0; cls < kTunedClasses; ++cls) {
+    int i = 0;
+    while (i < variant_count(cls) && !variant_ok(cls, i)) ++i;
+    if (i == variant_count(cls)) return report_error(MHD_ERR_CUDA, "no pass-kernel variant fits on this device");
+    sel[cls] = i;
+  }
+  return MHD_OK;
+}
+
+int OpsBase::variant_count(int cls) const {
+  if (cls == KC_XFUSED) return (int)xv.size();
+  return is_col(cls) ? (int)cv.size() : 0;
+}
+
+bool OpsBase::variant_ok(int cls, int i) const {
+  if (i < 0 || i >= variant_count(cls)) return false;
+  if (cls == KC_XFUSED) return xv[i].ctas > 0;
+  return is_inv(cls) ? cv[i].ctas_inv > 0 : cv[i].ctas_fwd > 0;
+}
+
+std::string OpsBase::variant_name(int cls, int i) const {
+  if (i < 0 || i >= variant_count(cls)) return "";
+  return cls == KC_XFUSED ? xv[i].name : cv[i].name;
+}
+
+int OpsBase::select(int cls, int i) {
+  if (cls < 0 || cls >= kTunedClasses || !variant_ok(cls, i))
+    return report_error(MHD_ERR_INVALID, "no such kernel variant (class " + std::to_string(cls) + ", index " +
+                                             std::to_string(i) + ")");
+  sel[cls] = i;
+  return MHD_OK;
+}
+
+int OpsBase::select_by_name(int cls, const std::string& name) {
+  for (int i = 0; i < variant_count(cls); ++i)
+    if (variant_name(cls, i) == name) return select(cls, i);
+  return report_error(MHD_ERR_INVALID, "no kernel variant named " + name);
+}
+
+void OpsBase::col(int cls, const ColArgs& a, const Geom& g, int outer, int nf, BatchRef br, int cap,
+                  cudaStream_t s) const {
+  const ColVariant& c = cv[sel[cls]];
+  const bool inv = is_inv(cls);
+  const ColWork w{(g.kx + c.tx - 1) / c.tx, outer, nf, inv ? g.k2 : n};
+  const long long total = (long long)cap * w.tiles_x * w.outer * w.nf;
+  const int ctas = inv ? c.ctas_inv : c.ctas_fwd;
+  const int grid = (int)(total < ctas ? total : ctas);
+  const ColFn f = inv ? c.inv : c.fwd;
+  f<<<grid, c.threads, c.smem, s>>>(a, g, w, br, tw_dev + c.tw);
+}
+
+void OpsBase::x_fused(float2* pool, const Geom& g, long long rowstride, long long slot, long long istride,
+                      BatchRef br, int cap, unsigned int* vmax, cudaStream_t s) const {
+  const XVariant& x = xv[sel[KC_XFUSED]];
+  const long long groups = (long long)cap * n * n / x.rpg;
+  const long long need = (groups + x.groups - 1) / x.groups;
+  const int grid = (int)(need < x.ctas ? need : x.ctas);
+  x.fn<<<grid, x.threads, x.smem, s>>>(pool, g, rowstride, slot, istride, br, tw_dev + x.tw, tw_dev + x.twr, vmax);
+}
+
+void OpsBase::x_c2r(const float2* src, float* dst, const Geom& g, long long srow, float scale, cudaStream_t s) const {
+  const long long pairs = (long long)n * n / 2;
+  c2r<<<(unsigned)(pairs / rows), row_threads, row_smem, s>>>(src, dst, g, srow, scale, tw_dev + row_tw);
+}
+
+void OpsBase::x_r2c(const float* src, float2* dst, const Geom& g, long long drow, cudaStream_t s) const {
+  const long long pairs = (long long)n * n / 2;
+  r2c<<<(unsigned)(pairs / rows), row_threads, row_smem, s>>>(src, dst, g, drow, tw_dev + row_tw);
+}
+
+}  // namespace mhdgb

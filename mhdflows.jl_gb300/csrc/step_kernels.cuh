@@ -1,0 +1,346 @@
+// Spectral epilogue, layout conversion, CFL and diagnostics kernels of the MHD step (sm_103a).
+// Included by the library's main translation unit only (the non-template kernels here have one
+// definition); the FFT pass kernels are in passes.cuh.
+#pragma once
+#include "passes.cuh"
+
+namespace mhdgb {
+
+// Runge-Kutta stage operations of the epilogue.
+enum StageOp : int {
+  OP_RHS = 0,       // out <- R
+  OP_RK4_FIRST = 1, // acc <- R/6 ; xn <- sol + h R            (X = sol)
+  OP_RK4_MID = 2,   // acc <- acc + R/3 ; xn <- sol + h R
+  OP_RK4_LAST = 3,  // sol <- sol + dt (acc + R/6)
+  OP_LS_FIRST = 4,  // du <- dt R ; u <- u + b du              (X = u)
+  OP_LS = 5,        // du <- a du + dt R ; u <- u + b du
+};
+
+// ------------------------------------------------------------------------------------------
+// Streaming right-hand side + Runge-Kutta stage update over the compact retained band.
+// prod: compact spectra of the 8 products [p][kz'][ky'][kx] (Dxz Dyz Txy Txz Tyz Axy Axz Ayz).
+// Momentum: R_u = i (V - k (k.V)/k^2) - nu k^2 X_u with V = (kx Dxz + ky Txy + kz Txz,
+// kx Txy + ky Dyz + kz Tyz, kx Txz + ky Tyz) (the stress tensor minus Tzz*I, whose gradient the
+// projection removes).  Induction: R_b = i k x E - eta k^2 X_b with E = (Ayz, -Axz, Axy) = u x B.
+// ------------------------------------------------------------------------------------------
+struct RkArgs {
+  const float2* prod;   // 8 compact planes (slot stride prodI)
+  const float2* X;      // stage state (6 fields, slot stride stI)
+  const float2* H;      // Hermitian part of X on the kx = 0 plane, [f][kz'][ky'] (slot stride hI)
+  float2* sol;          // RK4 step-start state
+  float2* acc;          // RK4 accumulator / LSRK4 du / OP_RHS output
+  float2* xn;           // RK4 next stage state / LSRK4 u
+  const SlotParams* sp; // per-slot nu, eta, dt
+  long long fs;         // compact field stride (complex elements)
+  long long stI, prodI, hI;
+  float hf;             // RK4 stage fraction of dt (1/2 or 1)
+  float ca, cb;         // LSRK4 coefficients of the stage
+  float pscale;         // 1/n^6: the column and row passes are unnormalised in both directions
+  int op;
+};
+
+struct RkSlot {
+  float2* sol;
+  float2* acc;
+  float2* xn;
+  float h, dt, ca, cb;
+};
+
+template <int OP>
+__device__ __forceinline__ void rk_apply(const RkSlot& a, long long o, float2 x, float2 R) {
+  if constexpr (OP == OP_RHS) {
+    a.acc[o] = R;
+  } else if constexpr (OP == OP_RK4_FIRST) {
+    a.acc[o] = make_float2(R.x / 6.f, R.y / 6.f);
+    a.xn[o] = make_float2(x.x + a.h * R.x, x.y + a.h * R.y);
+  } else if constexpr (OP == OP_RK4_MID) {
+    const float2 s = a.sol[o], q = a.acc[o];
+    a.acc[o] = make_float2(q.x + R.x / 3.f, q.y + R.y / 3.f);
+    a.xn[o] = make_float2(s.x + a.h * R.x, s.y + a.h * R.y);
+  } else if constexpr (OP == OP_RK4_LAST) {
+    const float2 s = a.sol[o], q = a.acc[o];
+    const float2 tot = make_float2(q.x + R.x / 6.f, q.y + R.y / 6.f);
+    a.sol[o] = make_float2(s.x + a.dt * tot.x, s.y + a.dt * tot.y);
+  } else if constexpr (OP == OP_LS_FIRST) {
+    const float2 du = make_float2(a.dt * R.x, a.dt * R.y);
+    a.acc[o] = du;
+    a.xn[o] = make_float2(x.x + a.cb * du.x, x.y + a.cb * du.y);
+  } else if constexpr (OP == OP_LS) {
+    const float2 q = a.acc[o];
+    const float2 du = make_float2(a.ca * q.x + a.dt * R.x, a.ca * q.y + a.dt * R.y);
+    a.acc[o] = du;
+    a.xn[o] = make_float2(x.x + a.cb * du.x, x.y + a.cb * du.y);
+  }
+}
+
+// grid (ceil(kx / blockDim.x), k2, k2): one thread per retained mode, no index division.
+template <int OP>
+__global__ void __launch_bounds__(256) rk_epilogue_kernel(RkArgs a, Geom geo, BatchRef br) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  if (x >= geo.kx) return;
+  const int inst = blockIdx.z / geo.k2;
+  if (inst >= *br.count) return;
+  const int slot = br.list[inst];
+  const int jy = blockIdx.y, jz = blockIdx.z - inst * geo.k2;
+  const long long fs = a.fs;
+  const long long i = ((long long)jz * geo.k2 + jy) * geo.kxp + x;
+  const SlotParams sp = a.sp[slot];
+  const long long so = slot * a.stI;
+  RkSlot rs{a.sol + so, a.acc + so, a.xn + so, a.hf * sp.dt, sp.dt, a.ca, a.cb};
+  const float2* X = a.X + so;
+  const float2* prod = a.prod + slot * a.prodI;
+  const float kxv = geo.kscale * (float)x;
+  const float kyv = geo.kscale * (float)signed_of_kept(geo, jy);
+  const float kzv = geo.kscale * (float)signed_of_kept(geo, jz);
+  const float k2 = kxv * kxv + kyv * kyv + kzv * kzv;
+  float2 p[8];
+#pragma unroll
+  for (int q = 0; q < 8; ++q) p[q] = cscale(__ldcs(prod + q * fs + i), a.pscale);
+  float2 xv[6], xd[6];
+#pragma unroll
+  for (int c = 0; c < 6; ++c) xv[c] = xd[c] = X[c * fs + i];
+  if (x == 0) {
+    const long long p = (long long)jz * geo.k2 + jy, pl = (long long)geo.k2 * geo.k2;
+    const float2* H = a.H + slot * a.hI;
+#pragma unroll
+    for (int c = 0; c < 6; ++c) xd[c] = H[c * pl + p];
+  }
+  const float2 dxz = p[0], dyz = p[1], txy = p[2], txz = p[3], tyz = p[4];
+  const float2 axy = p[5], axz = p[6], ayz = p[7];
+  float2 Vx, Vy, Vz;
+  Vx.x = kxv * dxz.x + kyv * txy.x + kzv * txz.x;  Vx.y = kxv * dxz.y + kyv * txy.y + kzv * txz.y;
+  Vy.x = kxv * txy.x + kyv * dyz.x + kzv * tyz.x;  Vy.y = kxv * txy.y + kyv * dyz.y + kzv * tyz.y;
+  Vz.x = kxv * txz.x + kyv * tyz.x;                Vz.y = kxv * txz.y + kyv * tyz.y;
+  const float ik2 = k2 > 0.f ? 1.0f / k2 : 0.f;
+  const float kvx = (kxv * Vx.x + kyv * Vy.x + kzv * Vz.x) * ik2;
+  const float kvy = (kxv * Vx.y + kyv * Vy.y + kzv * Vz.y) * ik2;
+  float2 nl[6];
+  nl[0] = make_float2(-(Vx.y - kxv * kvy), Vx.x - kxv * kvx);
+  nl[1] = make_float2(-(Vy.y - kyv * kvy), Vy.x - kyv * kvx);
+  nl[2] = make_float2(-(Vz.y - kzv * kvy), Vz.x - kzv * kvx);
+  // W = i k x E with E = (Ayz, -Axz, Axy): Wx = i(ky Axy + kz Axz), Wy = i(kz Ayz - kx Axy), Wz = -i(kx Axz + ky Ayz)
+  const float2 wx = make_float2(kyv * axy.x + kzv * axz.x, kyv * axy.y + kzv * axz.y);
+  const float2 wy = make_float2(kzv * ayz.x - kxv * axy.x, kzv * ayz.y - kxv * axy.y);
+  const float2 wz = make_float2(-(kxv * axz.x + kyv * ayz.x), -(kxv * axz.y + kyv * ayz.y));
+  nl[3] = make_float2(-wx.y, wx.x);
+  nl[4] = make_float2(-wy.y, wy.x);
+  nl[5] = make_float2(-wz.y, wz.x);
+  const float du = -sp.nu * k2, db = -sp.eta * k2;
+#pragma unroll
+  for (int c = 0; c < 6; ++c) {
+    const float dk = c < 3 ? du : db;
+    rk_apply<OP>(rs, c * fs + i, xv[c], make_float2(nl[c].x + dk * xd[c].x, nl[c].y + dk * xd[c].y));
+  }
+}
+
+// Hermitian part of the kx = 0 plane of the six fields: H(k) = (X(k) + conj X(-k)) / 2, with
+// X(-k) = 0 when -k is in the alias band.  The reference's diffusion term is computed from the
+// re-transformed physical field, rfft(irfft(X)), which is exactly this on the kx = 0 plane.
+__global__ void herm_kx0_kernel(const float2* __restrict__ Xpool, float2* __restrict__ Hpool, Geom geo, long long fs,
+                                long long stI, long long hI, BatchRef br) {
+  const int per = 6 * geo.k2 * geo.k2;
+  const int total = *br.count * per;
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < total; t += gridDim.x * blockDim.x) {
+    const int inst = t / per, i = t - inst * per;
+    const int slot = br.list[inst];
+    const float2* X = Xpool + slot * stI;
+    float2* H = Hpool + slot * hI;
+    const int jy = i % geo.k2;
+    const int r = i / geo.k2;
+    const int jz = r % geo.k2, c = r / geo.k2;
+    const long long base = (long long)c * fs;
+    const float2 xk = X[base + ((long long)jz * geo.k2 + jy) * geo.kxp];
+    const int py = kept_of_signed(geo, -signed_of_kept(geo, jy));
+    const int pz = kept_of_signed(geo, -signed_of_kept(geo, jz));
+    float2 xp = make_float2(0.f, 0.f);
+    if (py >= 0 && pz >= 0) xp = X[base + ((long long)pz * geo.k2 + py) * geo.kxp];
+    H[i] = make_float2(0.5f * (xk.x + xp.x), 0.5f * (xk.y - xp.y));
+  }
+}
+
+// On-device getCFL! (src/integrator.jl:158-198 of MHDFlows.jl) after a step of every active
+// slot: t += dt of the step just taken; next dt = min(coef * dx / max(|u|max, |B|max), tdiff)
+// from the maxima x_fused recorded on the step's last stage; the maxima are cleared for the next
+// step.  A slot with no finite positive maximum keeps its dt.
+// vmax holds maxima of the unnormalised fields the passes work with (n^3 times the physical
+// values); vscale = 1/n^3 converts them.
+__global__ void cfl_update_kernel(BatchRef br, SlotParams* sp, unsigned int* vmax, double* t, float coef_dx,
+                                  float vscale, int advance) {
+  const int n = *br.count;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const int s = br.list[i];
+    SlotParams p = sp[s];
+    if (advance) t[s] += (double)p.dt;
+    const float vm = vscale * fmaxf(__uint_as_float(vmax[2 * s]), __uint_as_float(vmax[2 * s + 1]));
+    if (vm > 0.f && isfinite(vm)) {
+      float dt = coef_dx / vm;
+      if (p.tdiff > 0.f) dt = fminf(dt, p.tdiff);
+      p.dt = dt;
+      sp[s] = p;
+    }
+    vmax[2 * s] = 0u;
+    vmax[2 * s + 1] = 0u;
+  }
+}
+
+// max |field| of one physical field into vmax[which] (initial fields before the first CFL step).
+__global__ void maxabs_into_kernel(const float* __restrict__ a, long long n, unsigned int* out) {
+  unsigned int m = 0;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    m = max(m, __float_as_uint(fabsf(a[i])));
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_down_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0) atomicMax(out, m);
+}
+
+// ------------------------------------------------------------------------------------------
+// Layout conversion between the reference's column-major sol[kx, ky, kz, f] (half spectrum,
+// nkr = n/2+1) and the compact retained-band state.
+// ------------------------------------------------------------------------------------------
+__global__ void gather_state_kernel(const float2* __restrict__ ref, float2* __restrict__ S, Geom geo, int nf) {
+  const long long total = (long long)nf * geo.k2 * geo.k2 * geo.kxp;
+  const int nkr = geo.n / 2 + 1;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total; i += (long long)gridDim.x * blockDim.x) {
+    const int x = (int)(i % geo.kxp);
+    long long r = i / geo.kxp;
+    const int jy = (int)(r % geo.k2); r /= geo.k2;
+    const int jz = (int)(r % geo.k2);
+    const int f = (int)(r / geo.k2);
+    float2 val = make_float2(0.f, 0.f);
+    if (x < geo.kx) {
+      const int fy = freq_of_kept(geo, jy), fz = freq_of_kept(geo, jz);
+      val = ref[(((long long)f * geo.n + fz) * geo.n + fy) * nkr + x];
+    }
+    S[i] = val;
+  }
+}
+
+__global__ void scatter_state_kernel(const float2* __restrict__ S, float2* __restrict__ ref, Geom geo, int nf) {
+  const int nkr = geo.n / 2 + 1;
+  const long long total = (long long)nf * geo.n * geo.n * nkr;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total; i += (long long)gridDim.x * blockDim.x) {
+    const int x = (int)(i % nkr);
+    long long r = i / nkr;
+    const int fy = (int)(r % geo.n); r /= geo.n;
+    const int fz = (int)(r % geo.n);
+    const int f = (int)(r / geo.n);
+    float2 val = make_float2(0.f, 0.f);
+    const int jy = kept_of_freq(geo, fy), jz = kept_of_freq(geo, fz);
+    if (x < geo.kx && jy >= 0 && jz >= 0) val = S[(((long long)f * geo.k2 + jz) * geo.k2 + jy) * geo.kxp + x];
+    ref[i] = val;
+  }
+}
+
+// ------------------------------------------------------------------------------------------
+// Diagnostics.
+// ------------------------------------------------------------------------------------------
+// Per-block partial sums over the compact state (double accumulation, fixed order):
+//   [0] sum w|u|^2  [1] sum w|b|^2  [2] sum w Re(u.conj b)  [3] max|k.u|  [4] max|k.b|  [5] non-finite count
+// w = 1 on the kx = 0 plane and 2 elsewhere (the half spectrum stands for both +-kx).
+constexpr int kDiagSlots = 6;
+constexpr int kDiagThreads = 256;
+
+__device__ __forceinline__ void block_reduce_diag(double (&acc)[kDiagSlots], double* out) {
+  __shared__ double red[kDiagThreads / 32][kDiagSlots];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+  for (int s = 0; s < kDiagSlots; ++s) {
+    double x = acc[s];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const double y = __shfl_down_sync(0xffffffffu, x, o);
+      x = (s == 3 || s == 4) ? fmax(x, y) : x + y;
+    }
+    if (lane == 0) red[wid][s] = x;
+  }
+  __syncthreads();
+  if (threadIdx.x < kDiagSlots) {
+    const int s = threadIdx.x;
+    double x = red[0][s];
+    for (int w = 1; w < kDiagThreads / 32; ++w) x = (s == 3 || s == 4) ? fmax(x, red[w][s]) : x + red[w][s];
+    out[s] = x;
+  }
+}
+
+__global__ void __launch_bounds__(kDiagThreads) diag_partial_kernel(const float2* __restrict__ S, Geom geo, double* partial) {
+  const long long plane = (long long)geo.k2 * geo.k2 * geo.kxp;  // one field
+  double acc[kDiagSlots] = {0, 0, 0, 0, 0, 0};
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < plane; i += (long long)gridDim.x * blockDim.x) {
+    const int x = (int)(i % geo.kxp);
+    if (x >= geo.kx) continue;
+    long long r = i / geo.kxp;
+    const int jy = (int)(r % geo.k2);
+    const int jz = (int)(r / geo.k2);
+    const double w = x == 0 ? 1.0 : 2.0;
+    const double kx = (double)geo.kscale * x;
+    const double ky = (double)geo.kscale * signed_of_kept(geo, jy);
+    const double kz = (double)geo.kscale * signed_of_kept(geo, jz);
+    double2 ku = make_double2(0, 0), kb = make_double2(0, 0);
+    double eu = 0, eb = 0, hc = 0;
+    bool bad = false;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      const float2 u = S[c * plane + i], b = S[(c + 3) * plane + i];
+      bad |= !isfinite(u.x) || !isfinite(u.y) || !isfinite(b.x) || !isfinite(b.y);
+      eu += (double)u.x * u.x + (double)u.y * u.y;
+      eb += (double)b.x * b.x + (double)b.y * b.y;
+      hc += (double)u.x * b.x + (double)u.y * b.y;
+      const double kc = c == 0 ? kx : (c == 1 ? ky : kz);
+      ku.x += kc * u.x; ku.y += kc * u.y;
+      kb.x += kc * b.x; kb.y += kc * b.y;
+    }
+    acc[0] += w * eu;
+    acc[1] += w * eb;
+    acc[2] += w * hc;
+    acc[3] = fmax(acc[3], sqrt(ku.x * ku.x + ku.y * ku.y));
+    acc[4] = fmax(acc[4], sqrt(kb.x * kb.x + kb.y * kb.y));
+    acc[5] += bad ? 1.0 : 0.0;
+  }
+  block_reduce_diag(acc, partial + (long long)blockIdx.x * kDiagSlots);
+}
+
+// Second pass: reduce the block partials in block order (deterministic).
+__global__ void __launch_bounds__(kDiagThreads) diag_final_kernel(const double* __restrict__ partial, int nblocks, double* out) {
+  double acc[kDiagSlots] = {0, 0, 0, 0, 0, 0};
+  for (int b = threadIdx.x; b < nblocks; b += blockDim.x) {
+#pragma unroll
+    for (int s = 0; s < kDiagSlots; ++s) {
+      const double x = partial[b * kDiagSlots + s];
+      acc[s] = (s == 3 || s == 4) ? fmax(acc[s], x) : acc[s] + x;
+    }
+  }
+  block_reduce_diag(acc, out);
+}
+
+// i k.B into a one-field compact buffer (input of the div B inverse transform).
+__global__ void divb_spectrum_kernel(const float2* __restrict__ S, float2* __restrict__ out, Geom geo) {
+  const long long plane = (long long)geo.k2 * geo.k2 * geo.kxp;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < plane; i += (long long)gridDim.x * blockDim.x) {
+    const int x = (int)(i % geo.kxp);
+    long long r = i / geo.kxp;
+    const int jy = (int)(r % geo.k2);
+    const int jz = (int)(r / geo.k2);
+    const float kx = geo.kscale * x, ky = geo.kscale * signed_of_kept(geo, jy), kz = geo.kscale * signed_of_kept(geo, jz);
+    const float2 bx = S[3 * plane + i], by = S[4 * plane + i], bz = S[5 * plane + i];
+    const float re = kx * bx.x + ky * by.x + kz * bz.x;
+    const float im = kx * bx.y + ky * by.y + kz * bz.y;
+    out[i] = x < geo.kx ? make_float2(-im, re) : make_float2(0.f, 0.f);
+  }
+}
+
+// max |x| over a float array via the ordered bit pattern of non-negative floats (NaN wins).
+__global__ void maxabs_kernel(const float* __restrict__ a, long long n, unsigned int* out) {
+  unsigned int m = 0;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const unsigned int b = __float_as_uint(fabsf(a[i]));
+    m = b > m ? b : m;
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const unsigned int y = __shfl_down_sync(0xffffffffu, m, o);
+    m = y > m ? y : m;
+  }
+  if ((threadIdx.x & 31) == 0) atomicMax(out, m);
+}
+
+}  // namespace mhdgb
