@@ -268,7 +268,8 @@ def run_gpu(args, rank, world, local, dist: Dist):
     lib = pkg._lib.load()
     n = args.n
     s0 = initial_state(n)
-    prob = pkg.Problem(pkg.GPU(local), nx=n, Lx=2 * math.pi, nu=NU, eta=ETA, dt=DT, stepper="RK4")
+    prob = pkg.Problem(pkg.GPU(local), nx=n, Lx=2 * math.pi, nu=NU, eta=ETA, dt=DT, stepper="RK4",
+                       precision=args.precision)
     h = prob.handle
     chk = pkg._lib.check
     prob.set_sol(s0.T)
@@ -361,7 +362,8 @@ def run_gpu(args, rank, world, local, dist: Dist):
     if args.secondary and rank == 0:
         n2 = 512
         s2 = initial_state(n2)
-        p2 = pkg.Problem(pkg.GPU(local), nx=n2, Lx=2 * math.pi, nu=5e-4, eta=5e-4, dt=2.5e-4, stepper="RK4")
+        p2 = pkg.Problem(pkg.GPU(local), nx=n2, Lx=2 * math.pi, nu=5e-4, eta=5e-4, dt=2.5e-4, stepper="RK4",
+                         precision=args.precision)
         p2.set_sol(s2.T)
         variants2 = pkg.autotune(p2)
         pkg.stepforward(p2, 3)
@@ -406,6 +408,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--n", type=int, default=256)
+    ap.add_argument("--precision", default="fp32", choices=["fp32", "split_fp16", "split_bf16"],
+                    help="x-row transforms in FP32 (plain form) or as split 16-bit tensor-core DFTs")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-secondary", dest="secondary", action="store_false")
     ap.add_argument("--workload", default="step", choices=["step", "ensemble", "serve"])
@@ -415,7 +419,8 @@ def main():
     args.warmup = max(args.warmup, 3)
     rank, world, local = dist_env()
     config = {"workload": f"MHD RK4 step, {args.n}^3 FP32, nu=eta=1e-3, dt=5e-4, seeded k^4 exp(-2(k/4)^2) u and B",
-              "n": args.n, "scheme": "RK4", "l2": "inputs larger than L2 (step working set > 1 GB)",
+              "n": args.n, "scheme": "RK4", "precision": args.precision,
+              "l2": "inputs larger than L2 (step working set > 1 GB)",
               "parallelism": "replicas" if args.gpus > 1 else "single"}
 
     if args.workload != "step" and args.impl != "reference":

@@ -49,7 +49,9 @@ extern "C" {
 #define MHD_RK4 0
 #define MHD_LSRK4 1
 
-#define MHD_PREC_FP32 0
+#define MHD_PREC_FP32 0        /* FP32 everywhere (the reference's T = Float32) */
+#define MHD_PREC_SPLIT_FP16 1  /* x-row transforms as tensor-core DFT products, FP16 hi+lo operands */
+#define MHD_PREC_SPLIT_BF16 2  /* the same with BF16 hi+lo operands (n = 128, 256, 512 only) */
 
 typedef struct mhd_params {
   int n;          /* grid points per axis (nx = ny = nz); supported: 16,32,48,64,96,128,256,512 */
@@ -60,7 +62,7 @@ typedef struct mhd_params {
   int neta;       /* hyper-resistivity order; values > 1 are rejected */
   double dt;      /* fixed time step */
   int scheme;     /* MHD_RK4 or MHD_LSRK4 */
-  int precision;  /* MHD_PREC_FP32 */
+  int precision;  /* MHD_PREC_FP32, MHD_PREC_SPLIT_FP16 or MHD_PREC_SPLIT_BF16 */
   int device;     /* CUDA device ordinal */
 } mhd_params;
 

@@ -30,7 +30,7 @@ __all__ = [
     "GPU", "CPU", "Problem", "SetUpProblemIC", "stepforward", "updatevars", "ProbDiagnostic",
     "Diagnostics", "TimeIntegrator", "MHDError", "kept_modes", "supported_sizes", "footprint_bytes",
     "Batch", "Ensemble", "slot_bytes", "Diagnostic", "autotune", "variants", "select_variant",
-    "TUNED_CLASSES",
+    "TUNED_CLASSES", "PRECISIONS",
 ]
 
 FIELDS = ("ux", "uy", "uz", "bx", "by", "bz")
@@ -63,8 +63,21 @@ def kept_modes(n: int):
     return a.value, b.value, c.value
 
 
-def _params(n, L, nu, eta, nnu, neta, dt, scheme, device):
-    return _lib.MhdParams(n, L, nu, eta, nnu, neta, dt, scheme, _lib.MHD_PREC_FP32, device)
+PRECISIONS = {"fp32": 0, "split_fp16": 1, "split_bf16": 2}
+
+
+def _precision(precision) -> int:
+    """Precision form: "fp32" (plain), "split_fp16" or "split_bf16" (tensor-core x-row DFTs)."""
+    if isinstance(precision, int) and precision in PRECISIONS.values():
+        return precision
+    key = str(precision).lower()
+    if key not in PRECISIONS:
+        raise MHDError(_lib.MHD_ERR_INVALID, f"unknown precision {precision!r} (fp32, split_fp16, split_bf16)")
+    return PRECISIONS[key]
+
+
+def _params(n, L, nu, eta, nnu, neta, dt, scheme, device, precision=0):
+    return _lib.MhdParams(n, L, nu, eta, nnu, neta, dt, scheme, _precision(precision), device)
 
 
 def footprint_bytes(n: int, L: float = 2 * math.pi, stepper: str = "RK4") -> int:
@@ -156,7 +169,7 @@ class Problem:
     def __init__(self, dev=None, *, nx=64, ny=None, nz=None, Lx=2 * math.pi, Ly=None, Lz=None,
                  dt=0.0, nu=None, eta=None, nnu=0, neta=0, B_field=True, EMHD=False,
                  Compressibility=False, Shear=False, VP_method=False, Dye_Module=False,
-                 stepper="RK4", calcF=None, T=np.float32, aliased_fraction=1 / 3, **kw):
+                 stepper="RK4", calcF=None, T=np.float32, aliased_fraction=1 / 3, precision="fp32", **kw):
         nu = kw.pop("ν", nu)
         eta = kw.pop("η", eta)
         nnu = kw.pop("nν", nnu)
@@ -184,8 +197,9 @@ class Problem:
         self.n = int(nx)
         self.L = float(Lx)
         self.stepper = str(stepper).upper()
+        self.precision = _precision(precision)
         p = _params(self.n, self.L, float(nu or 0.0), float(eta or 0.0), int(nnu), int(neta), float(dt),
-                    scheme, dev.device)
+                    scheme, dev.device, self.precision)
         h = C.c_void_p()
         _lib.check(self._lib.mhd_create(C.byref(p), C.byref(h)))
         self._h = h
@@ -411,14 +425,15 @@ class Batch:
     (6, n, n, nkr) complex64 for states and (n, n, n) float32 for physical fields.
     """
 
-    def __init__(self, n: int, capacity: int, stepper: str = "RK4", L: float = 2 * math.pi, device: int = 0):
+    def __init__(self, n: int, capacity: int, stepper: str = "RK4", L: float = 2 * math.pi, device: int = 0,
+                 precision="fp32"):
         scheme = {"RK4": MHD_RK4, "LSRK4": MHD_LSRK4}.get(str(stepper).upper())
         if scheme is None:
             raise MHDError(_lib.MHD_ERR_INVALID, f"unknown stepper {stepper!r}")
         self._lib = _lib.load()
         self.n, self.L, self.stepper = int(n), float(L), str(stepper).upper()
         self.nkr = self.n // 2 + 1
-        p = _params(self.n, self.L, 0.0, 0.0, 0, 0, 0.0, scheme, device)
+        p = _params(self.n, self.L, 0.0, 0.0, 0, 0, 0.0, scheme, device, precision)
         h = C.c_void_p()
         _lib.check(self._lib.mhd_batch_create(C.byref(p), int(capacity), C.byref(h)))
         self._h = h

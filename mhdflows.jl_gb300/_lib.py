@@ -22,6 +22,8 @@ MHD_ERR_STATE = 5
 MHD_RK4 = 0
 MHD_LSRK4 = 1
 MHD_PREC_FP32 = 0
+MHD_PREC_SPLIT_FP16 = 1
+MHD_PREC_SPLIT_BF16 = 2
 MHD_TUNE_FORCE = 1
 MHD_TUNE_NO_FILE = 2
 

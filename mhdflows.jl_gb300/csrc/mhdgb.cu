@@ -162,12 +162,12 @@ std::string tune_file() {
   return "";
 }
 
-std::string tune_key(int device, int n) {
+std::string tune_key(int device, int n, int prec) {
   cudaDeviceProp prop;
   if (cudaGetDeviceProperties(&prop, device) != cudaSuccess) return "";
   std::string name(prop.name);
   for (auto& c : name) if (c == '|' || c == '\n') c = ' ';
-  return name + "|" + std::to_string(prop.multiProcessorCount) + "|" + std::to_string(n);
+  return name + "|" + std::to_string(prop.multiProcessorCount) + "|" + std::to_string(n) + (prec ? "p" + std::to_string(prec) : "");
 }
 
 std::vector<std::string> split_bar(const std::string& line) {
@@ -521,7 +521,7 @@ struct mhd_problem {
     if (profiling) return fail(MHD_ERR_STATE, "autotune does not run with per-kernel profiling enabled");
     int rc;
     if ((rc = sync_lists())) return rc;
-    const std::string key = tune_key(device, g.n);
+    const std::string key = tune_key(device, g.n, p.precision);
     std::vector<std::string> names;
     if (!force && !key.empty() && tuned_lookup(key, &names) && apply_names(names) == MHD_OK) return MHD_OK;
     if (active.empty()) return fail(MHD_ERR_STATE, "autotune needs at least one active slot");
@@ -623,7 +623,10 @@ int validate(const mhd_params* p) {
   if (p->nnu > 1 || p->neta > 1) return fail(MHD_ERR_INVALID, "hyper-diffusion (nnu > 1 or neta > 1) is not on this path");
   if (!std::isfinite(p->dt)) return fail(MHD_ERR_INVALID, "dt must be finite");
   if (p->scheme != MHD_RK4 && p->scheme != MHD_LSRK4) return fail(MHD_ERR_INVALID, "scheme must be MHD_RK4 or MHD_LSRK4");
-  if (p->precision != MHD_PREC_FP32) return fail(MHD_ERR_INVALID, "only MHD_PREC_FP32 is available");
+  if (p->precision != MHD_PREC_FP32 && p->precision != MHD_PREC_SPLIT_FP16 && p->precision != MHD_PREC_SPLIT_BF16)
+    return fail(MHD_ERR_INVALID, "precision must be MHD_PREC_FP32, MHD_PREC_SPLIT_FP16 or MHD_PREC_SPLIT_BF16");
+  if (p->precision != MHD_PREC_FP32 && p->n != 128 && p->n != 256 && p->n != 512)
+    return fail(MHD_ERR_INVALID, "the split-precision tensor-core forms exist for n = 128, 256, 512");
   return MHD_OK;
 }
 
@@ -648,11 +651,12 @@ int create_class(const mhd_params* params, int cap, mhd_handle* out) {
   h->sz = sizes_of(h->g);
   h->ops.reset(make_ops(params->n));
   if (!h->ops) return fail(MHD_ERR_INVALID, "no plan for n");
+  h->ops->prec = params->precision;
   if ((rc = h->ops->setup(h->g))) return rc;
   {
     // a selection the autotuner made earlier for this device and grid size (this process or the
     // tuning file); the defaults otherwise
-    const std::string key = tune_key(h->device, h->g.n);
+    const std::string key = tune_key(h->device, h->g.n, params->precision);
     std::vector<std::string> names;
     if (!key.empty() && tuned_lookup(key, &names)) h->apply_names(names);
   }

@@ -14,6 +14,7 @@
 #include <vector>
 
 #include "passes.cuh"
+#include "tc_rows.cuh"
 
 namespace mhdgb {
 
@@ -38,6 +39,12 @@ struct XVariant {
   size_t tw = 0, twr = 0;             // offsets of the plan's twiddles and of its reverse's
   size_t smem = 0;
   int ctas = 0;                       // resident CTAs on the device (0: does not fit)
+  // precision form: 0 FP32, 1 split FP16 tensor cores, 2 split BF16 tensor cores; the split
+  // forms read a per-device constant table (DFT fragments, twiddles) built by build_table
+  int prec = 0;
+  size_t table_words = 0;
+  int (*build_table)(uint32_t* table) = nullptr;
+  uint32_t* table = nullptr;
 };
 
 struct ColVariant {
@@ -62,6 +69,7 @@ class OpsBase {
   void x_r2c(const float* src, float2* dst, const Geom& g, long long drow, cudaStream_t s) const;
 
   int n = 0;
+  int prec = 0;  // precision form of the x rows (mhd_params.precision)
   std::vector<XVariant> xv;
   std::vector<ColVariant> cv;
   int sel[kTunedClasses] = {0, 0, 0, 0, 0};  // selected variant of each tuned class
@@ -142,6 +150,23 @@ class Ops : public OpsBase {
     v.group_words = &XC::group_words;
     v.tw = twiddles<R>();
     v.twr = twiddles<typename Reverse<R>::type>();
+    xv.push_back(v);
+  }
+
+  // x rows on the tensor cores (split FP16 or BF16 operands), GROUPS warps (rows) per CTA
+  template <int KIND, int GROUPS, int MINB>
+  void add_x_tc() {
+    XVariant v;
+    v.name = std::string("xtc:") + (KIND == SPLIT_F16 ? "f16" : "bf16") + "/16x" + std::to_string(N / 16) + "/c" +
+             std::to_string(GROUPS) + "/b" + std::to_string(MINB);
+    v.fn = x_fused_tc_kernel<N, KIND, GROUPS, MINB>;
+    v.threads = GROUPS * 32;
+    v.rpg = 1;
+    v.groups = GROUPS;
+    v.group_words = &tc_group_words<N>;
+    v.prec = KIND == SPLIT_F16 ? 1 : 2;
+    v.table_words = TcLayout<N>::WORDS;
+    v.build_table = &tc_build_table<N, KIND>;
     xv.push_back(v);
   }
 

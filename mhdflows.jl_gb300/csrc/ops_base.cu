@@ -8,6 +8,8 @@ namespace mhdgb {
 
 OpsBase::~OpsBase() {
   if (tw_dev) cudaFree(tw_dev);
+  for (auto& x : xv)
+    if (x.table) cudaFree(x.table);
 }
 
 namespace {
@@ -48,7 +50,12 @@ int OpsBase::setup(const Geom& g) {
   for (auto& x : xv) {
     x.smem = sizeof(float2) * (size_t)x.groups * x.group_words(g.kxp);
     x.ctas = 0;
-    if ((int)x.smem > smem_max) continue;
+    if (x.prec != prec || (int)x.smem > smem_max) continue;  // only this problem's precision form
+    if (x.build_table) {
+      e = cudaMalloc(&x.table, x.table_words * sizeof(uint32_t));
+      if (e != cudaSuccess) return report_error(MHD_ERR_OOM, std::string("tensor-core tables: ") + cudaGetErrorString(e));
+      if (x.build_table(x.table)) return report_error(MHD_ERR_CUDA, "building the tensor-core DFT tables failed");
+    }
     if ((rc = set_smem((const void*)x.fn, x.smem))) return rc;
     if ((rc = resident_ctas((const void*)x.fn, x.threads, x.smem, sms, &x.ctas))) return rc;
   }
@@ -66,7 +73,10 @@ int OpsBase::setup(const Geom& g) {
   for (int cls = 0; cls < kTunedClasses; ++cls) {
     int i = 0;
     while (i < variant_count(cls) && !variant_ok(cls, i)) ++i;
-    if (i == variant_count(cls)) return report_error(MHD_ERR_CUDA, "no pass-kernel variant fits on this device");
+    if (i == variant_count(cls))
+      return report_error(cls == KC_XFUSED && prec ? MHD_ERR_INVALID : MHD_ERR_CUDA,
+                          cls == KC_XFUSED && prec ? "no x-row kernel of this precision form for this grid size"
+                                                   : "no pass-kernel variant fits on this device");
     sel[cls] = i;
   }
   return MHD_OK;
@@ -79,7 +89,7 @@ int OpsBase::variant_count(int cls) const {
 
 bool OpsBase::variant_ok(int cls, int i) const {
   if (i < 0 || i >= variant_count(cls)) return false;
-  if (cls == KC_XFUSED) return xv[i].ctas > 0;
+  if (cls == KC_XFUSED) return xv[i].ctas > 0 && xv[i].prec == prec;
   return is_inv(cls) ? cv[i].ctas_inv > 0 : cv[i].ctas_fwd > 0;
 }
 
@@ -120,7 +130,9 @@ void OpsBase::x_fused(float2* pool, const Geom& g, long long rowstride, long lon
   const long long groups = (long long)cap * n * n / x.rpg;
   const long long need = (groups + x.groups - 1) / x.groups;
   const int grid = (int)(need < x.ctas ? need : x.ctas);
-  x.fn<<<grid, x.threads, x.smem, s>>>(pool, g, rowstride, slot, istride, br, tw_dev + x.tw, tw_dev + x.twr, vmax);
+  const float2* t1 = x.table ? reinterpret_cast<const float2*>(x.table) : tw_dev + x.tw;
+  const float2* t2 = x.table ? nullptr : tw_dev + x.twr;
+  x.fn<<<grid, x.threads, x.smem, s>>>(pool, g, rowstride, slot, istride, br, t1, t2, vmax);
 }
 
 void OpsBase::x_c2r(const float2* src, float* dst, const Geom& g, long long srow, float scale, cudaStream_t s) const {
