@@ -85,16 +85,17 @@ __device__ __forceinline__ void mma16816(float (&d)[4], const uint32_t (&a)[4], 
         : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
   }
 }
-// d += A B with both factors split: lo*hi and hi*lo first, then hi*hi
-template <int KIND>
-__device__ __forceinline__ void mma3(float (&d)[4], const uint32_t (&ah)[4], const uint32_t (&al)[4], uint32_t bh0,
-                                     uint32_t bh1, uint32_t bl0, uint32_t bl1) {
-  float t[4] = {0.f, 0.f, 0.f, 0.f};
-  mma16816<KIND>(t, al, bh0, bh1);
-  mma16816<KIND>(t, ah, bl0, bl1);
-  mma16816<KIND>(t, ah, bh0, bh1);
+// d += A B with both factors split, for NB independent B operands (one A): the three terms
+// lo*hi, hi*lo, hi*hi go term by term across the NB tiles, so consecutive MMAs are independent
+template <int KIND, int NB>
+__device__ __forceinline__ void mma3n(float (&d)[NB][4], const uint32_t (&ah)[4], const uint32_t (&al)[4],
+                                      const uint32_t (&bh)[NB][2], const uint32_t (&bl)[NB][2]) {
 #pragma unroll
-  for (int i = 0; i < 4; ++i) d[i] += t[i];
+  for (int j = 0; j < NB; ++j) mma16816<KIND>(d[j], al, bh[j][0], bh[j][1]);
+#pragma unroll
+  for (int j = 0; j < NB; ++j) mma16816<KIND>(d[j], ah, bl[j][0], bl[j][1]);
+#pragma unroll
+  for (int j = 0; j < NB; ++j) mma16816<KIND>(d[j], ah, bh[j][0], bh[j][1]);
 }
 
 // ------------------------------------------------------------------------------------------
@@ -302,8 +303,7 @@ __device__ __forceinline__ void tc_inverse(const float (&zr)[N / 128][4], const 
     for (int mt = 0; mt < 2; ++mt) {
       uint32_t ah[4], al[4];
       ldfrag4(tab + L::INVA + (mt * 2 + kb) * 2 * 32 * 4 + lane * 4, ah, al);
-#pragma unroll
-      for (int nt = 0; nt < NT; ++nt) mma3<KIND>(c[mt][nt], ah, al, bh[nt][0], bh[nt][1], bl[nt][0], bl[nt][1]);
+      mma3n<KIND, NT>(c[mt], ah, al, bh, bl);
     }
   }
   // twiddle W_N^{n2 k1}
@@ -338,12 +338,14 @@ __device__ __forceinline__ void tc_inverse(const float (&zr)[N / 128][4], const 
     split_pair<KIND>(t0[2], t0[3], ah[1], al[1]);
     split_pair<KIND>(t1[0], t1[1], ah[2], al[2]);
     split_pair<KIND>(t1[2], t1[3], ah[3], al[3]);
+    uint32_t bh[L::NTQ][2], bl[L::NTQ][2];
 #pragma unroll
     for (int nt2 = 0; nt2 < L::NTQ; ++nt2) {
       const uint2* f = reinterpret_cast<const uint2*>(tab + L::INVB + (kb * L::NTQ + nt2) * 2 * 32 * 2);
-      const uint2 bh = __ldg(f + lane), bl = __ldg(f + 32 + lane);
-      mma3<KIND>(d[nt2], ah, al, bh.x, bh.y, bl.x, bl.y);
+      const uint2 h = __ldg(f + lane), l = __ldg(f + 32 + lane);
+      bh[nt2][0] = h.x; bh[nt2][1] = h.y; bl[nt2][0] = l.x; bl[nt2][1] = l.y;
     }
+    mma3n<KIND, L::NTQ>(d, ah, al, bh, bl);
   }
 #pragma unroll
   for (int nt2 = 0; nt2 < L::NTQ; ++nt2) {
@@ -391,8 +393,7 @@ __device__ __forceinline__ void tc_forward(Prod prod, float s, float2* buf, cons
     for (int mt = 0; mt < L::MQ; ++mt) {
       uint32_t ah[4], al[4];
       ldfrag4(tab + L::FWDA + (mt * L::KBQ + kb) * 2 * 32 * 4 + lane * 4, ah, al);
-#pragma unroll
-      for (int nb = 0; nb < 2; ++nb) mma3<KIND>(c[mt][nb], ah, al, bh[nb][0], bh[nb][1], bl[nb][0], bl[nb][1]);
+      mma3n<KIND, 2>(c[mt], ah, al, bh, bl);
     }
   }
   // twiddle W_N^{-b k1}: real part of row k1 at tile (k1 / 16, element 0/1 or 2/3), imaginary
@@ -455,13 +456,16 @@ __device__ __forceinline__ void tc_forward(Prod prod, float s, float2* buf, cons
     for (int nh = 0; nh < 2; ++nh) {  // output columns k2 = 8 nh + ..: real tile nh, imaginary tile nh + 2
       float d[2][4] = {{0.f, 0.f, 0.f, 0.f}, {0.f, 0.f, 0.f, 0.f}};
 #pragma unroll
-      for (int ri = 0; ri < 2; ++ri)
+      for (int kb = 0; kb < 2; ++kb) {
+        uint32_t bh[2][2], bl[2][2];
 #pragma unroll
-        for (int kb = 0; kb < 2; ++kb) {
+        for (int ri = 0; ri < 2; ++ri) {
           const uint2* f = reinterpret_cast<const uint2*>(tab + L::FWDB + (kb * 4 + nh + 2 * ri) * 2 * 32 * 2);
-          const uint2 bh = __ldg(f + lane), bl = __ldg(f + 32 + lane);
-          mma3<KIND>(d[ri], ah[kb], al[kb], bh.x, bh.y, bl.x, bl.y);
+          const uint2 h = __ldg(f + lane), l = __ldg(f + 32 + lane);
+          bh[ri][0] = h.x; bh[ri][1] = h.y; bl[ri][0] = l.x; bl[ri][1] = l.y;
         }
+        mma3n<KIND, 2>(d, ah[kb], al[kb], bh, bl);
+      }
       // element (row k1, col k2): rows 16 mt + g (+8), cols 8 nh + 2 tq + {0,1}
 #pragma unroll
       for (int i = 0; i < 4; ++i) {
