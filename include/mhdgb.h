@@ -64,6 +64,9 @@ typedef struct mhd_params {
   int scheme;     /* MHD_RK4 or MHD_LSRK4 */
   int precision;  /* MHD_PREC_FP32, MHD_PREC_SPLIT_FP16 or MHD_PREC_SPLIT_BF16 */
   int device;     /* CUDA device ordinal */
+  int hydro_only; /* 0: MHD (B_field = true, 6 fields); 1: hydrodynamics (B_field = false,
+                     HDcalcN! of src/pgen.jl:176-182: 3 fields ux, uy, uz; the state layout of
+                     set/get_state is then (nkr, n, n, 3) and field indices are 0..2) */
 } mhd_params;
 
 typedef struct mhd_problem* mhd_handle;
@@ -176,6 +179,21 @@ int mhd_time_steps(mhd_handle h, int nsteps, double* ms);
 /* Timing helper: nsteps steps back to back with an event between consecutive steps; fills
  * ms_per_step[0..nsteps) with each step's device milliseconds (synchronises at the end). */
 int mhd_step_timed(mhd_handle h, int nsteps, double* ms_per_step);
+
+/* A99 random solenoidal forcing of the velocity, the calcF! hook of MHDcalcN!'s addforcing!
+ * (src/pgen.jl:159,231-234) with GetA99vars_And_function / SetUpFk! / A99ForceDriving!
+ * (src/pgen/A99ForceDriving_GPU.jl:18-130).  P > 0 turns it on (P = 0 off); kf, sigma, b are
+ * SetUpFk!'s arguments.  As in the reference, A is computed from the spectrum peaked at kf, the
+ * forcing kernel then uses kf = b (SetUpFk! stores b there), every right-hand-side evaluation
+ * draws new random numbers, and the whole velocity right-hand side keeps only its real part on
+ * the kx = 0 plane.  The device rand() of the reference is replaced by a counter-based
+ * generator of (seed, 8 * step + stage, mode index, draw), so runs are reproducible; the step
+ * counter is the slot's clock step (mhd_set_clock sets it).  mhd_get_forcing returns A and the
+ * kf the kernel uses. */
+int mhd_set_forcing(mhd_handle h, double P, double kf, double sigma, double b, unsigned long long seed);
+int mhd_slot_set_forcing(mhd_handle h, int slot, double P, double kf, double sigma, double b,
+                         unsigned long long seed);
+int mhd_get_forcing(mhd_handle h, int slot, double* A, double* kf_used);
 
 /* Autotuner (no counterpart in the reference, whose FFTs are FFTW / cuFFT plans made with
  * MEASURE).  Each FFT pass class (z_inverse, y_inverse, x_fused, y_forward, z_forward: classes

@@ -30,7 +30,8 @@ __all__ = [
     "GPU", "CPU", "Problem", "SetUpProblemIC", "stepforward", "updatevars", "ProbDiagnostic",
     "Diagnostics", "TimeIntegrator", "MHDError", "kept_modes", "supported_sizes", "footprint_bytes",
     "Batch", "Ensemble", "slot_bytes", "Diagnostic", "autotune", "variants", "select_variant",
-    "TUNED_CLASSES", "PRECISIONS",
+    "TUNED_CLASSES", "PRECISIONS", "savefile", "Restart", "readMHDFlows", "checkpoint_path", "FIELDS",
+    "SetUpFk", "forcing_amplitude",
 ]
 
 FIELDS = ("ux", "uy", "uz", "bx", "by", "bz")
@@ -76,8 +77,8 @@ def _precision(precision) -> int:
     return PRECISIONS[key]
 
 
-def _params(n, L, nu, eta, nnu, neta, dt, scheme, device, precision=0):
-    return _lib.MhdParams(n, L, nu, eta, nnu, neta, dt, scheme, _precision(precision), device)
+def _params(n, L, nu, eta, nnu, neta, dt, scheme, device, precision=0, hydro_only=False):
+    return _lib.MhdParams(n, L, nu, eta, nnu, neta, dt, scheme, _precision(precision), device, int(bool(hydro_only)))
 
 
 def footprint_bytes(n: int, L: float = 2 * math.pi, stepper: str = "RK4") -> int:
@@ -131,8 +132,8 @@ class Clock:
 class Vars:
     """Physical fields ux..bz (MVars, src/Structure/MHDVars.jl:1-24), filled by updatevars."""
 
-    def __init__(self, n):
-        for f in FIELDS:
+    def __init__(self, n, nfields=6):
+        for f in FIELDS[:nfields]:
             setattr(self, f, np.zeros((n, n, n), dtype=np.float32, order="F"))
 
 
@@ -180,8 +181,6 @@ class Problem:
             dev = GPU()
         if isinstance(dev, CPU) or dev is CPU:
             raise MHDError(_lib.MHD_ERR_INVALID, "this library runs on the GPU only: use Problem(GPU(); ...)")
-        if not B_field:
-            raise MHDError(_lib.MHD_ERR_INVALID, "only the MHD path (B_field=true) is provided")
         if EMHD or Compressibility or Shear or VP_method or Dye_Module or calcF is not None:
             raise MHDError(_lib.MHD_ERR_INVALID, "EMHD, compressibility, shear, VP, dye and forcing are not on this path")
         if (ny not in (None, nx)) or (nz not in (None, nx)) or (Ly not in (None, Lx)) or (Lz not in (None, Lx)):
@@ -198,14 +197,18 @@ class Problem:
         self.L = float(Lx)
         self.stepper = str(stepper).upper()
         self.precision = _precision(precision)
+        self.B_field = bool(B_field)
+        self.nfields = 6 if self.B_field else 3
+        if not self.B_field:  # HDcalcN! (src/pgen.jl:176-182): the three velocity fields only
+            eta, neta = 0.0, 0
         p = _params(self.n, self.L, float(nu or 0.0), float(eta or 0.0), int(nnu), int(neta), float(dt),
-                    scheme, dev.device, self.precision)
+                    scheme, dev.device, self.precision, hydro_only=not self.B_field)
         h = C.c_void_p()
         _lib.check(self._lib.mhd_create(C.byref(p), C.byref(h)))
         self._h = h
         self.grid = Grid(self.n, self.L)
         self.params = Params(float(nu or 0.0), float(eta or 0.0), int(nnu), int(neta))
-        self.vars = Vars(self.n)
+        self.vars = Vars(self.n, self.nfields)
         self.clock = Clock(self)
         self.device = dev
 
@@ -234,8 +237,9 @@ class Problem:
     # -- state
     @property
     def sol(self):
-        """Copy of prob.sol, complex64 (nkr, n, n, 6) Fortran order; alias band is zero."""
-        out = np.empty((6, self.n, self.n, self.grid.nkr), dtype=np.complex64)
+        """Copy of prob.sol, complex64 (nkr, n, n, 6) Fortran order ((nkr, n, n, 3) for a hydrodynamic
+        problem); alias band is zero."""
+        out = np.empty((self.nfields, self.n, self.n, self.grid.nkr), dtype=np.complex64)
         _lib.check(self._lib.mhd_get_state(self._h, out.ctypes.data))
         return out.T
 
@@ -245,22 +249,23 @@ class Problem:
 
     def set_sol(self, value):
         a = np.asarray(value)
-        if a.shape == (self.grid.nkr, self.n, self.n, 6):
+        nf = self.nfields
+        if a.shape == (self.grid.nkr, self.n, self.n, nf):
             a = a.T
-        if a.shape != (6, self.n, self.n, self.grid.nkr):
-            raise MHDError(_lib.MHD_ERR_INVALID, f"sol must have shape (nkr, n, n, 6) = {(self.grid.nkr, self.n, self.n, 6)}")
+        if a.shape != (nf, self.n, self.n, self.grid.nkr):
+            raise MHDError(_lib.MHD_ERR_INVALID, f"sol must have shape (nkr, n, n, {nf}) = {(self.grid.nkr, self.n, self.n, nf)}")
         a = np.ascontiguousarray(a, dtype=np.complex64)
         _lib.check(self._lib.mhd_set_state(self._h, a.ctypes.data))
 
     def sol_c(self):
-        """prob.sol as a C-ordered (6, nz, ny, nkr) array (same memory order as the Julia array)."""
-        out = np.empty((6, self.n, self.n, self.grid.nkr), dtype=np.complex64)
+        """prob.sol as a C-ordered (nfields, nz, ny, nkr) array (same memory order as the Julia array)."""
+        out = np.empty((self.nfields, self.n, self.n, self.grid.nkr), dtype=np.complex64)
         _lib.check(self._lib.mhd_get_state(self._h, out.ctypes.data))
         return out
 
     def rhs_c(self):
-        """calcN!(N, sol, ...) of the current state, C-ordered (6, nz, ny, nkr)."""
-        out = np.empty((6, self.n, self.n, self.grid.nkr), dtype=np.complex64)
+        """calcN!(N, sol, ...) of the current state, C-ordered (nfields, nz, ny, nkr)."""
+        out = np.empty((self.nfields, self.n, self.n, self.grid.nkr), dtype=np.complex64)
         _lib.check(self._lib.mhd_compute_rhs(self._h, out.ctypes.data))
         return out
 
@@ -324,6 +329,8 @@ def SetUpProblemIC(prob: Problem, *, ux=None, uy=None, uz=None, bx=None, by=None
     for f, arr in enumerate((ux, uy, uz, bx, by, bz)):
         if arr is None:
             continue
+        if f >= prob.nfields:
+            raise MHDError(_lib.MHD_ERR_INVALID, "a hydrodynamic problem (B_field=false) has no magnetic field")
         c = _to_c_phys(arr, prob.n)
         prob.set_physical_c(f, c)
         getattr(prob.vars, FIELDS[f])[...] = c.T
@@ -338,7 +345,7 @@ def stepforward(prob: Problem, nsteps: int = 1):
 
 def updatevars(prob: Problem):
     """updatevars!(prob): vars.ux..bz <- normalised c2r of the current sol."""
-    for f, name in enumerate(FIELDS):
+    for f, name in enumerate(FIELDS[: prob.nfields]):
         getattr(prob.vars, name)[...] = prob.physical_c(f).T
     return None
 
@@ -584,4 +591,69 @@ def select_variant(obj, cls, idx: int):
     lib = _lib.load()
     ci = TUNED_CLASSES.index(cls) if isinstance(cls, str) else int(cls)
     _lib.check(lib.mhd_select_variant(obj.handle, ci, int(idx)))
+
+
+# ---- checkpoint / restart (src/integrator.jl:208-288, src/utils/IC.jl:245-257) ----------------
+# The reference writes HDF5 files through HDF5.jl.  No HDF5 library exists on this system, so the
+# same datasets -- i_velocity, j_velocity, k_velocity, i_mag_field, j_mag_field, k_mag_field
+# (Float32, (nx, ny, nz) in the reference's index order) and time -- go into a NumPy .npz archive
+# with the reference's file pattern <name>_t_<4-digit number>.npz.
+_DATASETS = ("i_velocity", "j_velocity", "k_velocity", "i_mag_field", "j_mag_field", "k_mag_field")
+
+
+def checkpoint_path(file_path_and_name: str, file_number: int) -> str:
+    """<name>_t_0001.npz: the number zero-padded to four digits like savefile."""
+    return f"{file_path_and_name}_t_{int(file_number):04d}.npz"
+
+
+def savefile(prob: Problem, file_number: int, file_path_and_name: str = "") -> str:
+    """savefile(prob, file_number; file_path_and_name) (src/integrator.jl:260-288): the physical
+    fields of the current state and the time.  Returns the path written."""
+    updatevars(prob)
+    data = {name: np.asarray(getattr(prob.vars, FIELDS[f])) for f, name in enumerate(_DATASETS[: prob.nfields])}
+    data["time"] = np.float64(prob.clock.t)
+    path = checkpoint_path(file_path_and_name, file_number)
+    with open(path, "wb") as fh:
+        np.savez(fh, **data)
+    return path
+
+
+def readMHDFlows(path: str):
+    """readMHDFlows(FileName) (src/utils/IC.jl:245-257): (iv, jv, kv, ib, jb, kb, t), Float32
+    fields in the reference's (nx, ny, nz) index order."""
+    with np.load(path) as f:
+        fields = [np.asarray(f[name], dtype=np.float32) for name in _DATASETS]
+        t = float(f["time"])
+    return (*fields, t)
+
+
+def Restart(prob: Problem, path: str):
+    """Restart!(prob, file_path_and_name) (src/integrator.jl:208-258): fields -> r2c into sol,
+    clock.t <- time."""
+    with np.load(path) as f:
+        kw = {FIELDS[i]: np.asarray(f[name]) for i, name in enumerate(_DATASETS[: prob.nfields])}
+        t = float(f["time"])
+    SetUpProblemIC(prob, **kw)
+    prob.clock.t = t
+    return None
+
+
+# ---- A99 random forcing (src/pgen/A99ForceDriving_GPU.jl) ----------------------------------
+def SetUpFk(prob, kf: float = 2.0, P: float = 1.0, sigma: float = 1.0, b: float = 1.0, seed: int = 0, slot: int = 0):
+    """SetUpFk!(prob; kf, P, σ, b) (src/pgen/A99ForceDriving_GPU.jl:24-48) plus the A99ForceDriving!
+    hook: the velocity right-hand side of every stage gets the A99 random forcing.  P = 0 turns
+    it off.  ``prob`` is a Problem (slot 0) or a Batch (``slot``).  Random numbers come from a
+    counter-based generator keyed by ``seed`` (the reference draws them with the device rand())."""
+    lib = _lib.load()
+    _lib.check(lib.mhd_slot_set_forcing(prob.handle, int(slot), float(P), float(kf), float(sigma), float(b),
+                                        int(seed) & 0xFFFFFFFFFFFFFFFF))
+    return None
+
+
+def forcing_amplitude(prob, slot: int = 0):
+    """(A, kf the forcing kernel uses) of a slot (A = 0: no forcing)."""
+    lib = _lib.load()
+    a, k = C.c_double(), C.c_double()
+    _lib.check(lib.mhd_get_forcing(prob.handle, int(slot), C.byref(a), C.byref(k)))
+    return a.value, k.value
 

@@ -48,6 +48,7 @@ class MhdParams(C.Structure):
         ("scheme", C.c_int),
         ("precision", C.c_int),
         ("device", C.c_int),
+        ("hydro_only", C.c_int),
     ]
 
 
@@ -96,6 +97,10 @@ _SIGS = {
     "mhd_ensemble_destroy": (C.c_int, [C.c_void_p]),
     "mhd_set_cfl": (C.c_int, [C.c_void_p, C.c_int, C.c_double]),
     "mhd_diagnostics_noalloc": (C.c_int, [C.c_void_p, C.c_int, C.c_double, C.c_void_p, C.c_void_p]),
+    "mhd_set_forcing": (C.c_int, [C.c_void_p, C.c_double, C.c_double, C.c_double, C.c_double, C.c_ulonglong]),
+    "mhd_slot_set_forcing": (C.c_int, [C.c_void_p, C.c_int, C.c_double, C.c_double, C.c_double, C.c_double,
+                                       C.c_ulonglong]),
+    "mhd_get_forcing": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     "mhd_autotune": (C.c_int, [C.c_void_p, C.c_int]),
     "mhd_variant_count": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_int)]),
     "mhd_variant_name": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_char_p, C.c_int]),

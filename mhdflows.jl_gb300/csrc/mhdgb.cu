@@ -259,6 +259,10 @@ struct mhd_problem {
   // on-device CFL: per-slot maxima of |u|, |B| (float bits) and device clock
   unsigned int* dvmax = nullptr;
   double* dtime = nullptr;
+  // per-slot step counters on the device (the random forcing's call counter) and whether any
+  // slot is forced (the step then ends with step_tick_kernel)
+  long long* dstep = nullptr;
+  bool forcing = false;
   bool cfl = false;
   double cfl_coef = 0.3;
   int graph_version = 0;   // active slots, then the identity list (cap each), then counts
@@ -288,11 +292,12 @@ struct mhd_problem {
     recs.clear();
     for (auto e : pool) cudaEventDestroy(e);
     pool.clear();
-    void* ptrs[] = {sol, xs, acc, aux, colbuf, rowbuf, ref, phys, diag_partial, diag_out, maxabs, dparams, dlist, dvmax, dtime};
+    void* ptrs[] = {sol, xs, acc, aux, colbuf, rowbuf, ref, phys, diag_partial, diag_out, maxabs, dparams, dlist, dvmax, dtime,
+                    dstep};
     for (void* q : ptrs) if (q) cudaFree(q);
     sol = xs = acc = aux = colbuf = rowbuf = ref = nullptr;
     phys = nullptr; diag_partial = nullptr; diag_out = nullptr; maxabs = nullptr; dparams = nullptr; dlist = nullptr;
-    dvmax = nullptr; dtime = nullptr;
+    dvmax = nullptr; dtime = nullptr; dstep = nullptr;
     if (own_stream) cudaStreamDestroy(own_stream);
     own_stream = nullptr;
   }
@@ -378,7 +383,7 @@ struct mhd_problem {
     return launch(KC_ZFWD, [&] { ops->col(KC_ZFWD, a, g, g.k2, nf, br, cap, stream); });
   }
   // Stage epilogue: RHS from the 8 compact product planes (in rowbuf) and the stage state X.
-  int epilogue(const float2* X, int op, float hf, float ca, float cb, BatchRef br) {
+  int epilogue(const float2* X, int op, float hf, float ca, float cb, BatchRef br, int stage) {
     int rc = launch(KC_HERM, [&] {
       const long long total = (long long)cap * 6 * g.k2 * g.k2;
       const long long blocks = (total + 255) / 256;
@@ -401,6 +406,9 @@ struct mhd_problem {
     a.ca = ca;
     a.cb = cb;
     a.op = op;
+    a.step = dstep;
+    a.stage = stage;
+    a.hydro = p.hydro_only;
     const double n3 = (double)g.n * g.n * g.n;
     a.pscale = (float)(1.0 / (n3 * n3));
     const int bx = g.kx <= 256 ? (g.kx + 31) / 32 * 32 : 256;
@@ -417,28 +425,33 @@ struct mhd_problem {
     });
   }
   // record: the stage whose physical fields getCFL! reads (the last one of a step)
-  int rhs(const float2* X, int op, float hf, float ca, float cb, BatchRef br, bool record = false) {
+  // stage: right-hand-side evaluation within the step (7 outside a step)
+  int rhs(const float2* X, int op, float hf, float ca, float cb, BatchRef br, int stage, bool record = false) {
     int rc;
     if ((rc = z_inverse(X, ST(), 6, br))) return rc;
     if ((rc = y_inverse(6, br))) return rc;
     if ((rc = x_fused(br, (record && cfl) ? dvmax : nullptr))) return rc;
     if ((rc = y_forward(kSlots, br))) return rc;
     if ((rc = z_forward(rowbuf, sz.rowbuf, kSlots, br))) return rc;
-    return epilogue(X, op, hf, ca, cb, br);
+    return epilogue(X, op, hf, ca, cb, br, stage);
   }
   // One step of every active slot (launches only; see run_steps for graphs and clocks).
   int issue_step() {
     const BatchRef br = active_ref();
     int rc;
     if (p.scheme == MHD_RK4) {
-      if ((rc = rhs(sol, OP_RK4_FIRST, 0.5f, 0.f, 0.f, br))) return rc;
-      if ((rc = rhs(xs, OP_RK4_MID, 0.5f, 0.f, 0.f, br))) return rc;
-      if ((rc = rhs(xs, OP_RK4_MID, 1.0f, 0.f, 0.f, br))) return rc;
-      if ((rc = rhs(xs, OP_RK4_LAST, 0.f, 0.f, 0.f, br, true))) return rc;
+      if ((rc = rhs(sol, OP_RK4_FIRST, 0.5f, 0.f, 0.f, br, 0))) return rc;
+      if ((rc = rhs(xs, OP_RK4_MID, 0.5f, 0.f, 0.f, br, 1))) return rc;
+      if ((rc = rhs(xs, OP_RK4_MID, 1.0f, 0.f, 0.f, br, 2))) return rc;
+      if ((rc = rhs(xs, OP_RK4_LAST, 0.f, 0.f, 0.f, br, 3, true))) return rc;
     } else {
       for (int i = 0; i < 5; ++i)
-        if ((rc = rhs(sol, i == 0 ? OP_LS_FIRST : OP_LS, 0.f, (float)kLsA[i], (float)kLsB[i], br, i == 4))) return rc;
+        if ((rc = rhs(sol, i == 0 ? OP_LS_FIRST : OP_LS, 0.f, (float)kLsA[i], (float)kLsB[i], br, i, i == 4))) return rc;
     }
+    if (forcing && (rc = launch(KC_OTHER, [&] {
+          step_tick_kernel<<<(cap + 127) / 128, 128, 0, stream>>>(br, dstep);
+        })))
+      return rc;
     if (cfl) return cfl_update(1);
     return MHD_OK;
   }
@@ -485,7 +498,7 @@ struct mhd_problem {
             if ((rc = fold_records())) break;
             for (int c = 0; c < KC_COUNT; ++c) { prof_launches[c] = 0; prof_ms[c] = 0; }
           }
-          rc = rhs(sol, OP_RHS, 0.f, 0.f, 0.f, br);
+          rc = rhs(sol, OP_RHS, 0.f, 0.f, 0.f, br, 7);
         }
         if (rc == MHD_OK) rc = fold_records();
         for (int c = 0; c < kTunedClasses && rc == MHD_OK; ++c)
@@ -597,6 +610,13 @@ struct mhd_problem {
     return z_forward(dst, dI, 1, br);
   }
   bool valid_slot(int s) const { return s >= 0 && s < cap && used[s]; }
+  // Hydrodynamics runs the MHD kernels with B = 0: the epilogue sets the induction right-hand
+  // side to zero, so B stays exactly zero, and the momentum right-hand side is HDcalcN!'s (the
+  // x rows pair uz with bx in one transform, so they see FP32 roundoff in place of bx = 0; its
+  // products enter the momentum at ~1e-14 relative).  Only the three velocity fields cross the
+  // boundary.
+  int nfields() const { return p.hydro_only ? 3 : 6; }
+  long long ref_elems() const { return sz.ref / 6 * nfields(); }
 };
 
 namespace {
@@ -623,6 +643,7 @@ int validate(const mhd_params* p) {
   if (p->nnu > 1 || p->neta > 1) return fail(MHD_ERR_INVALID, "hyper-diffusion (nnu > 1 or neta > 1) is not on this path");
   if (!std::isfinite(p->dt)) return fail(MHD_ERR_INVALID, "dt must be finite");
   if (p->scheme != MHD_RK4 && p->scheme != MHD_LSRK4) return fail(MHD_ERR_INVALID, "scheme must be MHD_RK4 or MHD_LSRK4");
+  if (p->hydro_only != 0 && p->hydro_only != 1) return fail(MHD_ERR_INVALID, "hydro_only must be 0 or 1");
   if (p->precision != MHD_PREC_FP32 && p->precision != MHD_PREC_SPLIT_FP16 && p->precision != MHD_PREC_SPLIT_BF16)
     return fail(MHD_ERR_INVALID, "precision must be MHD_PREC_FP32, MHD_PREC_SPLIT_FP16 or MHD_PREC_SPLIT_BF16");
   if (p->precision != MHD_PREC_FP32 && p->n != 128 && p->n != 256 && p->n != 512)
@@ -679,6 +700,8 @@ int create_class(const mhd_params* params, int cap, mhd_handle* out) {
   MHD_CUDA(cudaMalloc(&h->dlist, (2 * c + 2) * sizeof(int)));
   MHD_CUDA(cudaMalloc(&h->dvmax, 2 * c * sizeof(unsigned int)));
   MHD_CUDA(cudaMalloc(&h->dtime, c * sizeof(double)));
+  MHD_CUDA(cudaMalloc(&h->dstep, c * sizeof(long long)));
+  MHD_CUDA(cudaMemsetAsync(h->dstep, 0, c * sizeof(long long), h->stream));
   MHD_CUDA(cudaMemsetAsync(h->dvmax, 0, 2 * c * sizeof(unsigned int), h->stream));
   MHD_CUDA(cudaMemsetAsync(h->dtime, 0, c * sizeof(double), h->stream));
   MHD_CUDA(cudaMemsetAsync(h->sol, 0, c * s.state * sizeof(float2), h->stream));
@@ -705,6 +728,7 @@ int add_slot(mhd_handle h, double nu, double eta, double dt, int* slot) {
   const double dl = h->p.L / h->g.n, vi = nu > eta ? nu : eta;
   h->hparams[s] = SlotParams{(float)nu, (float)eta, (float)dt, vi > 0 ? (float)(h->cfl_coef * dl * dl / vi) : 0.f};
   if (h->cfl) MHD_CUDA(cudaMemsetAsync(h->dtime + s, 0, sizeof(double), h->stream));
+  MHD_CUDA(cudaMemsetAsync(h->dstep + s, 0, sizeof(long long), h->stream));
   h->t[s] = 0.0;
   h->stepc[s] = 0;
   h->list_dirty = true;
@@ -795,9 +819,9 @@ int mhd_slot_set_state(mhd_handle h, int slot, const float* sol) {
   int rc = check_slot(h, slot);
   if (rc) return rc;
   if (!sol) return fail(MHD_ERR_INVALID, "null sol");
-  MHD_CUDA(cudaMemcpyAsync(h->ref, sol, h->sz.ref * sizeof(float2), cudaMemcpyHostToDevice, h->stream));
+  MHD_CUDA(cudaMemcpyAsync(h->ref, sol, h->ref_elems() * sizeof(float2), cudaMemcpyHostToDevice, h->stream));
   float2* dst = h->sol + slot * h->sz.state;
-  if ((rc = h->launch(KC_OTHER, [&] { gather_state_kernel<<<1216, 256, 0, h->stream>>>(h->ref, dst, h->g, 6); }))) return rc;
+  if ((rc = h->launch(KC_OTHER, [&] { gather_state_kernel<<<1216, 256, 0, h->stream>>>(h->ref, dst, h->g, h->nfields()); }))) return rc;
   MHD_CUDA(cudaStreamSynchronize(h->stream));
   return MHD_OK;
 }
@@ -807,8 +831,8 @@ int mhd_slot_get_state(mhd_handle h, int slot, float* sol) {
   if (rc) return rc;
   if (!sol) return fail(MHD_ERR_INVALID, "null sol");
   const float2* src = h->sol + slot * h->sz.state;
-  if ((rc = h->launch(KC_OTHER, [&] { scatter_state_kernel<<<1216, 256, 0, h->stream>>>(src, h->ref, h->g, 6); }))) return rc;
-  MHD_CUDA(cudaMemcpyAsync(sol, h->ref, h->sz.ref * sizeof(float2), cudaMemcpyDeviceToHost, h->stream));
+  if ((rc = h->launch(KC_OTHER, [&] { scatter_state_kernel<<<1216, 256, 0, h->stream>>>(src, h->ref, h->g, h->nfields()); }))) return rc;
+  MHD_CUDA(cudaMemcpyAsync(sol, h->ref, h->ref_elems() * sizeof(float2), cudaMemcpyDeviceToHost, h->stream));
   MHD_CUDA(cudaStreamSynchronize(h->stream));
   return MHD_OK;
 }
@@ -816,7 +840,8 @@ int mhd_slot_get_state(mhd_handle h, int slot, float* sol) {
 int mhd_slot_set_physical(mhd_handle h, int slot, int field, const float* phys) {
   int rc = check_slot(h, slot);
   if (rc) return rc;
-  if (field < 0 || field > 5) return fail(MHD_ERR_INVALID, "field must be 0..5 (ux uy uz bx by bz)");
+  if (field < 0 || field >= h->nfields())
+    return fail(MHD_ERR_INVALID, h->p.hydro_only ? "field must be 0..2 (ux uy uz)" : "field must be 0..5 (ux uy uz bx by bz)");
   if (!phys) return fail(MHD_ERR_INVALID, "null field array");
   MHD_CUDA(cudaMemcpyAsync(h->phys, phys, h->sz.phys * sizeof(float), cudaMemcpyHostToDevice, h->stream));
   if ((rc = h->forward_field(h->sol + field * h->sz.fs, h->sz.state, slot))) return rc;
@@ -827,7 +852,8 @@ int mhd_slot_set_physical(mhd_handle h, int slot, int field, const float* phys) 
 int mhd_slot_get_physical(mhd_handle h, int slot, int field, float* phys) {
   int rc = check_slot(h, slot);
   if (rc) return rc;
-  if (field < 0 || field > 5) return fail(MHD_ERR_INVALID, "field must be 0..5 (ux uy uz bx by bz)");
+  if (field < 0 || field >= h->nfields())
+    return fail(MHD_ERR_INVALID, h->p.hydro_only ? "field must be 0..2 (ux uy uz)" : "field must be 0..5 (ux uy uz bx by bz)");
   if (!phys) return fail(MHD_ERR_INVALID, "null field array");
   if ((rc = h->inverse_field(h->sol + field * h->sz.fs, h->sz.state, slot))) return rc;
   MHD_CUDA(cudaMemcpyAsync(phys, h->phys, h->sz.phys * sizeof(float), cudaMemcpyDeviceToHost, h->stream));
@@ -859,6 +885,12 @@ int mhd_slot_set_clock(mhd_handle h, int slot, double t, long long step, double 
   if (!std::isfinite(t) || !std::isfinite(dt)) return fail(MHD_ERR_INVALID, "t and dt must be finite");
   h->t[slot] = t;
   h->stepc[slot] = step;
+  {
+    int rc = check_handle(h);
+    if (rc) return rc;
+    MHD_CUDA(cudaMemcpyAsync(h->dstep + slot, &h->stepc[slot], sizeof(long long), cudaMemcpyHostToDevice, h->stream));
+    MHD_CUDA(cudaStreamSynchronize(h->stream));
+  }
   if ((float)dt != h->hparams[slot].dt) {
     h->hparams[slot].dt = (float)dt;
     h->list_dirty = true;
@@ -869,6 +901,61 @@ int mhd_slot_set_clock(mhd_handle h, int slot, double t, long long step, double 
     MHD_CUDA(cudaMemcpyAsync(h->dtime + slot, &h->t[slot], sizeof(double), cudaMemcpyHostToDevice, h->stream));
     MHD_CUDA(cudaStreamSynchronize(h->stream));
   }
+  return MHD_OK;
+}
+
+int mhd_slot_set_forcing(mhd_handle h, int slot, double P, double kf, double sigma, double b,
+                         unsigned long long seed) {
+  int rc = check_slot(h, slot);
+  if (rc) return rc;
+  if (!std::isfinite(P) || P < 0 || !std::isfinite(kf) || !(sigma > 0) || !std::isfinite(sigma) || !(b > 0) ||
+      !std::isfinite(b))
+    return fail(MHD_ERR_INVALID, "forcing needs P >= 0, finite kf, sigma > 0 and b > 0");
+  SlotParams& sp = h->hparams[slot];
+  if (P == 0) {
+    sp.fA = 0.f;
+  } else {
+    // SetUpFk! (src/pgen/A99ForceDriving_GPU.jl:24-48): A = sqrt(P 3 (L/dx)^3 / I / dx^3) with
+    // I = sum over the (nkr, n, n) grid of exp(-(k - kf)^2 / sigma^2) / (k + 1)^2
+    const int n = h->g.n, nkr = n / 2 + 1;
+    const double ks = 2.0 * M_PI / h->p.L, dx = h->p.L / n;
+    double integral = 0.0;
+    for (int z = 0; z < n; ++z) {
+      const double kz = ks * (z < (n + 1) / 2 ? z : z - n);
+      for (int y = 0; y < n; ++y) {
+        const double ky = ks * (y < (n + 1) / 2 ? y : y - n);
+        for (int x = 0; x < nkr; ++x) {
+          const double kx = ks * x;
+          const double k = std::sqrt(kx * kx + ky * ky + kz * kz);
+          integral += std::exp(-(k - kf) * (k - kf) / (sigma * sigma)) / ((k + 1) * (k + 1));
+        }
+      }
+    }
+    sp.fA = (float)std::sqrt(P * 3.0 * (double)n * n * n / integral * (1.0 / (dx * dx * dx)));
+    sp.fkf = (float)b;  // SetUpFk! stores kf = b (src/pgen/A99ForceDriving_GPU.jl:46), kept as is
+    sp.fs2 = (float)(sigma * sigma);
+    sp.fb = (float)b;
+    sp.fseed = seed;
+  }
+  h->list_dirty = true;
+  bool any = false;
+  for (int s = 0; s < h->cap; ++s) any = any || (h->used[s] && h->hparams[s].fA != 0.f);
+  if (any != h->forcing) {
+    h->forcing = any;
+    h->invalidate_graph();
+  }
+  return h->sync_lists();
+}
+
+int mhd_set_forcing(mhd_handle h, double P, double kf, double sigma, double b, unsigned long long seed) {
+  return mhd_slot_set_forcing(h, 0, P, kf, sigma, b, seed);
+}
+
+int mhd_get_forcing(mhd_handle h, int slot, double* A, double* kf_used) {
+  if (!h) return fail(MHD_ERR_INVALID, "null handle");
+  if (!h->valid_slot(slot)) return fail(MHD_ERR_INVALID, "slot " + std::to_string(slot) + " is not active");
+  if (A) *A = h->hparams[slot].fA;
+  if (kf_used) *kf_used = h->hparams[slot].fkf;
   return MHD_OK;
 }
 
@@ -962,9 +1049,9 @@ int mhd_compute_rhs(mhd_handle h, float* rhs_out) {
   int rc = check_slot(h, 0);
   if (rc) return rc;
   if (!rhs_out) return fail(MHD_ERR_INVALID, "null output");
-  if ((rc = h->rhs(h->sol, OP_RHS, 0.f, 0.f, 0.f, h->slot_ref(0)))) return rc;
-  if ((rc = h->launch(KC_OTHER, [&] { scatter_state_kernel<<<1216, 256, 0, h->stream>>>(h->acc, h->ref, h->g, 6); }))) return rc;
-  MHD_CUDA(cudaMemcpyAsync(rhs_out, h->ref, h->sz.ref * sizeof(float2), cudaMemcpyDeviceToHost, h->stream));
+  if ((rc = h->rhs(h->sol, OP_RHS, 0.f, 0.f, 0.f, h->slot_ref(0), 7))) return rc;
+  if ((rc = h->launch(KC_OTHER, [&] { scatter_state_kernel<<<1216, 256, 0, h->stream>>>(h->acc, h->ref, h->g, h->nfields()); }))) return rc;
+  MHD_CUDA(cudaMemcpyAsync(rhs_out, h->ref, h->ref_elems() * sizeof(float2), cudaMemcpyDeviceToHost, h->stream));
   MHD_CUDA(cudaStreamSynchronize(h->stream));
   return MHD_OK;
 }

@@ -71,6 +71,10 @@ struct BatchRef {
 struct SlotParams {
   float nu, eta, dt;
   float tdiff;  // diffusive time-step limit of the on-device CFL (0: none)
+  // A99 random forcing of the velocity (fA = 0: off): amplitude, spectrum peak, width^2,
+  // shape parameter b and generator seed
+  float fA, fkf, fs2, fb;
+  unsigned long long fseed;
 };
 
 struct ColArgs {

@@ -37,7 +37,53 @@ struct RkArgs {
   float ca, cb;         // LSRK4 coefficients of the stage
   float pscale;         // 1/n^6: the column and row passes are unnormalised in both directions
   int op;
+  const long long* step; // per-slot step counters (random forcing: call = 8 * step + stage)
+  int stage;             // right-hand-side evaluation within the step (7: outside a step)
+  int hydro;             // hydrodynamics: the induction right-hand side is zero, B stays zero
 };
+
+// ------------------------------------------------------------------------------------------
+// A99 random solenoidal forcing (src/pgen/A99ForceDriving_GPU.jl:76-130 of MHDFlows.jl), with
+// a counter-based generator in place of the device rand(): uniform numbers from the SplitMix64
+// finaliser of (seed, call, mode index in the reference's (nkr, n, n) layout, draw).
+// ------------------------------------------------------------------------------------------
+__host__ __device__ inline unsigned long long mix64(unsigned long long z) {
+  z += 0x9E3779B97F4A7C15ull;
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+__device__ __forceinline__ float a99_uniform(unsigned long long key, unsigned long long index, int draw) {
+  const unsigned long long z = mix64(key ^ (index * 4ull + (unsigned long long)draw));
+  return (float)(z >> 40) * (1.0f / 16777216.0f);
+}
+// forcing of the three velocity components at wavenumber (kx, ky, kz)
+__device__ __forceinline__ void a99_force(const SlotParams& sp, unsigned long long key, unsigned long long index,
+                                          float kx, float ky, float kz, float2 (&F)[3]) {
+  constexpr float kPi = 3.14159265358979f;
+  const float k = sqrtf(kx * kx + ky * ky + kz * kz);
+  const float kp = sqrtf(kx * kx + kz * kz);
+  const float kinv = k > 0.f ? 1.f / k : 0.f;
+  const float pinv = kp > 0.f ? 1.f / kp : 0.f;
+  const float dk = k - sp.fkf;
+  const float Fk = sp.fA * sqrtf(expf(-dk * dk / sp.fs2) / 2.f / kPi) * kinv;
+  const float e1x = kz * pinv, e1z = -kx * pinv;
+  const float e2x = kx * ky * pinv * kinv, e2y = -kp * kinv, e2z = kz * ky * pinv * kinv;
+  const float th1 = a99_uniform(key, index, 0) * 2.f * kPi;
+  const float phi = a99_uniform(key, index, 1) * kPi;
+  const float th2 = a99_uniform(key, index, 2) * 2.f * kPi;
+  float gi = -tanhf(sp.fb * (phi - kPi / 2)) / tanhf(sp.fb * kPi / 2);
+  if (fabsf(gi) >= 1.f) gi = copysignf(1.f, gi);
+  const float gj = sqrtf(1.f - gi * gi);
+  float s1, c1, s2, c2;
+  sincosf(th1, &s1, &c1);
+  sincosf(th2, &s2, &c2);
+  const float amp = sp.fA * Fk;
+  const float a1 = amp * gi, a2 = amp * gj;
+  F[0] = make_float2(a1 * e1x * c1 + a2 * e2x * c2, a1 * e1x * s1 + a2 * e2x * s2);
+  F[1] = make_float2(a2 * e2y * c2, a2 * e2y * s2);
+  F[2] = make_float2(a1 * e1z * c1 + a2 * e2z * c2, a1 * e1z * s1 + a2 * e2z * s2);
+}
 
 struct RkSlot {
   float2* sol;
@@ -126,11 +172,33 @@ __global__ void __launch_bounds__(256) rk_epilogue_kernel(RkArgs a, Geom geo, Ba
   nl[4] = make_float2(-wy.y, wy.x);
   nl[5] = make_float2(-wz.y, wz.x);
   const float du = -sp.nu * k2, db = -sp.eta * k2;
+  float2 R[6];
 #pragma unroll
   for (int c = 0; c < 6; ++c) {
     const float dk = c < 3 ? du : db;
-    rk_apply<OP>(rs, c * fs + i, xv[c], make_float2(nl[c].x + dk * xd[c].x, nl[c].y + dk * xd[c].y));
+    R[c] = make_float2(nl[c].x + dk * xd[c].x, nl[c].y + dk * xd[c].y);
   }
+  if (sp.fA != 0.f) {  // addforcing!: N[u] += F, then the kx = 0 plane keeps its real part
+    const unsigned long long call = 8ull * (unsigned long long)a.step[slot] + (unsigned long long)a.stage;
+    const unsigned long long key = mix64(sp.fseed ^ mix64(call));
+    const int nkr = geo.n / 2 + 1;
+    const unsigned long long index =
+        (unsigned long long)x + (unsigned long long)nkr * ((unsigned long long)freq_of_kept(geo, jy) +
+                                                            (unsigned long long)geo.n * freq_of_kept(geo, jz));
+    float2 F[3];
+    a99_force(sp, key, index, kxv, kyv, kzv, F);
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      R[c] = make_float2(R[c].x + F[c].x, R[c].y + F[c].y);
+      if (x == 0) R[c].y = 0.f;
+    }
+  }
+  if (a.hydro) {  // B = 0: only roundoff of the paired x-row transforms would feed it
+#pragma unroll
+    for (int c = 3; c < 6; ++c) R[c] = make_float2(0.f, 0.f);
+  }
+#pragma unroll
+  for (int c = 0; c < 6; ++c) rk_apply<OP>(rs, c * fs + i, xv[c], R[c]);
 }
 
 // Hermitian part of the kx = 0 plane of the six fields: H(k) = (X(k) + conj X(-k)) / 2, with
@@ -181,6 +249,12 @@ __global__ void cfl_update_kernel(BatchRef br, SlotParams* sp, unsigned int* vma
     vmax[2 * s] = 0u;
     vmax[2 * s + 1] = 0u;
   }
+}
+
+// one step of every active slot taken: advance the per-slot step counters (random forcing)
+__global__ void step_tick_kernel(BatchRef br, long long* steps) {
+  const int n = *br.count;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) steps[br.list[i]] += 1;
 }
 
 // max |field| of one physical field into vmax[which] (initial fields before the first CFL step).

@@ -28,6 +28,7 @@ struct MhdParams
   scheme::Cint
   precision::Cint
   device::Cint
+  hydro_only::Cint
 end
 
 check(rc) = rc == 0 ? nothing : error(unsafe_string(ccall((:mhd_last_error, libmhdgb), Cstring, ())))
@@ -37,10 +38,15 @@ mutable struct GB300TimeStepper{T} <: FourierFlows.AbstractTimeStepper{T}
   n::Int
 end
 
-function GB300TimeStepper(grid, params, dt; scheme::Symbol = :RK4, device::Integer = 0)
+function GB300TimeStepper(grid, params, dt; scheme::Symbol = :RK4, device::Integer = 0,
+                          B_field::Bool = true, precision::Symbol = :FP32)
   grid.nx == grid.ny == grid.nz || error("GB300TimeStepper needs a cubic grid")
-  p = MhdParams(grid.nx, grid.Lx, params.ν, params.η, params.nν, params.nη, dt,
-                scheme == :RK4 ? 0 : 1, 0, device)
+  prec = precision == :FP32 ? 0 : precision == :SPLIT_FP16 ? 1 : precision == :SPLIT_BF16 ? 2 :
+         error("precision must be :FP32, :SPLIT_FP16 or :SPLIT_BF16")
+  eta = B_field ? params.η : 0.0
+  neta = B_field ? params.nη : 0
+  p = MhdParams(grid.nx, grid.Lx, params.ν, eta, params.nν, neta, dt,
+                scheme == :RK4 ? 0 : 1, prec, device, B_field ? 0 : 1)
   h = Ref{Ptr{Cvoid}}(C_NULL)
   check(ccall((:mhd_create, libmhdgb), Cint, (Ref{MhdParams}, Ref{Ptr{Cvoid}}), p, h))
   ts = GB300TimeStepper{Array{ComplexF32,4}}(h[], grid.nx)
@@ -73,7 +79,8 @@ end
 # updatevars!(prob): vars.ux..bz <- irfft(sol) of the current state
 function gb300_updatevars!(prob)
   ts = prob.timestepper
-  for (f, name) in enumerate((:ux, :uy, :uz, :bx, :by, :bz))
+  names = hasproperty(prob.vars, :bx) ? (:ux, :uy, :uz, :bx, :by, :bz) : (:ux, :uy, :uz)
+  for (f, name) in enumerate(names)
     host = Array{Float32}(undef, ts.n, ts.n, ts.n)
     check(ccall((:mhd_get_physical, libmhdgb), Cint, (Ptr{Cvoid}, Cint, Ptr{Float32}), ts.handle, f - 1, host))
     copyto!(getfield(prob.vars, name), host)

@@ -268,28 +268,35 @@ class Stepper:
             raise ValueError(f"unknown stepper {scheme!r}")
         self.vars = [np.zeros((grid.n,) * 3, dtype=grid.dtype) for _ in range(6)]
 
-    def calcN(self, N, X):
+    # A99 forcing (add_a99_forcing): None or dict(A, kf_used, sigma2, b, seed)
+    forcing = None
+
+    def calcN(self, N, X, stage=0):
         if self.literal:
-            return calcN_literal(N, X, self.g, self.nu, self.eta, self.nnu, self.neta, self.vars)
-        return calcN_fast(N, X, self.g, self.nu, self.eta)
+            calcN_literal(N, X, self.g, self.nu, self.eta, self.nnu, self.neta, self.vars)
+        else:
+            calcN_fast(N, X, self.g, self.nu, self.eta)
+        if self.forcing is not None:
+            add_a99_forcing(N, self.g, self.forcing, 8 * self.step + stage)
+        return N
 
     def stepforward(self, sol):
         dt = self.dt
         if self.scheme == "RK4":
             R1, R2, R3, R4 = self.R
             s1 = self.sol1
-            self.calcN(R1, sol)
+            self.calcN(R1, sol, 0)
             np.add(sol, (dt / 2) * R1, out=s1)
-            self.calcN(R2, s1)
+            self.calcN(R2, s1, 1)
             np.add(sol, (dt / 2) * R2, out=s1)
-            self.calcN(R3, s1)
+            self.calcN(R3, s1, 2)
             np.add(sol, dt * R3, out=s1)
-            self.calcN(R4, s1)
+            self.calcN(R4, s1, 3)
             sol += dt * (R1 / 6 + R2 / 3 + R3 / 3 + R4 / 6)
         else:
             S2, R = self.S2, self.RHS
             for i in range(5):
-                self.calcN(R, sol)
+                self.calcN(R, sol, i)
                 if i == 0:
                     S2[...] = dt * R
                 else:
@@ -479,3 +486,85 @@ def rel_l2(a, b, mask=None):
         b = b[..., mask]
     den = np.linalg.norm(b)
     return float(np.linalg.norm(a - b) / (den if den > 0 else 1.0))
+
+
+# ----------------------------------------------------------------------------------------------
+# A99 random solenoidal forcing (src/pgen/A99ForceDriving_GPU.jl of MHDFlows.jl), restated.
+# SetUpFk! (:24-48) computes the amplitude A from the forcing spectrum over the whole (nkr, n, n)
+# grid; A99Force_Driving_CUDA! (:76-130) adds A*Fk*(e^{i th1} gi e1 + e^{i th2} gj e2) to the
+# velocity right-hand side at every call with fresh random numbers, then keeps only the real part
+# of the whole right-hand side on the kx = 0 (and Nyquist) planes.  Restated as the reference
+# does it, including two of its quirks: SetUpFk! stores kf = b (:46), so the kernel's spectrum
+# peaks at k = b; and Fk already carries the factor A, so the amplitude is A^2 Fk/A.
+# The reference draws its random numbers with the device rand(); here they come from a
+# counter-based generator (SplitMix64 finaliser) keyed by (seed, call, mode, draw), which the
+# GPU kernels evaluate identically: call = 8 * step + stage, mode = x + nkr * (y + n * z) in the
+# reference's (nkr, n, n) layout, draws 0, 1, 2 = th1 / 2pi, phi / pi, th2 / 2pi.
+# ----------------------------------------------------------------------------------------------
+_M64 = np.uint64(0xFFFFFFFFFFFFFFFF)
+
+
+def _mix64(z):
+    """SplitMix64 finaliser on uint64 arrays (wrapping arithmetic)."""
+    with np.errstate(over="ignore"):
+        z = np.asarray(z, dtype=np.uint64) + np.uint64(0x9E3779B97F4A7C15)
+        z = (z ^ (z >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)
+        z = (z ^ (z >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)
+        return z ^ (z >> np.uint64(31))
+
+
+def a99_uniform(seed: int, call: int, index, draw: int):
+    """Uniform numbers in [0, 1) with 24 bits, float32, for mode indices ``index``."""
+    key = _mix64(np.uint64(seed) ^ _mix64(np.uint64(call)))
+    with np.errstate(over="ignore"):
+        z = _mix64(key ^ (np.asarray(index, dtype=np.uint64) * np.uint64(4) + np.uint64(draw)))
+    return ((z >> np.uint64(40)).astype(np.float64) * (1.0 / 16777216.0)).astype(np.float32)
+
+
+def a99_amplitude(grid: Grid, kf: float = 2.0, P: float = 1.0, sigma: float = 1.0) -> float:
+    """A of SetUpFk! (src/pgen/A99ForceDriving_GPU.jl:24-48), in float64."""
+    g = grid
+    k = np.sqrt(g.Krsq.astype(np.float64))
+    integral = float(np.sum(np.exp(-(k - kf) ** 2 / sigma ** 2) / (k + 1) ** 2))
+    return math.sqrt(P * 3 * g.n ** 3 / integral * (1 / g.dx ** 3))
+
+
+def a99_force(grid: Grid, A: float, kf_used: float, sigma2: float, b: float, seed: int, call: int):
+    """Forcing of the three velocity components, (3, n, n, nkr) complex128, of one call."""
+    g = grid
+    kx = np.broadcast_to(g.kr.astype(np.float64), g.Krsq.shape)
+    ky = np.broadcast_to(g.l.astype(np.float64), g.Krsq.shape)
+    kz = np.broadcast_to(g.m.astype(np.float64), g.Krsq.shape)
+    k = np.sqrt(kx ** 2 + ky ** 2 + kz ** 2)
+    kp = np.sqrt(kx ** 2 + kz ** 2)
+    with np.errstate(divide="ignore", invalid="ignore"):
+        kinv = np.where(k > 0, 1 / k, 0.0)
+        pinv = np.where(kp > 0, 1 / kp, 0.0)
+    Fk = A * np.sqrt(np.exp(-(k - kf_used) ** 2 / sigma2) / 2 / math.pi) * kinv
+    e1x, e1z = kz * pinv, -kx * pinv
+    e2x, e2y, e2z = kx * ky * pinv * kinv, -kp * kinv, kz * ky * pinv * kinv
+    index = np.arange(k.size, dtype=np.uint64).reshape(k.shape)
+    th1 = a99_uniform(seed, call, index, 0).astype(np.float64) * 2 * math.pi
+    phi = a99_uniform(seed, call, index, 1).astype(np.float64) * math.pi
+    th2 = a99_uniform(seed, call, index, 2).astype(np.float64) * 2 * math.pi
+    gi = -np.tanh(b * (phi - math.pi / 2)) / math.tanh(b * math.pi / 2)
+    gi = np.where(np.abs(gi) >= 1.0, np.sign(gi), gi)
+    gj = np.sqrt(1 - gi ** 2)
+    p1, p2 = np.exp(1j * th1), np.exp(1j * th2)
+    amp = A * Fk
+    F = np.empty((3,) + k.shape, dtype=np.complex128)
+    F[0] = amp * (p1 * gi * e1x + p2 * gj * e2x)
+    F[1] = amp * p2 * gj * e2y
+    F[2] = amp * (p1 * gi * e1z + p2 * gj * e2z)
+    return F
+
+
+def add_a99_forcing(N, grid: Grid, forcing: dict, call: int):
+    """addforcing! with the A99 hook: N[u] += F, then the kx = 0 and Nyquist planes of the whole
+    velocity right-hand side keep only their real parts (src/pgen/A99ForceDriving_GPU.jl:121-127)."""
+    F = a99_force(grid, forcing["A"], forcing["kf_used"], forcing["sigma2"], forcing["b"], forcing["seed"], call)
+    N[0:3] += F.astype(N.dtype)
+    for c in range(3):
+        N[c, :, :, 0] = N[c, :, :, 0].real
+        N[c, :, :, -1] = N[c, :, :, -1].real
+    return N
