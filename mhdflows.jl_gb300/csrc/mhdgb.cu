@@ -414,17 +414,22 @@ struct mhd_problem {
     const int bx = g.kx <= 256 ? (g.kx + 31) / 32 * 32 : 256;
     const dim3 grid((g.kx + bx - 1) / bx, g.k2, g.k2 * cap);
     return launch(KC_RKEPI, [&] {
-      switch (op) {
-        case OP_RHS: rk_epilogue_kernel<OP_RHS><<<grid, bx, 0, stream>>>(a, g, br); break;
-        case OP_RK4_FIRST: rk_epilogue_kernel<OP_RK4_FIRST><<<grid, bx, 0, stream>>>(a, g, br); break;
-        case OP_RK4_MID: rk_epilogue_kernel<OP_RK4_MID><<<grid, bx, 0, stream>>>(a, g, br); break;
-        case OP_RK4_LAST: rk_epilogue_kernel<OP_RK4_LAST><<<grid, bx, 0, stream>>>(a, g, br); break;
-        case OP_LS_FIRST: rk_epilogue_kernel<OP_LS_FIRST><<<grid, bx, 0, stream>>>(a, g, br); break;
-        default: rk_epilogue_kernel<OP_LS><<<grid, bx, 0, stream>>>(a, g, br); break;
-      }
+      if (forcing) launch_epilogue<true>(op, grid, bx, a, br);
+      else launch_epilogue<false>(op, grid, bx, a, br);
     });
   }
   // record: the stage whose physical fields getCFL! reads (the last one of a step)
+  template <bool F>
+  void launch_epilogue(int op, dim3 grid, int bx, const RkArgs& a, BatchRef br) {
+    switch (op) {
+      case OP_RHS: rk_epilogue_kernel<OP_RHS, F><<<grid, bx, 0, stream>>>(a, g, br); break;
+      case OP_RK4_FIRST: rk_epilogue_kernel<OP_RK4_FIRST, F><<<grid, bx, 0, stream>>>(a, g, br); break;
+      case OP_RK4_MID: rk_epilogue_kernel<OP_RK4_MID, F><<<grid, bx, 0, stream>>>(a, g, br); break;
+      case OP_RK4_LAST: rk_epilogue_kernel<OP_RK4_LAST, F><<<grid, bx, 0, stream>>>(a, g, br); break;
+      case OP_LS_FIRST: rk_epilogue_kernel<OP_LS_FIRST, F><<<grid, bx, 0, stream>>>(a, g, br); break;
+      default: rk_epilogue_kernel<OP_LS, F><<<grid, bx, 0, stream>>>(a, g, br); break;
+    }
+  }
   // stage: right-hand-side evaluation within the step (7 outside a step)
   int rhs(const float2* X, int op, float hf, float ca, float cb, BatchRef br, int stage, bool record = false) {
     int rc;
@@ -815,13 +820,47 @@ int mhd_batch_info(mhd_handle h, int* capacity, int* active) {
   return MHD_OK;
 }
 
+}  // extern "C"
+
+namespace {
+
+// Device address of a host buffer of `bytes` bytes that kernels can read and write directly:
+// page-locked memory mapped into the device address space (mhd_host_alloc, cudaHostAlloc,
+// cudaHostRegister), where a kernel reaches the host over NVLink-C2C / PCIe without a staging
+// copy.  Both ends of the range must lie in one mapping.  nullptr for anything else (pageable
+// memory goes through the staging buffer and cudaMemcpyAsync).
+void* mapped_host(const void* p, size_t bytes) {
+  cudaPointerAttributes a0, a1;
+  const char* q = static_cast<const char*>(p);
+  if (cudaPointerGetAttributes(&a0, q) != cudaSuccess || cudaPointerGetAttributes(&a1, q + bytes - 1) != cudaSuccess) {
+    cudaGetLastError();  // clear the error of a pointer the runtime does not know
+    return nullptr;
+  }
+  if (a0.type != cudaMemoryTypeHost || a1.type != cudaMemoryTypeHost || !a0.devicePointer || !a1.devicePointer)
+    return nullptr;
+  if (static_cast<char*>(a1.devicePointer) - static_cast<char*>(a0.devicePointer) != (ptrdiff_t)(bytes - 1))
+    return nullptr;
+  return a0.devicePointer;
+}
+
+}  // namespace
+
+extern "C" {
+
 int mhd_slot_set_state(mhd_handle h, int slot, const float* sol) {
   int rc = check_slot(h, slot);
   if (rc) return rc;
   if (!sol) return fail(MHD_ERR_INVALID, "null sol");
-  MHD_CUDA(cudaMemcpyAsync(h->ref, sol, h->ref_elems() * sizeof(float2), cudaMemcpyHostToDevice, h->stream));
+  const size_t bytes = h->ref_elems() * sizeof(float2);
+  // mapped host memory: the gather kernel reads only the retained band straight from the
+  // caller's array; otherwise the whole array is staged first
+  const float2* src = static_cast<const float2*>(mapped_host(sol, bytes));
+  if (!src) {
+    MHD_CUDA(cudaMemcpyAsync(h->ref, sol, bytes, cudaMemcpyHostToDevice, h->stream));
+    src = h->ref;
+  }
   float2* dst = h->sol + slot * h->sz.state;
-  if ((rc = h->launch(KC_OTHER, [&] { gather_state_kernel<<<1216, 256, 0, h->stream>>>(h->ref, dst, h->g, h->nfields()); }))) return rc;
+  if ((rc = h->launch(KC_OTHER, [&] { gather_state_kernel<<<1216, 256, 0, h->stream>>>(src, dst, h->g, h->nfields()); }))) return rc;
   MHD_CUDA(cudaStreamSynchronize(h->stream));
   return MHD_OK;
 }
@@ -831,8 +870,13 @@ int mhd_slot_get_state(mhd_handle h, int slot, float* sol) {
   if (rc) return rc;
   if (!sol) return fail(MHD_ERR_INVALID, "null sol");
   const float2* src = h->sol + slot * h->sz.state;
-  if ((rc = h->launch(KC_OTHER, [&] { scatter_state_kernel<<<1216, 256, 0, h->stream>>>(src, h->ref, h->g, h->nfields()); }))) return rc;
-  MHD_CUDA(cudaMemcpyAsync(sol, h->ref, h->ref_elems() * sizeof(float2), cudaMemcpyDeviceToHost, h->stream));
+  const size_t bytes = h->ref_elems() * sizeof(float2);
+  float2* out = static_cast<float2*>(mapped_host(sol, bytes));  // scatter straight into mapped memory
+  if ((rc = h->launch(KC_OTHER, [&] {
+         scatter_state_kernel<<<1216, 256, 0, h->stream>>>(src, out ? out : h->ref, h->g, h->nfields());
+       })))
+    return rc;
+  if (!out) MHD_CUDA(cudaMemcpyAsync(sol, h->ref, bytes, cudaMemcpyDeviceToHost, h->stream));
   MHD_CUDA(cudaStreamSynchronize(h->stream));
   return MHD_OK;
 }

@@ -120,7 +120,7 @@ __device__ __forceinline__ void rk_apply(const RkSlot& a, long long o, float2 x,
 }
 
 // grid (ceil(kx / blockDim.x), k2, k2): one thread per retained mode, no index division.
-template <int OP>
+template <int OP, bool FORCED>
 __global__ void __launch_bounds__(256) rk_epilogue_kernel(RkArgs a, Geom geo, BatchRef br) {
   const int x = blockIdx.x * blockDim.x + threadIdx.x;
   if (x >= geo.kx) return;
@@ -178,7 +178,7 @@ __global__ void __launch_bounds__(256) rk_epilogue_kernel(RkArgs a, Geom geo, Ba
     const float dk = c < 3 ? du : db;
     R[c] = make_float2(nl[c].x + dk * xd[c].x, nl[c].y + dk * xd[c].y);
   }
-  if (sp.fA != 0.f) {  // addforcing!: N[u] += F, then the kx = 0 plane keeps its real part
+  if (FORCED && sp.fA != 0.f) {  // addforcing!: N[u] += F, then the kx = 0 plane keeps its real part
     const unsigned long long call = 8ull * (unsigned long long)a.step[slot] + (unsigned long long)a.stage;
     const unsigned long long key = mix64(sp.fseed ^ mix64(call));
     const int nkr = geo.n / 2 + 1;

@@ -1,0 +1,53 @@
+"""State transfer through page-locked host buffers (mhd_host_alloc): the gather / scatter kernels
+read and write the mapped buffer directly.  Results must equal the pageable-memory path bit for
+bit; a pageable buffer goes through the staging copy."""
+import ctypes as C
+import math
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _pinned(lib, pkg, nbytes):
+    p = C.c_void_p()
+    pkg._lib.check(lib.mhd_host_alloc(nbytes, C.byref(p)))
+    return p
+
+
+@pytest.mark.parametrize("n", [32, 96])
+def test_pinned_state_roundtrip_equals_pageable(pkg, mo, lib, n):
+    g = mo.Grid(n)
+    s = mo.random_spectrum_state(g, seed=51).astype(np.complex64)
+    s[:, 3, 2, 1] += 0.5 - 0.25j
+    nbytes = s.nbytes
+    pin_in, pin_out = _pinned(lib, pkg, nbytes), _pinned(lib, pkg, nbytes)
+    try:
+        C.memmove(pin_in, s.ctypes.data, nbytes)
+        with pkg.Problem(pkg.GPU(0), nx=n, Lx=2 * math.pi, nu=1e-3, eta=1e-3, dt=1e-3) as prob:
+            pkg._lib.check(lib.mhd_set_state(prob.handle, pin_in))
+            pageable = prob.sol_c()
+            C.memset(pin_out, 0x7f, nbytes)  # garbage: every element must be overwritten
+            pkg._lib.check(lib.mhd_get_state(prob.handle, pin_out))
+            got = np.frombuffer((C.c_char * nbytes).from_address(pin_out.value), dtype=np.complex64).reshape(s.shape).copy()
+            pkg.stepforward(prob, 2)
+            after_pageable = prob.sol_c()
+            pkg._lib.check(lib.mhd_get_state(prob.handle, pin_out))
+            after_pinned = np.frombuffer((C.c_char * nbytes).from_address(pin_out.value), dtype=np.complex64).reshape(s.shape).copy()
+        assert np.array_equal(got, pageable)
+        assert np.array_equal(got, g.dealias(s.copy()))
+        assert np.array_equal(after_pinned, after_pageable)
+    finally:
+        lib.mhd_host_free(pin_in)
+        lib.mhd_host_free(pin_out)
+
+
+def test_pageable_buffer_uses_staging(pkg, mo, lib):
+    n = 32
+    g = mo.Grid(n)
+    s = mo.random_spectrum_state(g, seed=52).astype(np.complex64)
+    buf = np.ascontiguousarray(s)  # pageable host array
+    with pkg.Problem(pkg.GPU(0), nx=n, Lx=2 * math.pi, nu=1e-3, eta=1e-3, dt=1e-3) as prob:
+        pkg._lib.check(lib.mhd_set_state(prob.handle, buf.ctypes.data))
+        assert np.array_equal(prob.sol_c(), g.dealias(s.copy()))
