@@ -104,7 +104,7 @@ struct ColWork {
 // PIN the rows are kept indices and land at their frequency position row' (non-negative modes
 // in place, negative modes at row + n - K2); the alias rows in between are zero-filled, so the
 // transform reads every row unconditionally.
-template <int TX, int NT, int N, bool PIN>
+template <int TX, int NT, int N, bool PIN, int G>
 __device__ __forceinline__ void col_prefetch(float2* buf, const float2* src, long long sR, int rows, int col0,
                                              const Geom& geo) {
   constexpr int CH = TX / 2;       // 16-byte chunks per row
@@ -112,9 +112,16 @@ __device__ __forceinline__ void col_prefetch(float2* buf, const float2* src, lon
   const int q = threadIdx.x % CH;
   int row = threadIdx.x / CH;
   if (PIN) {
-    float4* zb = reinterpret_cast<float4*>(buf + geo.kp * TX);
-    const int nz = (N - geo.k2) * CH;
-    for (int c = threadIdx.x; c < nz; c += NT) zb[c] = make_float4(0.f, 0.f, 0.f, 0.f);
+    // the transform reads the alias rows only inside lane groups (G consecutive rows) that also
+    // hold kept rows; groups wholly inside the alias band are compile-time zeros
+    constexpr int KP = kept_kx_of(N), KN = kept_kn_of(N);
+    float4* zb = reinterpret_cast<float4*>(buf + KP * TX);
+    constexpr int nz = (N - KP - KN) * CH;
+    for (int c = threadIdx.x; c < nz; c += NT) {
+      const int r = KP + c / CH;
+      const int gs = r / G * G;
+      if (gs < KP || gs + G - 1 >= N - KN) zb[c] = make_float4(0.f, 0.f, 0.f, 0.f);
+    }
   }
   if (col0 + 2 * q >= geo.kxp) return;
   const float2* s = src + row * sR + col0 + 2 * q;
@@ -168,14 +175,14 @@ __global__ void __launch_bounds__(TX * P0::G, MINB)
   };
   int t = blockIdx.x;
   Cur cur_t = decompose(t);
-  if (t < total) col_prefetch<TX, NT, N, PIN>(smem, tile_src(cur_t), a.sR, w.rows_in, cur_t.tx * TX, geo);
+  if (t < total) col_prefetch<TX, NT, N, PIN, P::G>(smem, tile_src(cur_t), a.sR, w.rows_in, cur_t.tx * TX, geo);
   cp_async_commit();
   for (int it = 0; t < total; t += gridDim.x, ++it) {
     float2* cur = smem + (it & 1) * (N * TX);
     const int tn = t + gridDim.x;
     const Cur nxt = advance(cur_t);
     if (tn < total)
-      col_prefetch<TX, NT, N, PIN>(smem + ((it + 1) & 1) * (N * TX), tile_src(nxt), a.sR, w.rows_in, nxt.tx * TX, geo);
+      col_prefetch<TX, NT, N, PIN, P::G>(smem + ((it + 1) & 1) * (N * TX), tile_src(nxt), a.sR, w.rows_in, nxt.tx * TX, geo);
     cp_async_commit();
     cp_async_wait<1>();
     __syncthreads();
