@@ -170,16 +170,17 @@ class Ops : public OpsBase {
     xv.push_back(v);
   }
 
-  // column passes (y and z): plan C, TX kx columns per tile, MINB CTAs per SM
-  template <class C, int TX, int MINB>
+  // column passes (y and z): plan C, TX kx columns per tile, MINB CTAs per SM, NBUF tile buffers
+  template <class C, int TX, int MINB, int NBUF = 2>
   void add_col() {
     ColVariant c;
-    c.name = "col:" + plan_name<C>() + "/tx" + std::to_string(TX) + "/b" + std::to_string(MINB);
-    c.inv = col_pass_kernel<C, TX, +1, true, false, MINB>;
-    c.fwd = col_pass_kernel<C, TX, -1, false, true, MINB>;
+    c.name = "col:" + plan_name<C>() + "/tx" + std::to_string(TX) + "/b" + std::to_string(MINB) +
+             (NBUF == 2 ? std::string() : "/q" + std::to_string(NBUF));
+    c.inv = col_pass_kernel<C, TX, +1, true, false, MINB, NBUF>;
+    c.fwd = col_pass_kernel<C, TX, -1, false, true, MINB, NBUF>;
     c.threads = TX * C::G;
     c.tx = TX;
-    c.smem = sizeof(float2) * 2 * (size_t)N * TX;
+    c.smem = sizeof(float2) * NBUF * (size_t)N * TX;
     c.tw = twiddles<C>();
     cv.push_back(c);
   }

@@ -131,9 +131,11 @@ __device__ __forceinline__ void col_prefetch(float2* buf, const float2* src, lon
   }
 }
 
-template <class P0, int TX, int DIR, bool PIN, bool POUT, int MINB>
+// NBUF tile buffers: NBUF - 1 tiles are being fetched while one is transformed.
+template <class P0, int TX, int DIR, bool PIN, bool POUT, int MINB, int NBUF>
 __global__ void __launch_bounds__(TX * P0::G, MINB)
     col_pass_kernel(ColArgs a, Geom geo, ColWork w, BatchRef br, const float2* __restrict__ tw) {
+  static_assert(NBUF >= 2 && NBUF <= 4, "two to four tile buffers");
   using P = Unpadded<P0>;
   extern __shared__ float2 smem[];
   constexpr int G = P::G, V = P::V, N = P::N, NT = TX * P0::G;
@@ -175,20 +177,31 @@ __global__ void __launch_bounds__(TX * P0::G, MINB)
   };
   int t = blockIdx.x;
   Cur cur_t = decompose(t);
-  if (t < total) col_prefetch<TX, NT, N, PIN, P::G>(smem, tile_src(cur_t), a.sR, w.rows_in, cur_t.tx * TX, geo);
-  cp_async_commit();
-  for (int it = 0; t < total; t += gridDim.x, ++it) {
-    float2* cur = smem + (it & 1) * (N * TX);
-    const int tn = t + gridDim.x;
-    const Cur nxt = advance(cur_t);
-    if (tn < total)
-      col_prefetch<TX, NT, N, PIN, P::G>(smem + ((it + 1) & 1) * (N * TX), tile_src(nxt), a.sR, w.rows_in, nxt.tx * TX, geo);
+  // prologue: the first NBUF - 1 tiles of this CTA (one commit group each, empty past the end)
+  int tp = t;
+  Cur pre_t = cur_t;
+#pragma unroll
+  for (int j = 0; j < NBUF - 1; ++j) {
+    if (tp < total) col_prefetch<TX, NT, N, PIN, P::G>(smem + j * (N * TX), tile_src(pre_t), a.sR, w.rows_in, pre_t.tx * TX, geo);
     cp_async_commit();
-    cp_async_wait<1>();
+    tp += gridDim.x;
+    pre_t = advance(pre_t);
+  }
+  for (int it = 0; t < total; t += gridDim.x, ++it) {
+    float2* cur = smem + (it % NBUF) * (N * TX);
+    // tile it + NBUF - 1 into the buffer that tile it - 1 used (freed by the barrier ending the
+    // previous iteration)
+    if (tp < total)
+      col_prefetch<TX, NT, N, PIN, P::G>(smem + ((it + NBUF - 1) % NBUF) * (N * TX), tile_src(pre_t), a.sR, w.rows_in,
+                                         pre_t.tx * TX, geo);
+    cp_async_commit();
+    tp += gridDim.x;
+    pre_t = advance(pre_t);
+    cp_async_wait<NBUF - 1>();
     __syncthreads();
     const int inst = cur_t.inst, f = cur_t.f, o = cur_t.o;
     const int kxg = cur_t.tx * TX + tx;
-    cur_t = nxt;
+    cur_t = advance(cur_t);
     float2 v[1][V];
 #pragma unroll
     for (int d = 0; d < P::DI; ++d)
