@@ -289,19 +289,28 @@ __global__ void gather_state_kernel(const float2* __restrict__ ref, float2* __re
   }
 }
 
+// One element of the reference layout from the compact state (zero in the alias band).
+__device__ __forceinline__ float2 ref_value(const float2* __restrict__ S, const Geom& geo, long long i, int nkr) {
+  const int x = (int)(i % nkr);
+  long long r = i / nkr;
+  const int fy = (int)(r % geo.n); r /= geo.n;
+  const int fz = (int)(r % geo.n);
+  const int f = (int)(r / geo.n);
+  const int jy = kept_of_freq(geo, fy), jz = kept_of_freq(geo, fz);
+  if (x < geo.kx && jy >= 0 && jz >= 0) return S[(((long long)f * geo.k2 + jz) * geo.k2 + jy) * geo.kxp + x];
+  return make_float2(0.f, 0.f);
+}
+
+// Compact state -> reference layout, two elements (one 16-byte store) per thread and step: the
+// element count nf n^2 nkr is even and ref is 16-byte aligned, so every pair is aligned.  The
+// output may be mapped host memory, where wide stores use the host link better.
 __global__ void scatter_state_kernel(const float2* __restrict__ S, float2* __restrict__ ref, Geom geo, int nf) {
   const int nkr = geo.n / 2 + 1;
-  const long long total = (long long)nf * geo.n * geo.n * nkr;
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total; i += (long long)gridDim.x * blockDim.x) {
-    const int x = (int)(i % nkr);
-    long long r = i / nkr;
-    const int fy = (int)(r % geo.n); r /= geo.n;
-    const int fz = (int)(r % geo.n);
-    const int f = (int)(r / geo.n);
-    float2 val = make_float2(0.f, 0.f);
-    const int jy = kept_of_freq(geo, fy), jz = kept_of_freq(geo, fz);
-    if (x < geo.kx && jy >= 0 && jz >= 0) val = S[(((long long)f * geo.k2 + jz) * geo.k2 + jy) * geo.kxp + x];
-    ref[i] = val;
+  const long long pairs = (long long)nf * geo.n * geo.n * nkr / 2;
+  float4* out = reinterpret_cast<float4*>(ref);
+  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < pairs; p += (long long)gridDim.x * blockDim.x) {
+    const float2 a = ref_value(S, geo, 2 * p, nkr), b = ref_value(S, geo, 2 * p + 1, nkr);
+    out[p] = make_float4(a.x, a.y, b.x, b.y);
   }
 }
 
