@@ -1,6 +1,6 @@
 """Benchmark: MHD RK4 step, 256^3, FP32 (plain form), on N GPUs as independent replicas.
 
-    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference] [--n 256]
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference] [--grid 256]
 
 A step is one RK4 step (4 right-hand-side evaluations, 24 kernel launches) of the seeded random
 k^4 exp(-2(k/4)^2) problem with nu = eta = 1e-3, dt = 5e-4.  `value` is whole-job grid-point
@@ -407,7 +407,7 @@ def main():
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--n", type=int, default=256)
+    ap.add_argument("--grid", dest="n", type=int, default=256, help="grid points per axis of the step workload")
     ap.add_argument("--precision", default="fp32", choices=["fp32", "split_fp16", "split_bf16"],
                     help="x-row transforms in FP32 (plain form) or as split 16-bit tensor-core DFTs")
     ap.add_argument("--no-cpu-baseline", action="store_true")

@@ -13,7 +13,8 @@ module MHDFlowsGB300
 using FourierFlows
 import FourierFlows: stepforward!
 
-export GB300TimeStepper, gb300_updatevars!, sync_sol!, push_sol!, gb300_diagnostics
+export GB300TimeStepper, gb300_updatevars!, sync_sol!, push_sol!, gb300_diagnostics, gb300_autotune!,
+       gb300_SetUpFk!
 
 const libmhdgb = get(ENV, "MHDGB_LIB", joinpath(@__DIR__, "..", "lib", "libmhdgb.so"))
 
@@ -95,5 +96,16 @@ function gb300_diagnostics(ts::GB300TimeStepper)
   check(rc)
   return out
 end
+
+# Kernel variants: time the candidates of each FFT pass once for this device and grid size (the
+# choice is cached per process and in the tuning file; flags: 1 = force, 2 = no file).
+gb300_autotune!(ts::GB300TimeStepper; force::Bool = false) =
+  check(ccall((:mhd_autotune, libmhdgb), Cint, (Ptr{Cvoid}, Cint), ts.handle, force ? 1 : 0))
+
+# SetUpFk!(prob; kf, P, σ, b) + the A99ForceDriving! calcF! hook (src/pgen/A99ForceDriving_GPU.jl):
+# P = 0 turns the forcing off; the random numbers come from a generator keyed by `seed`.
+gb300_SetUpFk!(ts::GB300TimeStepper; kf = 2.0, P = 1.0, σ = 1.0, b = 1.0, seed::Integer = 0) =
+  check(ccall((:mhd_set_forcing, libmhdgb), Cint,
+              (Ptr{Cvoid}, Cdouble, Cdouble, Cdouble, Cdouble, Culonglong), ts.handle, P, kf, σ, b, seed))
 
 end # module

@@ -79,3 +79,24 @@ def test_split_512_rhs_vs_plain(pkg, prec):
 def test_split_rejected_where_absent(pkg):
     with pytest.raises(pkg.MHDError):
         pkg.Problem(pkg.GPU(0), nx=64, nu=1e-3, eta=1e-3, dt=1e-3, precision="split_fp16")
+
+
+@pytest.mark.parametrize("prec", ["split_fp16", "split_bf16"])
+def test_split_512_twenty_steps_vs_plain(pkg, prec):
+    """The precision configuration: 512^3, nu = eta = 5e-4, dt = 2.5e-4, 20 RK4 steps; the split
+    form against the plain FP32 form from the same state (relative L2 of the final spectra)."""
+    n = 512
+    s0 = _state(pkg, n, 24)
+    kw = dict(nx=n, Lx=2 * math.pi, nu=5e-4, eta=5e-4, dt=2.5e-4)
+    out = {}
+    for form in ("fp32", prec):
+        with pkg.Problem(pkg.GPU(0), precision=form, **kw) as p:
+            p.set_sol(s0.T)
+            pkg.stepforward(p, 20)
+            out[form] = p.sol_c()
+            d = p.diagnostics()
+            assert d.nonfinite == 0
+    ref, got = out["fp32"], out[prec]
+    err = float(np.linalg.norm((got - ref).ravel()) / np.linalg.norm(ref.ravel()))
+    print(f"{prec} n=512 20 RK4 steps rel L2 vs plain FP32: {err:.3e}")
+    assert err < TOL[prec], err
