@@ -385,9 +385,9 @@ struct mhd_problem {
   // Stage epilogue: RHS from the 8 compact product planes (in rowbuf) and the stage state X.
   int epilogue(const float2* X, int op, float hf, float ca, float cb, BatchRef br, int stage) {
     int rc = launch(KC_HERM, [&] {
-      const long long total = (long long)cap * 6 * g.k2 * g.k2;
-      const long long blocks = (total + 255) / 256;
-      herm_kx0_kernel<<<(unsigned)(blocks < 4096 ? blocks : 4096), 256, 0, stream>>>(X, aux, g, FS(), ST(), FS(), br);
+      const int bxh = g.k2 <= 256 ? (g.k2 + 31) / 32 * 32 : 256;
+      const dim3 gh((g.k2 + bxh - 1) / bxh, g.k2, cap);
+      herm_kx0_kernel<<<gh, bxh, 0, stream>>>(X, aux, g, FS(), ST(), FS(), br);
     });
     if (rc) return rc;
     RkArgs a{};
