@@ -11,6 +11,7 @@
 // The state is kept only on the retained (2/3-rule) band, which is all the reference's dynamics
 // ever read: dealias! zeroes the alias band of the stage state before every RHS evaluation.
 #include <cuda_runtime.h>
+#include <cudaTypedefs.h>
 
 #include <sys/stat.h>
 
@@ -142,6 +143,36 @@ int report_error(int code, const std::string& msg) { return fail(code, msg); }
 
 namespace {
 
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no link to libcuda).
+PFN_cuTensorMapEncodeTiled_v12000 tmap_encoder() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = []() -> PFN_cuTensorMapEncodeTiled_v12000 {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess) {
+      cudaGetLastError();
+      return nullptr;
+    }
+    return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+  }();
+  return fn;
+}
+
+// 5-D tensor map over 8-byte elements (complex float pairs), no swizzle, zero fill out of range
+bool make_tmap(CUtensorMap* m, void* base, const cuuint64_t (&dims)[5], const cuuint64_t (&strides)[4],
+               const cuuint32_t (&box)[5]) {
+  auto enc = tmap_encoder();
+  if (!enc) return false;
+  const cuuint32_t es[5] = {1, 1, 1, 1, 1};
+  return enc(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 5, base, dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
+             CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) ==
+         CUDA_SUCCESS;
+}
+
+}  // namespace
+
+namespace {
+
 // ------------------------------------------------------------------------------------------
 // Autotuner results: the selected variant name of each tuned kernel class, keyed by device
 // (name and SM count) and grid size.  Kept for the process and, unless disabled, in a text file
@@ -263,6 +294,10 @@ struct mhd_problem {
   // slot is forced (the step then ends with step_tick_kernel)
   long long* dstep = nullptr;
   bool forcing = false;
+  // TMA sources of the column passes (used when a TMA-fed variant is selected) and the device
+  // word a timed-out tile wait is recorded in
+  TmaPass tm_zinv_sol, tm_zinv_xs, tm_yinv, tm_yfwd, tm_zfwd;
+  int* derr = nullptr;
   bool cfl = false;
   double cfl_coef = 0.3;
   int graph_version = 0;   // active slots, then the identity list (cap each), then counts
@@ -293,11 +328,11 @@ struct mhd_problem {
     for (auto e : pool) cudaEventDestroy(e);
     pool.clear();
     void* ptrs[] = {sol, xs, acc, aux, colbuf, rowbuf, ref, phys, diag_partial, diag_out, maxabs, dparams, dlist, dvmax, dtime,
-                    dstep};
+                    dstep, derr};
     for (void* q : ptrs) if (q) cudaFree(q);
     sol = xs = acc = aux = colbuf = rowbuf = ref = nullptr;
     phys = nullptr; diag_partial = nullptr; diag_out = nullptr; maxabs = nullptr; dparams = nullptr; dlist = nullptr;
-    dvmax = nullptr; dtime = nullptr; dstep = nullptr;
+    dvmax = nullptr; dtime = nullptr; dstep = nullptr; derr = nullptr;
     if (own_stream) cudaStreamDestroy(own_stream);
     own_stream = nullptr;
   }
@@ -363,11 +398,13 @@ struct mhd_problem {
   // compact fields (src + slot*sI, nf fields at stride FS) -> colbuf slots 0..nf-1
   int z_inverse(const float2* src, long long sI, int nf, BatchRef br) {
     ColArgs a{src, colbuf, FS(), (long long)g.kxp, (long long)g.k2 * g.kxp, (long long)g.kxp, SLK(), AZ(), sI, sz.colbuf};
-    return launch(KC_ZINV, [&] { ops->col(KC_ZINV, a, g, g.k2, nf, br, cap, stream); });
+    // the maps cover all six fields of a pool: only the right-hand side's call can use them
+    const TmaPass* tp = (nf == 6 && sI == ST()) ? (src == sol ? &tm_zinv_sol : src == xs ? &tm_zinv_xs : nullptr) : nullptr;
+    return launch(KC_ZINV, [&] { ops->col(KC_ZINV, a, g, g.k2, nf, br, cap, stream, tp); });
   }
   int y_inverse(int nf, BatchRef br) {
     ColArgs a{colbuf, rowbuf, (long long)g.kxp, AZ(), SLK(), (long long)g.kxp, BZ(), SLK(), sz.colbuf, sz.rowbuf};
-    return launch(KC_YINV, [&] { ops->col(KC_YINV, a, g, g.n, nf, br, cap, stream); });
+    return launch(KC_YINV, [&] { ops->col(KC_YINV, a, g, g.n, nf, br, cap, stream, &tm_yinv); });
   }
   int x_fused(BatchRef br, unsigned int* vmax) {
     // the six field rows of a physical row are contiguous (slot stride == kxp)
@@ -375,12 +412,12 @@ struct mhd_problem {
   }
   int y_forward(int nf, BatchRef br) {
     ColArgs a{rowbuf, colbuf, (long long)g.kxp, BZ(), SLK(), (long long)g.kxp, AZ(), SLK(), sz.rowbuf, sz.colbuf};
-    return launch(KC_YFWD, [&] { ops->col(KC_YFWD, a, g, g.n, nf, br, cap, stream); });
+    return launch(KC_YFWD, [&] { ops->col(KC_YFWD, a, g, g.n, nf, br, cap, stream, &tm_yfwd); });
   }
   // colbuf slots -> compact planes (nf fields/products) at dst + slot*dI, pruned output
   int z_forward(float2* dst, long long dI, int nf, BatchRef br) {
     ColArgs a{colbuf, dst, (long long)g.kxp, SLK(), AZ(), FS(), (long long)g.kxp, (long long)g.k2 * g.kxp, sz.colbuf, dI};
-    return launch(KC_ZFWD, [&] { ops->col(KC_ZFWD, a, g, g.k2, nf, br, cap, stream); });
+    return launch(KC_ZFWD, [&] { ops->col(KC_ZFWD, a, g, g.k2, nf, br, cap, stream, &tm_zfwd); });
   }
   // Stage epilogue: RHS from the 8 compact product planes (in rowbuf) and the stage state X.
   int epilogue(const float2* X, int op, float hf, float ca, float cb, BatchRef br, int stage) {
@@ -615,6 +652,43 @@ struct mhd_problem {
     return z_forward(dst, dI, 1, br);
   }
   bool valid_slot(int s) const { return s >= 0 && s < cap && used[s]; }
+  // Tensor maps of the column passes' sources (coordinates: kx first, then the dimensions
+  // named; rows = the transformed axis).  A map that cannot be encoded leaves the pass on the
+  // cp.async kernels.
+  void build_tma() {
+    const cuuint64_t E = sizeof(float2), kxp = g.kxp, k2 = g.k2, n = g.n, C = cap;
+    const cuuint32_t kp = g.kp, rb = g.n <= 256 ? g.n : 256;
+    auto set = [&](TmaPass& t, void* base, const cuuint64_t (&d)[5], const cuuint64_t (&st)[4],
+                   const cuuint32_t (&box)[5], TmaCoords tc) {
+      t.ok = make_tmap(&t.map, base, d, st, box);
+      t.tc = tc;
+      t.err = derr;
+    };
+    // z_inverse over sol / xs [slot][f][kz'][ky'][kx]: rows kz', outer ky'
+    const cuuint64_t dz[5] = {kxp, k2, k2, 6, C};
+    const cuuint64_t sz5[4] = {kxp * E, k2 * kxp * E, (cuuint64_t)sz.fs * E, (cuuint64_t)sz.state * E};
+    const cuuint32_t bz[5] = {16, 1, kp, 1, 1};
+    set(tm_zinv_sol, sol, dz, sz5, bz, TmaCoords{2, 1, 3, 4, (int)kp});
+    set(tm_zinv_xs, xs, dz, sz5, bz, TmaCoords{2, 1, 3, 4, (int)kp});
+    // colbuf [slot][z][ky'][8][kx] and rowbuf [slot][z][y][8][kx]
+    const cuuint64_t dc[5] = {kxp, 8, k2, n, C};
+    const cuuint64_t sc[4] = {kxp * E, 8 * kxp * E, k2 * 8 * kxp * E, (cuuint64_t)sz.colbuf * E};
+    const cuuint64_t dr[5] = {kxp, 8, n, n, C};
+    const cuuint64_t sr[4] = {kxp * E, 8 * kxp * E, n * 8 * kxp * E, (cuuint64_t)sz.rowbuf * E};
+    const cuuint32_t by_in[5] = {16, 1, kp, 1, 1};
+    const cuuint32_t by_out[5] = {16, 1, rb, 1, 1};
+    const cuuint32_t bz_out[5] = {16, 1, 1, rb, 1};
+    set(tm_yinv, colbuf, dc, sc, by_in, TmaCoords{2, 3, 1, 4, (int)kp});      // rows ky', outer z
+    set(tm_yfwd, rowbuf, dr, sr, by_out, TmaCoords{2, 3, 1, 4, (int)rb});     // rows y, outer z
+    set(tm_zfwd, colbuf, dc, sc, bz_out, TmaCoords{3, 2, 1, 4, (int)rb});     // rows z, outer ky'
+  }
+  // a TMA tile wait that timed out on the device (checked where the library synchronises)
+  int check_device_error() {
+    int e = 0;
+    MHD_CUDA(cudaMemcpy(&e, derr, sizeof(int), cudaMemcpyDeviceToHost));
+    if (e) return fail(MHD_ERR_CUDA, e == 2 ? "TMA buffer misaligned in shared memory" : "a TMA tile wait timed out on the device");
+    return MHD_OK;
+  }
   // Hydrodynamics runs the MHD kernels with B = 0: the epilogue sets the induction right-hand
   // side to zero, so B stays exactly zero, and the momentum right-hand side is HDcalcN!'s (the
   // x rows pair uz with bx in one transform, so they see FP32 roundoff in place of bx = 0; its
@@ -706,12 +780,15 @@ int create_class(const mhd_params* params, int cap, mhd_handle* out) {
   MHD_CUDA(cudaMalloc(&h->dvmax, 2 * c * sizeof(unsigned int)));
   MHD_CUDA(cudaMalloc(&h->dtime, c * sizeof(double)));
   MHD_CUDA(cudaMalloc(&h->dstep, c * sizeof(long long)));
+  MHD_CUDA(cudaMalloc(&h->derr, sizeof(int)));
+  MHD_CUDA(cudaMemsetAsync(h->derr, 0, sizeof(int), h->stream));
   MHD_CUDA(cudaMemsetAsync(h->dstep, 0, c * sizeof(long long), h->stream));
   MHD_CUDA(cudaMemsetAsync(h->dvmax, 0, 2 * c * sizeof(unsigned int), h->stream));
   MHD_CUDA(cudaMemsetAsync(h->dtime, 0, c * sizeof(double), h->stream));
   MHD_CUDA(cudaMemsetAsync(h->sol, 0, c * s.state * sizeof(float2), h->stream));
   MHD_CUDA(cudaMemsetAsync(h->xs, 0, c * s.state * sizeof(float2), h->stream));
   MHD_CUDA(cudaMemsetAsync(h->acc, 0, c * s.state * sizeof(float2), h->stream));
+  h->build_tma();
   h->hparams.assign(cap, SlotParams{0.f, 0.f, 0.f, 0.f});
   h->used.assign(cap, 0);
   h->t.assign(cap, 0.0);
@@ -1104,7 +1181,7 @@ int mhd_synchronize(mhd_handle h) {
   int rc = check_handle(h);
   if (rc) return rc;
   MHD_CUDA(cudaStreamSynchronize(h->stream));
-  return MHD_OK;
+  return h->check_device_error();
 }
 
 int mhd_set_stream(mhd_handle h, void* stream) {

@@ -28,6 +28,16 @@ int report_error(int code, const std::string& msg);
 using XFn = void (*)(float2*, Geom, long long, long long, long long, BatchRef, const float2*, const float2*,
                      unsigned int*);
 using ColFn = void (*)(ColArgs, Geom, ColWork, BatchRef, const float2*);
+using TmaColFn = void (*)(ColArgs, Geom, ColWork, BatchRef, const float2*, CUtensorMap, TmaCoords, int*);
+
+// A TMA source description for one column pass: the tensor map over the pass's source array,
+// its coordinate roles, and the device word a timed-out tile wait is recorded in.
+struct TmaPass {
+  CUtensorMap map;
+  TmaCoords tc;
+  int* err = nullptr;
+  bool ok = false;
+};
 using C2RFn = void (*)(const float2*, float*, Geom, long long, float, const float2*);
 using R2CFn = void (*)(const float*, float2*, Geom, long long, const float2*);
 
@@ -50,6 +60,7 @@ struct XVariant {
 struct ColVariant {
   std::string name;
   ColFn inv = nullptr, fwd = nullptr;
+  TmaColFn inv_tma = nullptr, fwd_tma = nullptr;  // set for TMA-fed variants (inv / fwd unused then)
   int threads = 0, tx = 0;
   size_t tw = 0;
   size_t smem = 0;
@@ -62,7 +73,9 @@ class OpsBase {
   int setup(const Geom& g);
   // cap: upper bound of the active instances (the grid covers cap instances; the kernels read
   // the actual count from the BatchRef)
-  void col(int cls, const ColArgs& a, const Geom& g, int outer, int nf, BatchRef br, int cap, cudaStream_t s) const;
+  // tp: the TMA source of this call (nullptr or !ok: a TMA-fed selection falls back to variant 0)
+  void col(int cls, const ColArgs& a, const Geom& g, int outer, int nf, BatchRef br, int cap, cudaStream_t s,
+           const TmaPass* tp = nullptr) const;
   void x_fused(float2* pool, const Geom& g, long long rowstride, long long slot, long long istride, BatchRef br,
                int cap, unsigned int* vmax, cudaStream_t s) const;
   void x_c2r(const float2* src, float* dst, const Geom& g, long long srow, float scale, cudaStream_t s) const;
@@ -181,6 +194,22 @@ class Ops : public OpsBase {
     c.threads = TX * C::G;
     c.tx = TX;
     c.smem = sizeof(float2) * NBUF * (size_t)N * TX;
+    c.tw = twiddles<C>();
+    cv.push_back(c);
+  }
+
+  // TMA-fed column passes (16 kx columns: 128-byte box rows keep every box destination aligned)
+  template <class C, int MINB, int NBUF>
+  void add_col_tma() {
+    constexpr int TX = 16;
+    ColVariant c;
+    c.name = "coltma:" + plan_name<C>() + "/tx" + std::to_string(TX) + "/b" + std::to_string(MINB) + "/q" +
+             std::to_string(NBUF);
+    c.inv_tma = col_pass_tma_kernel<C, TX, +1, true, false, MINB, NBUF>;
+    c.fwd_tma = col_pass_tma_kernel<C, TX, -1, false, true, MINB, NBUF>;
+    c.threads = TX * C::G;
+    c.tx = TX;
+    c.smem = sizeof(float2) * NBUF * (size_t)N * TX + NBUF * sizeof(unsigned long long) + 16;
     c.tw = twiddles<C>();
     cv.push_back(c);
   }

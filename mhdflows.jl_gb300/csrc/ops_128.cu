@@ -8,6 +8,7 @@ OpsBase* make_ops_128() {
   o->add_col<Plan<128, 8, 16, 8>, 16, 2>();
   o->add_col<Plan<128, 8, 16, 8>, 8, 4>();
   o->add_col<Plan<128, 16, 8, 4, 4>, 8, 3>();
+  o->add_col_tma<Plan<128, 8, 16, 8>, 2, 2>();
   o->add_x<Plan<128, 16, 8, 4, 4>, 4, 1, 1, 4>();
   o->add_x<Plan<128, 16, 8, 4, 4>, 4, 3, 1, 3>();
   o->add_x<Plan<128, 8, 16, 8>, 4, 1, 1, 2>();

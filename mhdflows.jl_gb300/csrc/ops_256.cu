@@ -14,6 +14,8 @@ OpsBase* make_ops_256() {
   o->add_col<Plan<256, 16, 16, 16>, 16, 2, 3>();
   o->add_col<Plan<256, 16, 16, 16>, 8, 4, 4>();
   o->add_col<Plan<256, 16, 16, 16>, 8, 6, 3>();
+  o->add_col_tma<Plan<256, 16, 16, 16>, 3, 2>();
+  o->add_col_tma<Plan<256, 16, 16, 16>, 2, 3>();
   o->add_x<Plan<256, 32, 8, 8, 4>, 4, 1, 1, 4>();
   o->add_x<Plan<256, 32, 8, 8, 4>, 4, 3, 1, 3>();
   o->add_x<Plan<256, 32, 8, 8, 4>, 4, 3, 2, 3>();

@@ -62,11 +62,14 @@ int OpsBase::setup(const Geom& g) {
   for (auto& c : cv) {
     c.ctas_inv = c.ctas_fwd = 0;
     if ((int)c.smem > smem_max) continue;
-    if ((rc = set_smem((const void*)c.inv, c.smem))) return rc;
-    if ((rc = set_smem((const void*)c.fwd, c.smem))) return rc;
-    if ((rc = resident_ctas((const void*)c.inv, c.threads, c.smem, sms, &c.ctas_inv))) return rc;
-    if ((rc = resident_ctas((const void*)c.fwd, c.threads, c.smem, sms, &c.ctas_fwd))) return rc;
+    const void* fi = c.inv_tma ? (const void*)c.inv_tma : (const void*)c.inv;
+    const void* ff = c.fwd_tma ? (const void*)c.fwd_tma : (const void*)c.fwd;
+    if ((rc = set_smem(fi, c.smem))) return rc;
+    if ((rc = set_smem(ff, c.smem))) return rc;
+    if ((rc = resident_ctas(fi, c.threads, c.smem, sms, &c.ctas_inv))) return rc;
+    if ((rc = resident_ctas(ff, c.threads, c.smem, sms, &c.ctas_fwd))) return rc;
   }
+  if (!cv.empty() && cv[0].inv_tma) return report_error(MHD_ERR_INVALID, "the default column variant must not be TMA-fed");
   if ((rc = set_smem((const void*)c2r, row_smem))) return rc;
   if ((rc = set_smem((const void*)r2c, row_smem))) return rc;
   // the default of each class is its first variant that fits on this device
@@ -113,9 +116,19 @@ int OpsBase::select_by_name(int cls, const std::string& name) {
 }
 
 void OpsBase::col(int cls, const ColArgs& a, const Geom& g, int outer, int nf, BatchRef br, int cap,
-                  cudaStream_t s) const {
-  const ColVariant& c = cv[sel[cls]];
+                  cudaStream_t s, const TmaPass* tp) const {
+  const bool tma_sel = cv[sel[cls]].inv_tma != nullptr;
+  const ColVariant& c = (tma_sel && !(tp && tp->ok)) ? cv[0] : cv[sel[cls]];
   const bool inv = is_inv(cls);
+  if (c.inv_tma) {
+    const ColWork w{(g.kx + c.tx - 1) / c.tx, outer, nf, inv ? g.k2 : n};
+    const long long total = (long long)cap * w.tiles_x * w.outer * w.nf;
+    const int ctas = inv ? c.ctas_inv : c.ctas_fwd;
+    const int grid = (int)(total < ctas ? total : ctas);
+    const TmaColFn f = inv ? c.inv_tma : c.fwd_tma;
+    f<<<grid, c.threads, c.smem, s>>>(a, g, w, br, tw_dev + c.tw, tp->map, tp->tc, tp->err);
+    return;
+  }
   const ColWork w{(g.kx + c.tx - 1) / c.tx, outer, nf, inv ? g.k2 : n};
   const long long total = (long long)cap * w.tiles_x * w.outer * w.nf;
   const int ctas = inv ? c.ctas_inv : c.ctas_fwd;

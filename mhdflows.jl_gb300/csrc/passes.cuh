@@ -7,6 +7,8 @@
 // 8 slots per (z, ky') and (z, y): fields 0..5 on the way in, products 0..7 on the way out.
 // A kept index j maps to frequency index j (j < Kp) or j + n - K2 (negative wavenumbers).
 #pragma once
+#include <cuda.h>
+
 #include "fft_core.cuh"
 
 namespace mhdgb {
@@ -237,6 +239,199 @@ __global__ void __launch_bounds__(TX * P0::G, MINB)
     __syncthreads();  // all exchange reads of cur done before it is refilled
   }
   cp_async_wait<0>();
+}
+
+// ------------------------------------------------------------------------------------------
+// TMA-fed column pass: the same transform as col_pass_kernel, with each tile brought into
+// shared memory by one thread's cp.async.bulk.tensor copies (a 5-D tensor map over the pass's
+// source array) completing on an mbarrier per buffer.  Pruned inputs take two boxes (the kept
+// non-negative rows, then the kept negative rows at their frequency position); full inputs one
+// box, or two of 256 rows.  Every wait is bounded (about one second of %globaltimer): on a
+// timeout the kernel records the failure in *err, stops taking tiles, waits (bounded again) for
+// the copies it issued and returns.
+// ------------------------------------------------------------------------------------------
+struct TmaCoords {
+  int rowdim, odim, fdim, idim;  // tensor-map dimensions of the transformed axis, outer index, field, slot
+  int rb;                        // rows per box
+};
+
+__device__ __forceinline__ unsigned int smem_u32(const void* p) { return (unsigned int)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ unsigned long long global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+// true when the barrier's phase `parity` completed within about a second
+__device__ __forceinline__ bool mbar_wait(unsigned int bar, unsigned int parity) {
+  const unsigned long long t0 = global_ns();
+  while (true) {
+    unsigned int done;
+    asm volatile(
+        "{\n .reg .pred P;\n mbarrier.try_wait.parity.shared::cta.b64 P, [%1], %2;\n selp.u32 %0, 1, 0, P;\n}\n"
+        : "=r"(done)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    if (done) return true;
+    if (global_ns() - t0 > 1000000000ull) return false;
+  }
+}
+__device__ __forceinline__ void tma_load5(unsigned int dst, const void* map, int c0, int c1, int c2, int c3, int c4,
+                                          unsigned int bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.5d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5, %6}], "
+      "[%7];\n" ::"r"(dst),
+      "l"(map), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(c4), "r"(bar)
+      : "memory");
+}
+
+template <class P0, int TX, int DIR, bool PIN, bool POUT, int MINB, int NBUF>
+__global__ void __launch_bounds__(TX * P0::G, MINB)
+    col_pass_tma_kernel(ColArgs a, Geom geo, ColWork w, BatchRef br, const float2* __restrict__ tw,
+                        const __grid_constant__ CUtensorMap map, TmaCoords tc, int* err) {
+  static_assert(NBUF >= 2 && NBUF <= 4, "two to four tile buffers");
+  using P = Unpadded<P0>;
+  // dynamic shared memory only (its base is then 1024-byte aligned): NBUF tile buffers, then the
+  // NBUF mbarriers and the abort flag
+  extern __shared__ __align__(128) float2 smem[];
+  constexpr int G = P::G, V = P::V, N = P::N, NT = TX * P0::G;
+  unsigned long long* bars = reinterpret_cast<unsigned long long*>(smem + NBUF * N * TX);
+  volatile int& abort_flag = *reinterpret_cast<volatile int*>(bars + NBUF);
+  constexpr int KP = kept_kx_of(N), KN = kept_kn_of(N);
+  const int tx = threadIdx.x % TX, g = threadIdx.x / TX;
+  const int per = w.tiles_x * w.outer * w.nf;
+  const int total = *br.count * per;
+  const int dR = (int)a.dR;
+  const int shift = (N - KP - KN) * dR;
+  const unsigned int tx_bytes = PIN ? 2u * tc.rb * TX * 8u : (unsigned int)N * TX * 8u;
+  if (threadIdx.x == 0) {
+    abort_flag = (smem_u32(smem) & 127u) != 0;  // TMA destinations must be 128-byte aligned
+    if (abort_flag) atomicExch(err, 2);
+    for (int b = 0; b < NBUF; ++b)
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&bars[b])) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  }
+  __syncthreads();
+  if (abort_flag) return;
+  struct Cur { int tx, o, f, inst; };
+  auto decompose = [&](int t) {
+    Cur c;
+    c.tx = t % w.tiles_x;
+    int r = t / w.tiles_x;
+    c.o = r % w.outer;
+    r /= w.outer;
+    c.f = r % w.nf;
+    c.inst = r / w.nf;
+    return c;
+  };
+  const Cur gstep = decompose(gridDim.x);
+  auto advance = [&](Cur c) {
+    int carry;
+    c.tx += gstep.tx; carry = c.tx >= w.tiles_x; if (carry) c.tx -= w.tiles_x;
+    c.o += gstep.o + carry; carry = c.o >= w.outer; if (carry) c.o -= w.outer;
+    c.f += gstep.f + carry; carry = c.f >= w.nf; if (carry) c.f -= w.nf;
+    c.inst += gstep.inst + carry;
+    return c;
+  };
+  // tile c into buffer b: zero the alias rows the transform reads (all threads), then thread 0
+  // arms the barrier and issues the box copies
+  auto issue = [&](const Cur& c, int b) {
+    float2* buf = smem + b * (N * TX);
+    if (PIN) {
+      constexpr int CH = TX / 2;
+      float4* zb = reinterpret_cast<float4*>(buf + KP * TX);
+      constexpr int nz = (N - KP - KN) * CH;
+      for (int q = threadIdx.x; q < nz; q += NT) {
+        const int r = KP + q / CH;
+        const int gs = r / G * G;
+        if (gs < KP || gs + G - 1 >= N - KN) zb[q] = make_float4(0.f, 0.f, 0.f, 0.f);
+      }
+    }
+    if (threadIdx.x == 0) {
+      const unsigned int bar = smem_u32(&bars[b]);
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // earlier generic reads of buf
+      asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(tx_bytes) : "memory");
+      int cc[5] = {c.tx * TX, 0, 0, 0, 0};
+      cc[tc.odim] = c.o;
+      cc[tc.fdim] = c.f;
+      cc[tc.idim] = br.list[c.inst];
+      if (PIN) {
+        cc[tc.rowdim] = 0;
+        tma_load5(smem_u32(buf), &map, cc[0], cc[1], cc[2], cc[3], cc[4], bar);
+        cc[tc.rowdim] = KP;
+        tma_load5(smem_u32(buf + (N - KN) * TX), &map, cc[0], cc[1], cc[2], cc[3], cc[4], bar);
+      } else {
+        for (int r0 = 0; r0 < N; r0 += tc.rb) {
+          cc[tc.rowdim] = r0;
+          tma_load5(smem_u32(buf + r0 * TX), &map, cc[0], cc[1], cc[2], cc[3], cc[4], bar);
+        }
+      }
+    }
+  };
+  int t = blockIdx.x;
+  Cur cur_t = decompose(t);
+  int tp = t;
+  Cur pre_t = cur_t;
+  int issued = 0;  // tiles issued by this CTA (tile k uses buffer k % NBUF, phase (k / NBUF) & 1)
+#pragma unroll
+  for (int j = 0; j < NBUF - 1; ++j) {
+    if (tp < total) { issue(pre_t, j); ++issued; }
+    tp += gridDim.x;
+    pre_t = advance(pre_t);
+  }
+  int it = 0;
+  for (; t < total; t += gridDim.x, ++it) {
+    if (tp < total) { issue(pre_t, (it + NBUF - 1) % NBUF); ++issued; }
+    tp += gridDim.x;
+    pre_t = advance(pre_t);
+    if (!mbar_wait(smem_u32(&bars[it % NBUF]), (unsigned int)((it / NBUF) & 1))) {
+      atomicExch(err, 1);
+      abort_flag = 1;
+    }
+    __syncthreads();
+    if (abort_flag) break;
+    float2* cur = smem + (it % NBUF) * (N * TX);
+    const int inst = cur_t.inst, f = cur_t.f, o = cur_t.o;
+    const int kxg = cur_t.tx * TX + tx;
+    cur_t = advance(cur_t);
+    float2 v[1][V];
+#pragma unroll
+    for (int d = 0; d < P::DI; ++d)
+#pragma unroll
+      for (int n0 = 0; n0 < P::R0; ++n0) {
+        const int rmin = G * d + P::LI * n0;
+        if (PIN && rmin >= KP && rmin + G - 1 < N - KN)
+          v[0][d * P::R0 + n0] = make_float2(0.f, 0.f);
+        else
+          v[0][d * P::R0 + n0] = cur[(g + rmin) * TX + tx];
+      }
+    __syncthreads();  // cur is now free: reuse it as the exchange buffer
+    fft_run<P, DIR, 1, 0, TX>(v, cur, tx, g, tw, BlockSync{});
+    if (kxg < geo.kx) {
+      float2* dst = a.dst + br.list[inst] * a.dI + f * a.dF + (long long)o * a.dO + kxg;
+#pragma unroll
+      for (int d = 0; d < P::DF; ++d) {
+        const int base = (g + G * d) * dR;
+#pragma unroll
+        for (int e = 0; e < P::RF; ++e) {
+          const int kmin = G * d + P::LF * e;
+          if (POUT && kmin >= KP && kmin + G - 1 < N - KN) continue;
+          const int k = g + kmin;
+          const int off = base + e * (P::LF * dR);
+          if (!POUT || k < KP) {
+            dst[off] = v[0][d * P::RF + e];
+          } else if (k >= N - KN) {
+            dst[off - shift] = v[0][d * P::RF + e];
+          }
+        }
+      }
+    }
+    __syncthreads();  // all exchange reads of cur done before it is refilled
+  }
+  // after an abort: let the copies this CTA issued and did not consume land before exiting
+  if (abort_flag && threadIdx.x == 0) {
+    for (int k = it; k < issued; ++k) (void)mbar_wait(smem_u32(&bars[k % NBUF]), (unsigned int)((k / NBUF) & 1));
+  }
 }
 
 // ------------------------------------------------------------------------------------------
