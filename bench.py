@@ -269,7 +269,11 @@ def run_gpu(args, rank, world, local, dist: Dist):
     n = args.n
     s0 = initial_state(n)
     prob = pkg.Problem(pkg.GPU(local), nx=n, Lx=2 * math.pi, nu=NU, eta=ETA, dt=DT, stepper="RK4",
-                       precision=args.precision)
+                       precision=args.precision, B_field=not args.hydro)
+    if args.hydro:
+        s0 = s0[:3]
+    if args.forcing:  # A99 forcing with SetUpFk!'s defaults (kf = 2, sigma = 1, b = 1), small P
+        pkg.SetUpFk(prob, kf=2.0, P=1e-6, sigma=1.0, b=1.0, seed=7)
     h = prob.handle
     chk = pkg._lib.check
     prob.set_sol(s0.T)
@@ -410,6 +414,8 @@ def main():
     ap.add_argument("--grid", dest="n", type=int, default=256, help="grid points per axis of the step workload")
     ap.add_argument("--precision", default="fp32", choices=["fp32", "split_fp16", "split_bf16"],
                     help="x-row transforms in FP32 (plain form) or as split 16-bit tensor-core DFTs")
+    ap.add_argument("--hydro", action="store_true", help="hydrodynamic problem (B_field = false)")
+    ap.add_argument("--forcing", action="store_true", help="A99 random forcing on (SetUpFk!)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-secondary", dest="secondary", action="store_false")
     ap.add_argument("--workload", default="step", choices=["step", "ensemble", "serve"])
@@ -419,7 +425,7 @@ def main():
     args.warmup = max(args.warmup, 3)
     rank, world, local = dist_env()
     config = {"workload": f"MHD RK4 step, {args.n}^3 FP32, nu=eta=1e-3, dt=5e-4, seeded k^4 exp(-2(k/4)^2) u and B",
-              "n": args.n, "scheme": "RK4", "precision": args.precision,
+              "n": args.n, "scheme": "RK4", "precision": args.precision, "hydro": args.hydro, "forcing": args.forcing,
               "l2": "inputs larger than L2 (step working set > 1 GB)",
               "parallelism": "replicas" if args.gpus > 1 else "single"}
 

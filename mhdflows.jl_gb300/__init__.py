@@ -643,7 +643,9 @@ def SetUpFk(prob, kf: float = 2.0, P: float = 1.0, sigma: float = 1.0, b: float 
     """SetUpFk!(prob; kf, P, σ, b) (src/pgen/A99ForceDriving_GPU.jl:24-48) plus the A99ForceDriving!
     hook: the velocity right-hand side of every stage gets the A99 random forcing.  P = 0 turns
     it off.  ``prob`` is a Problem (slot 0) or a Batch (``slot``).  Random numbers come from a
-    counter-based generator keyed by ``seed`` (the reference draws them with the device rand())."""
+    counter-based generator keyed by ``seed`` (the reference draws them with the device rand()).
+    A hydrodynamic problem stays unforced, as in the reference: HDcalcN! (src/pgen.jl:176-182)
+    adds the forcing before HDcalcN_advection!, which zeroes the velocity right-hand side."""
     lib = _lib.load()
     _lib.check(lib.mhd_slot_set_forcing(prob.handle, int(slot), float(P), float(kf), float(sigma), float(b),
                                         int(seed) & 0xFFFFFFFFFFFFFFFF))

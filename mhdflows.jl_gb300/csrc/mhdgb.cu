@@ -450,8 +450,10 @@ struct mhd_problem {
     a.pscale = (float)(1.0 / (n3 * n3));
     const int bx = g.kx <= 256 ? (g.kx + 31) / 32 * 32 : 256;
     const dim3 grid((g.kx + bx - 1) / bx, g.k2, g.k2 * cap);
+    // HDcalcN! (src/pgen.jl:176-182) calls addforcing! before HDcalcN_advection!, whose
+    // UᵢUpdate! starts by zeroing the velocity right-hand side: a hydrodynamic problem is unforced
     return launch(KC_RKEPI, [&] {
-      if (forcing) launch_epilogue<true>(op, grid, bx, a, br);
+      if (forcing && !p.hydro_only) launch_epilogue<true>(op, grid, bx, a, br);
       else launch_epilogue<false>(op, grid, bx, a, br);
     });
   }

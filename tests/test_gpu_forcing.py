@@ -89,3 +89,21 @@ def test_forcing_reproducible_by_seed(pkg, mo):
         prob.set_sol(s.T)
         pkg.stepforward(prob, 3)
         assert np.array_equal(prob.sol_c(), d)
+
+
+def test_hydrodynamic_problem_stays_unforced(pkg, mo):
+    """HDcalcN! (src/pgen.jl:176-182) adds the forcing before HDcalcN_advection!, whose UᵢUpdate!
+    zeroes the velocity right-hand side (src/Solver/HDSolver.jl:55): SetUpFk! leaves an HD run
+    unchanged, bit for bit."""
+    n = 32
+    s = mo.random_spectrum_state(mo.Grid(n), seed=44).astype(np.complex64)[:3]
+
+    def run(forced):
+        with pkg.Problem(pkg.GPU(0), nx=n, nu=1e-3, dt=1e-3, B_field=False) as prob:
+            prob.set_sol(s.T)
+            if forced:
+                pkg.SetUpFk(prob, kf=KF, P=P, sigma=SIGMA, b=B, seed=SEED)
+            pkg.stepforward(prob, 2)
+            return prob.sol_c()
+
+    assert np.array_equal(run(True), run(False))
