@@ -269,9 +269,13 @@ def run_gpu(args, rank, world, local, dist: Dist):
     n = args.n
     s0 = initial_state(n)
     prob = pkg.Problem(pkg.GPU(local), nx=n, Lx=2 * math.pi, nu=NU, eta=ETA, dt=DT, stepper="RK4",
-                       precision=args.precision, B_field=not args.hydro)
+                       precision=args.precision, B_field=not args.hydro, VP_method=args.vp)
     if args.hydro:
         s0 = s0[:3]
+    if args.vp:  # a smoothed ball obstacle of radius L/5 at the box centre, walls at rest
+        x = (np.arange(n, dtype=np.float32) - n / 2) * (2 * math.pi / n)
+        r = np.sqrt(x[:, None, None] ** 2 + x[None, :, None] ** 2 + x[None, None, :] ** 2)
+        prob.set_vp((0.5 * (1 - np.tanh((r - 2 * math.pi / 5) / (4 * 2 * math.pi / n)))).astype(np.float32))
     if args.forcing:  # A99 forcing with SetUpFk!'s defaults (kf = 2, sigma = 1, b = 1), small P
         pkg.SetUpFk(prob, kf=2.0, P=1e-6, sigma=1.0, b=1.0, seed=7)
     h = prob.handle
@@ -416,6 +420,7 @@ def main():
                     help="x-row transforms in FP32 (plain form) or as split 16-bit tensor-core DFTs")
     ap.add_argument("--hydro", action="store_true", help="hydrodynamic problem (B_field = false)")
     ap.add_argument("--forcing", action="store_true", help="A99 random forcing on (SetUpFk!)")
+    ap.add_argument("--vp", action="store_true", help="volume penalisation on (VP_method, a ball obstacle)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-secondary", dest="secondary", action="store_false")
     ap.add_argument("--workload", default="step", choices=["step", "ensemble", "serve"])
@@ -425,7 +430,7 @@ def main():
     args.warmup = max(args.warmup, 3)
     rank, world, local = dist_env()
     config = {"workload": f"MHD RK4 step, {args.n}^3 FP32, nu=eta=1e-3, dt=5e-4, seeded k^4 exp(-2(k/4)^2) u and B",
-              "n": args.n, "scheme": "RK4", "precision": args.precision, "hydro": args.hydro, "forcing": args.forcing,
+              "n": args.n, "scheme": "RK4", "precision": args.precision, "hydro": args.hydro, "forcing": args.forcing, "vp": args.vp,
               "l2": "inputs larger than L2 (step working set > 1 GB)",
               "parallelism": "replicas" if args.gpus > 1 else "single"}
 

@@ -67,6 +67,7 @@ typedef struct mhd_params {
   int hydro_only; /* 0: MHD (B_field = true, 6 fields); 1: hydrodynamics (B_field = false,
                      HDcalcN! of src/pgen.jl:176-182: 3 fields ux, uy, uz; the state layout of
                      set/get_state is then (nkr, n, n, 3) and field indices are 0..2) */
+  int vp;         /* 1: volume penalisation (VP_method = true, see mhd_set_vp); 0: off */
 } mhd_params;
 
 typedef struct mhd_problem* mhd_handle;
@@ -194,6 +195,29 @@ int mhd_set_forcing(mhd_handle h, double P, double kf, double sigma, double b, u
 int mhd_slot_set_forcing(mhd_handle h, int slot, double P, double kf, double sigma, double b,
                          unsigned long long seed);
 int mhd_get_forcing(mhd_handle h, int slot, double* A, double* kf_used);
+
+/* Volume penalisation, Problem(...; VP_method = true) (src/pgen.jl:29,111-124): with
+ * mhd_params.vp = 1 every right-hand side gains VP_UᵢUpdate! and, for MHD, VP_BᵢUpdate!
+ * (src/Solver/VPSolver.jl:20-58, called from src/Solver/MHDSolver.jl:85-88,160-163 and
+ * src/Solver/HDSolver.jl:76-79): N_a += -(δ_aj - k_a k_j / k^2) rfft(chi / eta (u_j - U0_j)) and
+ * the same with B and B0, eta = 13 dt / 7.  The handle holds per slot the mask chi and the wall
+ * fields, all zero at creation.  mhd_set_vp / mhd_slot_set_vp copy them in, in place of writing
+ * params.χ, params.U₀x..U₀z, params.B₀x..B₀z: chi is n^3 floats, U0 and B0 are 3 n^3 floats
+ * (x, y, z components one after another), all in the reference's (nx, ny, nz) column-major
+ * order; NULL sets zero (chi = NULL turns the penalty off for the slot; B0 is unused by HD).
+ * mhd_div_correct runs DivVCorrection! (fields & MHD_DIV_U) and DivBCorrection! (fields &
+ * MHD_DIV_B) (src/Solver/VPSolver.jl:60-138) on the state: u and B lose their gradient part.
+ * mhd_set_div_correction(h, 1) makes every step of every active slot end with both, as
+ * TimeIntegrator! does with VP (src/integrator.jl:84-88,118-122); with the on-device CFL the next
+ * dt then comes from the corrected fields, as getCFL! reads the corrected vars there.
+ * VP needs precision MHD_PREC_FP32. */
+#define MHD_DIV_U 1
+#define MHD_DIV_B 2
+int mhd_set_vp(mhd_handle h, const float* chi, const float* U0, const float* B0);
+int mhd_slot_set_vp(mhd_handle h, int slot, const float* chi, const float* U0, const float* B0);
+int mhd_div_correct(mhd_handle h, int fields);
+int mhd_slot_div_correct(mhd_handle h, int slot, int fields);
+int mhd_set_div_correction(mhd_handle h, int on);
 
 /* Autotuner (no counterpart in the reference, whose FFTs are FFTW / cuFFT plans made with
  * MEASURE).  Each FFT pass class (z_inverse, y_inverse, x_fused, y_forward, z_forward: classes

@@ -6,6 +6,7 @@ Host-side mirror of the reference's interface for this path, over the C ABI in
     prob = Problem(GPU(); nx=256, Lx=2pi, nu=1e-3, eta=1e-3, B_field=True, stepper="RK4",
                    T=np.float32, dt=5e-4)                 # src/pgen.jl:64-127
     SetUpProblemIC(prob, ux=..., uy=..., uz=..., bx=..., by=..., bz=...)   # src/utils/IC.jl:41-109
+    prob.set_vp(chi, U0=(...), B0=(...))   # with VP_method=True: params.χ, U₀, B₀ (VPSolver.jl)
     stepforward(prob)                                      # stepforward!(prob.sol, prob.clock, ...)
     updatevars(prob)                                       # vars <- irfft(sol)
     KE, ME = ProbDiagnostic(prob)                          # src/utils/UserInterface.jl:65-86
@@ -31,7 +32,7 @@ __all__ = [
     "Diagnostics", "TimeIntegrator", "MHDError", "kept_modes", "supported_sizes", "footprint_bytes",
     "Batch", "Ensemble", "slot_bytes", "Diagnostic", "autotune", "variants", "select_variant",
     "TUNED_CLASSES", "PRECISIONS", "savefile", "Restart", "readMHDFlows", "checkpoint_path", "FIELDS",
-    "SetUpFk", "forcing_amplitude",
+    "SetUpFk", "forcing_amplitude", "DivVCorrection", "DivBCorrection",
 ]
 
 FIELDS = ("ux", "uy", "uz", "bx", "by", "bz")
@@ -77,8 +78,33 @@ def _precision(precision) -> int:
     return PRECISIONS[key]
 
 
-def _params(n, L, nu, eta, nnu, neta, dt, scheme, device, precision=0, hydro_only=False):
-    return _lib.MhdParams(n, L, nu, eta, nnu, neta, dt, scheme, _precision(precision), device, int(bool(hydro_only)))
+def _params(n, L, nu, eta, nnu, neta, dt, scheme, device, precision=0, hydro_only=False, vp=False):
+    return _lib.MhdParams(n, L, nu, eta, nnu, neta, dt, scheme, _precision(precision), device, int(bool(hydro_only)),
+                          int(bool(vp)))
+
+
+def _vp_arrays(n, chi, U0, B0):
+    """Host buffers of set_vp: chi and the wall triples as float32 in the reference's (nx, ny, nz)
+    column-major order (arrays indexed [x, y, z], like prob.vars.ux)."""
+    def field(a, what):
+        a = np.asarray(a, dtype=np.float32)
+        if a.shape != (n, n, n):
+            raise MHDError(_lib.MHD_ERR_INVALID, f"{what} must be an (n, n, n) array indexed [x, y, z]")
+        return np.asfortranarray(a)
+
+    def triple(t, what):
+        if t is None:
+            return None
+        if len(t) != 3:
+            raise MHDError(_lib.MHD_ERR_INVALID, f"{what} must be three (n, n, n) arrays (x, y, z components)")
+        return np.concatenate([field(c, what).ravel(order="F") for c in t])
+
+    c = None if chi is None else field(chi, "chi")
+    return c, triple(U0, "U0"), triple(B0, "B0")
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data
 
 
 def footprint_bytes(n: int, L: float = 2 * math.pi, stepper: str = "RK4") -> int:
@@ -161,10 +187,11 @@ class Grid:
 
 
 class Problem:
-    """``Problem(GPU(); nx, Lx, ν/nu, η/eta, nν, nη, B_field=True, stepper, T=Float32, dt)``.
+    """``Problem(GPU(); nx, Lx, ν/nu, η/eta, nν, nη, B_field=True, VP_method=False, stepper, T=Float32, dt)``.
 
-    Only the MHD branch of src/pgen.jl:64-127 lives on this path: ``B_field`` must be true and
-    EMHD, compressibility, shear, VP, dye and forcing must be off.
+    The MHD and HD branches of src/pgen.jl:64-127, with or without volume penalisation
+    (``VP_method``; the mask and walls are set with ``set_vp``).  EMHD, compressibility, shear
+    and the dye module are not on this path; forcing is set with ``SetUpFk``.
     """
 
     def __init__(self, dev=None, *, nx=64, ny=None, nz=None, Lx=2 * math.pi, Ly=None, Lz=None,
@@ -181,8 +208,8 @@ class Problem:
             dev = GPU()
         if isinstance(dev, CPU) or dev is CPU:
             raise MHDError(_lib.MHD_ERR_INVALID, "this library runs on the GPU only: use Problem(GPU(); ...)")
-        if EMHD or Compressibility or Shear or VP_method or Dye_Module or calcF is not None:
-            raise MHDError(_lib.MHD_ERR_INVALID, "EMHD, compressibility, shear, VP, dye and forcing are not on this path")
+        if EMHD or Compressibility or Shear or Dye_Module or calcF is not None:
+            raise MHDError(_lib.MHD_ERR_INVALID, "EMHD, compressibility, shear, dye and calcF hooks are not on this path")
         if (ny not in (None, nx)) or (nz not in (None, nx)) or (Ly not in (None, Lx)) or (Lz not in (None, Lx)):
             raise MHDError(_lib.MHD_ERR_INVALID, "only cubic boxes (nx = ny = nz, Lx = Ly = Lz) are provided")
         if np.dtype(T) != np.float32:
@@ -198,11 +225,12 @@ class Problem:
         self.stepper = str(stepper).upper()
         self.precision = _precision(precision)
         self.B_field = bool(B_field)
+        self.VP = bool(VP_method)
         self.nfields = 6 if self.B_field else 3
         if not self.B_field:  # HDcalcN! (src/pgen.jl:176-182): the three velocity fields only
             eta, neta = 0.0, 0
         p = _params(self.n, self.L, float(nu or 0.0), float(eta or 0.0), int(nnu), int(neta), float(dt),
-                    scheme, dev.device, self.precision, hydro_only=not self.B_field)
+                    scheme, dev.device, self.precision, hydro_only=not self.B_field, vp=self.VP)
         h = C.c_void_p()
         _lib.check(self._lib.mhd_create(C.byref(p), C.byref(h)))
         self._h = h
@@ -256,6 +284,14 @@ class Problem:
             raise MHDError(_lib.MHD_ERR_INVALID, f"sol must have shape (nkr, n, n, {nf}) = {(self.grid.nkr, self.n, self.n, nf)}")
         a = np.ascontiguousarray(a, dtype=np.complex64)
         _lib.check(self._lib.mhd_set_state(self._h, a.ctypes.data))
+
+    def set_vp(self, chi, U0=None, B0=None):
+        """The volume-penalisation mask and walls, in place of writing params.χ, params.U₀x..U₀z and
+        params.B₀x..B₀z (src/Structure/datastructure.jl:79-95): ``chi`` an (n, n, n) array indexed
+        [x, y, z] (like prob.vars.ux), ``U0`` / ``B0`` None (zero) or three such arrays.  Needs
+        ``VP_method=True``."""
+        c, u, b = _vp_arrays(self.n, chi, U0, B0)
+        _lib.check(self._lib.mhd_set_vp(self._h, _ptr(c), _ptr(u), _ptr(b)))
 
     def sol_c(self):
         """prob.sol as a C-ordered (nfields, nz, ny, nkr) array (same memory order as the Julia array)."""
@@ -337,6 +373,16 @@ def SetUpProblemIC(prob: Problem, *, ux=None, uy=None, uz=None, bx=None, by=None
     return None
 
 
+def DivVCorrection(prob):
+    """DivVCorrection!(prob) (src/Solver/VPSolver.jl:100-138): u loses its gradient part."""
+    _lib.check(prob._lib.mhd_div_correct(prob._h, _lib.MHD_DIV_U))
+
+
+def DivBCorrection(prob):
+    """DivBCorrection!(prob) (src/Solver/VPSolver.jl:60-98): B loses its gradient part."""
+    _lib.check(prob._lib.mhd_div_correct(prob._h, _lib.MHD_DIV_B))
+
+
 def stepforward(prob: Problem, nsteps: int = 1):
     """stepforward!(prob.sol, prob.clock, prob.timestepper, ...): advance nsteps (default 1)."""
     _lib.check(prob._lib.mhd_step(prob._h, int(nsteps)))
@@ -391,21 +437,32 @@ def TimeIntegrator(prob: Problem, t0: float, N0: int, *, usr_dt: float = 0.0, CF
     updates per second, the reference's own throughput figure (src/integrator.jl:150-153)."""
     import time
 
+    vp = getattr(prob, "VP", False)
+    if vp:  # src/integrator.jl:84-88: clean the divergence before the loop
+        DivVCorrection(prob)
+        if prob.B_field:
+            DivBCorrection(prob)
     if usr_dt > 0:
         _lib.check(prob._lib.mhd_set_cfl(prob._h, 0, CFL_Coef))
         prob.clock.dt = usr_dt
     else:
         _lib.check(prob._lib.mhd_set_cfl(prob._h, 1, CFL_Coef))
     prob.clock.step = 0
+    if vp:  # src/integrator.jl:118-122: and after every step
+        _lib.check(prob._lib.mhd_set_div_correction(prob._h, 1))
     start = time.perf_counter()
-    if math.isinf(t0) and not diags:
-        stepforward(prob, N0 + 1)  # no stopping time to test: one call, no host round trips
-    else:
-        while N0 >= prob.clock.step and t0 >= prob.clock.t:
-            stepforward(prob)
-            for d in diags:
-                d.increment()
-    prob.synchronize()
+    try:
+        if math.isinf(t0) and not diags:
+            stepforward(prob, N0 + 1)  # no stopping time to test: one call, no host round trips
+        else:
+            while N0 >= prob.clock.step and t0 >= prob.clock.t:
+                stepforward(prob)
+                for d in diags:
+                    d.increment()
+        prob.synchronize()
+    finally:
+        if vp:
+            _lib.check(prob._lib.mhd_set_div_correction(prob._h, 0))
     el = time.perf_counter() - start
     return prob.clock.step * prob.n ** 3 / el if el > 0 else float("inf")
 
@@ -433,14 +490,14 @@ class Batch:
     """
 
     def __init__(self, n: int, capacity: int, stepper: str = "RK4", L: float = 2 * math.pi, device: int = 0,
-                 precision="fp32"):
+                 precision="fp32", VP_method=False):
         scheme = {"RK4": MHD_RK4, "LSRK4": MHD_LSRK4}.get(str(stepper).upper())
         if scheme is None:
             raise MHDError(_lib.MHD_ERR_INVALID, f"unknown stepper {stepper!r}")
         self._lib = _lib.load()
         self.n, self.L, self.stepper = int(n), float(L), str(stepper).upper()
         self.nkr = self.n // 2 + 1
-        p = _params(self.n, self.L, 0.0, 0.0, 0, 0, 0.0, scheme, device, precision)
+        p = _params(self.n, self.L, 0.0, 0.0, 0, 0, 0.0, scheme, device, precision, vp=VP_method)
         h = C.c_void_p()
         _lib.check(self._lib.mhd_batch_create(C.byref(p), int(capacity), C.byref(h)))
         self._h = h
@@ -493,6 +550,11 @@ class Batch:
     def set_physical(self, slot: int, field: int, arr):
         a = np.ascontiguousarray(arr, dtype=np.float32)
         _lib.check(self._lib.mhd_slot_set_physical(self._h, int(slot), int(field), a.ctypes.data))
+
+    def set_vp(self, slot: int, chi, U0=None, B0=None):
+        """Volume-penalisation mask and walls of a slot (Problem.set_vp); needs VP_method=True."""
+        c, u, b = _vp_arrays(self.n, chi, U0, B0)
+        _lib.check(self._lib.mhd_slot_set_vp(self._h, int(slot), _ptr(c), _ptr(u), _ptr(b)))
 
     def get_physical(self, slot: int, field: int):
         out = np.empty((self.n, self.n, self.n), dtype=np.float32)

@@ -21,6 +21,8 @@ MHD_ERR_NONFINITE = 4
 MHD_ERR_STATE = 5
 MHD_RK4 = 0
 MHD_LSRK4 = 1
+MHD_DIV_U = 1
+MHD_DIV_B = 2
 MHD_PREC_FP32 = 0
 MHD_PREC_SPLIT_FP16 = 1
 MHD_PREC_SPLIT_BF16 = 2
@@ -49,6 +51,7 @@ class MhdParams(C.Structure):
         ("precision", C.c_int),
         ("device", C.c_int),
         ("hydro_only", C.c_int),
+        ("vp", C.c_int),
     ]
 
 
@@ -101,6 +104,11 @@ _SIGS = {
     "mhd_slot_set_forcing": (C.c_int, [C.c_void_p, C.c_int, C.c_double, C.c_double, C.c_double, C.c_double,
                                        C.c_ulonglong]),
     "mhd_get_forcing": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
+    "mhd_set_vp": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "mhd_slot_set_vp": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "mhd_div_correct": (C.c_int, [C.c_void_p, C.c_int]),
+    "mhd_slot_div_correct": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),
+    "mhd_set_div_correction": (C.c_int, [C.c_void_p, C.c_int]),
     "mhd_autotune": (C.c_int, [C.c_void_p, C.c_int]),
     "mhd_variant_count": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_int)]),
     "mhd_variant_name": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_char_p, C.c_int]),

@@ -51,7 +51,8 @@ int fail(int code, const std::string& msg) {
     }                                                                                    \
   } while (0)
 
-constexpr int kSlots = 8;
+// pass-buffer slots per (z, ky') / (z, y): 8 products, plus 6 penalty fields with VP
+int slots_of(bool vp) { return vp ? 14 : 8; }
 
 OpsBase* make_ops(int n) {
   switch (n) {
@@ -111,12 +112,12 @@ struct Sizes {
   int diag_blocks;
 };
 
-Sizes sizes_of(const Geom& g) {
+Sizes sizes_of(const Geom& g, int ns) {
   Sizes s;
   s.fs = (long long)g.k2 * g.k2 * g.kxp;
   s.state = 6 * s.fs;
-  s.colbuf = (long long)g.n * g.k2 * kSlots * g.kxp;
-  s.rowbuf = (long long)g.n * g.n * kSlots * g.kxp;
+  s.colbuf = (long long)g.n * g.k2 * ns * g.kxp;
+  s.rowbuf = (long long)g.n * g.n * ns * g.kxp;
   s.ref = 6LL * (g.n / 2 + 1) * g.n * g.n;
   s.phys = (long long)g.n * g.n * g.n;
   long long b = (s.fs + kDiagThreads - 1) / kDiagThreads;
@@ -124,16 +125,17 @@ Sizes sizes_of(const Geom& g) {
   return s;
 }
 
-// Device bytes of one slot (state, stage arrays, pass buffers) and of the per-class staging.
-long long slot_bytes(const Geom& g) {
-  Sizes s = sizes_of(g);
-  return (3 * s.state + s.fs + s.colbuf + s.rowbuf) * 8 + 16 * 4;
+// Device bytes of one slot (state, stage arrays, pass buffers; with VP the mask and the six wall
+// fields) and of the per-class staging.
+long long slot_bytes(const Geom& g, bool vp = false) {
+  Sizes s = sizes_of(g, slots_of(vp));
+  return (3 * s.state + s.fs + s.colbuf + s.rowbuf) * 8 + 16 * 4 + (vp ? 7 * s.phys * 4 : 0);
 }
 long long class_bytes(const Geom& g) {
-  Sizes s = sizes_of(g);
+  Sizes s = sizes_of(g, 8);
   return s.ref * 8 + s.phys * 4 + 6LL * g.n * 8 + (long long)s.diag_blocks * kDiagSlots * 8 + 256;
 }
-long long footprint(const Geom& g, int cap) { return class_bytes(g) + (long long)cap * slot_bytes(g); }
+long long footprint(const Geom& g, int cap, bool vp = false) { return class_bytes(g) + (long long)cap * slot_bytes(g, vp); }
 
 }  // namespace
 
@@ -193,12 +195,13 @@ std::string tune_file() {
   return "";
 }
 
-std::string tune_key(int device, int n, int prec) {
+std::string tune_key(int device, int n, int prec, int vp) {
   cudaDeviceProp prop;
   if (cudaGetDeviceProperties(&prop, device) != cudaSuccess) return "";
   std::string name(prop.name);
   for (auto& c : name) if (c == '|' || c == '\n') c = ' ';
-  return name + "|" + std::to_string(prop.multiProcessorCount) + "|" + std::to_string(n) + (prec ? "p" + std::to_string(prec) : "");
+  return name + "|" + std::to_string(prop.multiProcessorCount) + "|" + std::to_string(n) + (prec ? "p" + std::to_string(prec) : "") +
+         (vp ? "v" + std::to_string(vp) : "");
 }
 
 std::vector<std::string> split_bar(const std::string& line) {
@@ -294,6 +297,14 @@ struct mhd_problem {
   // slot is forced (the step then ends with step_tick_kernel)
   long long* dstep = nullptr;
   bool forcing = false;
+  // volume penalisation (mhd_params.vp): ns pass-buffer slots, per-slot mask and wall fields in
+  // physical space, which slots have walls set, and whether each step ends with the divergence
+  // corrections of TimeIntegrator!
+  int ns = 8;
+  float* vchi = nullptr;
+  float* vwall = nullptr;
+  std::vector<char> walls;
+  bool divcorr = false;
   // TMA sources of the column passes (used when a TMA-fed variant is selected) and the device
   // word a timed-out tile wait is recorded in
   TmaPass tm_zinv_sol, tm_zinv_xs, tm_yinv, tm_yfwd, tm_zfwd;
@@ -328,8 +339,9 @@ struct mhd_problem {
     for (auto e : pool) cudaEventDestroy(e);
     pool.clear();
     void* ptrs[] = {sol, xs, acc, aux, colbuf, rowbuf, ref, phys, diag_partial, diag_out, maxabs, dparams, dlist, dvmax, dtime,
-                    dstep, derr};
+                    dstep, derr, vchi, vwall};
     for (void* q : ptrs) if (q) cudaFree(q);
+    vchi = vwall = nullptr;
     sol = xs = acc = aux = colbuf = rowbuf = ref = nullptr;
     phys = nullptr; diag_partial = nullptr; diag_out = nullptr; maxabs = nullptr; dparams = nullptr; dlist = nullptr;
     dvmax = nullptr; dtime = nullptr; dstep = nullptr; derr = nullptr;
@@ -391,9 +403,9 @@ struct mhd_problem {
   // ---- strides (complex elements)
   long long FS() const { return sz.fs; }
   long long ST() const { return sz.state; }
-  long long AZ() const { return (long long)g.k2 * kSlots * g.kxp; }
-  long long BZ() const { return (long long)g.n * kSlots * g.kxp; }
-  long long SLK() const { return (long long)kSlots * g.kxp; }
+  long long AZ() const { return (long long)g.k2 * ns * g.kxp; }
+  long long BZ() const { return (long long)g.n * ns * g.kxp; }
+  long long SLK() const { return (long long)ns * g.kxp; }
 
   // compact fields (src + slot*sI, nf fields at stride FS) -> colbuf slots 0..nf-1
   int z_inverse(const float2* src, long long sI, int nf, BatchRef br) {
@@ -408,7 +420,8 @@ struct mhd_problem {
   }
   int x_fused(BatchRef br, unsigned int* vmax) {
     // the six field rows of a physical row are contiguous (slot stride == kxp)
-    return launch(KC_XFUSED, [&] { ops->x_fused(rowbuf, g, SLK(), g.kxp, sz.rowbuf, br, cap, vmax, stream); });
+    const VpRef vp{vchi, vwall, sz.phys};
+    return launch(KC_XFUSED, [&] { ops->x_fused(rowbuf, g, SLK(), g.kxp, sz.rowbuf, br, cap, vmax, vp, stream); });
   }
   int y_forward(int nf, BatchRef br) {
     ColArgs a{rowbuf, colbuf, (long long)g.kxp, BZ(), SLK(), (long long)g.kxp, AZ(), SLK(), sz.rowbuf, sz.colbuf};
@@ -419,7 +432,8 @@ struct mhd_problem {
     ColArgs a{colbuf, dst, (long long)g.kxp, SLK(), AZ(), FS(), (long long)g.kxp, (long long)g.k2 * g.kxp, sz.colbuf, dI};
     return launch(KC_ZFWD, [&] { ops->col(KC_ZFWD, a, g, g.k2, nf, br, cap, stream, &tm_zfwd); });
   }
-  // Stage epilogue: RHS from the 8 compact product planes (in rowbuf) and the stage state X.
+  // Stage epilogue: RHS from the 8 compact product planes (in rowbuf; 14 with the VP penalty
+  // fields) and the stage state X.
   int epilogue(const float2* X, int op, float hf, float ca, float cb, BatchRef br, int stage) {
     int rc = launch(KC_HERM, [&] {
       const int bxh = g.k2 <= 256 ? (g.k2 + 31) / 32 * 32 : 256;
@@ -448,26 +462,36 @@ struct mhd_problem {
     a.hydro = p.hydro_only;
     const double n3 = (double)g.n * g.n * g.n;
     a.pscale = (float)(1.0 / (n3 * n3));
+    a.vscale = (float)(1.0 / n3);
     const int bx = g.kx <= 256 ? (g.kx + 31) / 32 * 32 : 256;
     const dim3 grid((g.kx + bx - 1) / bx, g.k2, g.k2 * cap);
     // HDcalcN! (src/pgen.jl:176-182) calls addforcing! before HDcalcN_advection!, whose
     // UᵢUpdate! starts by zeroing the velocity right-hand side: a hydrodynamic problem is unforced
+    const bool f = forcing && !p.hydro_only, v = p.vp != 0;
     return launch(KC_RKEPI, [&] {
-      if (forcing && !p.hydro_only) launch_epilogue<true>(op, grid, bx, a, br);
-      else launch_epilogue<false>(op, grid, bx, a, br);
+      if (f && v) launch_epilogue<true, true>(op, grid, bx, a, br);
+      else if (f) launch_epilogue<true, false>(op, grid, bx, a, br);
+      else if (v) launch_epilogue<false, true>(op, grid, bx, a, br);
+      else launch_epilogue<false, false>(op, grid, bx, a, br);
     });
   }
   // record: the stage whose physical fields getCFL! reads (the last one of a step)
-  template <bool F>
+  template <bool F, bool V>
   void launch_epilogue(int op, dim3 grid, int bx, const RkArgs& a, BatchRef br) {
     switch (op) {
-      case OP_RHS: rk_epilogue_kernel<OP_RHS, F><<<grid, bx, 0, stream>>>(a, g, br); break;
-      case OP_RK4_FIRST: rk_epilogue_kernel<OP_RK4_FIRST, F><<<grid, bx, 0, stream>>>(a, g, br); break;
-      case OP_RK4_MID: rk_epilogue_kernel<OP_RK4_MID, F><<<grid, bx, 0, stream>>>(a, g, br); break;
-      case OP_RK4_LAST: rk_epilogue_kernel<OP_RK4_LAST, F><<<grid, bx, 0, stream>>>(a, g, br); break;
-      case OP_LS_FIRST: rk_epilogue_kernel<OP_LS_FIRST, F><<<grid, bx, 0, stream>>>(a, g, br); break;
-      default: rk_epilogue_kernel<OP_LS, F><<<grid, bx, 0, stream>>>(a, g, br); break;
+      case OP_RHS: rk_epilogue_kernel<OP_RHS, F, V><<<grid, bx, 0, stream>>>(a, g, br); break;
+      case OP_RK4_FIRST: rk_epilogue_kernel<OP_RK4_FIRST, F, V><<<grid, bx, 0, stream>>>(a, g, br); break;
+      case OP_RK4_MID: rk_epilogue_kernel<OP_RK4_MID, F, V><<<grid, bx, 0, stream>>>(a, g, br); break;
+      case OP_RK4_LAST: rk_epilogue_kernel<OP_RK4_LAST, F, V><<<grid, bx, 0, stream>>>(a, g, br); break;
+      case OP_LS_FIRST: rk_epilogue_kernel<OP_LS_FIRST, F, V><<<grid, bx, 0, stream>>>(a, g, br); break;
+      default: rk_epilogue_kernel<OP_LS, F, V><<<grid, bx, 0, stream>>>(a, g, br); break;
     }
+  }
+  // DivVCorrection! / DivBCorrection! of the slots in br (mask: 1 u, 2 B)
+  int div_correct(BatchRef br, int ninst, int mask) {
+    const int bx = g.kx <= 256 ? (g.kx + 31) / 32 * 32 : 256;
+    const dim3 grid((g.kx + bx - 1) / bx, g.k2, g.k2 * ninst);
+    return launch(KC_OTHER, [&] { div_correct_kernel<<<grid, bx, 0, stream>>>(sol, g, FS(), ST(), br, mask); });
   }
   // stage: right-hand-side evaluation within the step (7 outside a step)
   int rhs(const float2* X, int op, float hf, float ca, float cb, BatchRef br, int stage, bool record = false) {
@@ -475,8 +499,8 @@ struct mhd_problem {
     if ((rc = z_inverse(X, ST(), 6, br))) return rc;
     if ((rc = y_inverse(6, br))) return rc;
     if ((rc = x_fused(br, (record && cfl) ? dvmax : nullptr))) return rc;
-    if ((rc = y_forward(kSlots, br))) return rc;
-    if ((rc = z_forward(rowbuf, sz.rowbuf, kSlots, br))) return rc;
+    if ((rc = y_forward(ns, br))) return rc;
+    if ((rc = z_forward(rowbuf, sz.rowbuf, ns, br))) return rc;
     return epilogue(X, op, hf, ca, cb, br, stage);
   }
   // One step of every active slot (launches only; see run_steps for graphs and clocks).
@@ -496,6 +520,12 @@ struct mhd_problem {
           step_tick_kernel<<<(cap + 127) / 128, 128, 0, stream>>>(br, dstep);
         })))
       return rc;
+    if (divcorr) {
+      // TimeIntegrator! with VP (src/integrator.jl:118-122): DivVCorrection!, and DivBCorrection!
+      // for MHD, after every step; they also refresh vars, which the next getCFL! reads
+      if ((rc = div_correct(br, cap, p.hydro_only ? 1 : 3))) return rc;
+      if (cfl && (rc = cfl_prime())) return rc;
+    }
     if (cfl) return cfl_update(1);
     return MHD_OK;
   }
@@ -578,7 +608,7 @@ struct mhd_problem {
     if (profiling) return fail(MHD_ERR_STATE, "autotune does not run with per-kernel profiling enabled");
     int rc;
     if ((rc = sync_lists())) return rc;
-    const std::string key = tune_key(device, g.n, p.precision);
+    const std::string key = tune_key(device, g.n, p.precision, ops->vp);
     std::vector<std::string> names;
     if (!force && !key.empty() && tuned_lookup(key, &names) && apply_names(names) == MHD_OK) return MHD_OK;
     if (active.empty()) return fail(MHD_ERR_STATE, "autotune needs at least one active slot");
@@ -672,11 +702,12 @@ struct mhd_problem {
     const cuuint32_t bz[5] = {16, 1, kp, 1, 1};
     set(tm_zinv_sol, sol, dz, sz5, bz, TmaCoords{2, 1, 3, 4, (int)kp});
     set(tm_zinv_xs, xs, dz, sz5, bz, TmaCoords{2, 1, 3, 4, (int)kp});
-    // colbuf [slot][z][ky'][8][kx] and rowbuf [slot][z][y][8][kx]
-    const cuuint64_t dc[5] = {kxp, 8, k2, n, C};
-    const cuuint64_t sc[4] = {kxp * E, 8 * kxp * E, k2 * 8 * kxp * E, (cuuint64_t)sz.colbuf * E};
-    const cuuint64_t dr[5] = {kxp, 8, n, n, C};
-    const cuuint64_t sr[4] = {kxp * E, 8 * kxp * E, n * 8 * kxp * E, (cuuint64_t)sz.rowbuf * E};
+    // colbuf [slot][z][ky'][ns][kx] and rowbuf [slot][z][y][ns][kx]
+    const cuuint64_t S = ns;
+    const cuuint64_t dc[5] = {kxp, S, k2, n, C};
+    const cuuint64_t sc[4] = {kxp * E, S * kxp * E, k2 * S * kxp * E, (cuuint64_t)sz.colbuf * E};
+    const cuuint64_t dr[5] = {kxp, S, n, n, C};
+    const cuuint64_t sr[4] = {kxp * E, S * kxp * E, n * S * kxp * E, (cuuint64_t)sz.rowbuf * E};
     const cuuint32_t by_in[5] = {16, 1, kp, 1, 1};
     const cuuint32_t by_out[5] = {16, 1, rb, 1, 1};
     const cuuint32_t bz_out[5] = {16, 1, 1, rb, 1};
@@ -729,6 +760,9 @@ int validate(const mhd_params* p) {
     return fail(MHD_ERR_INVALID, "precision must be MHD_PREC_FP32, MHD_PREC_SPLIT_FP16 or MHD_PREC_SPLIT_BF16");
   if (p->precision != MHD_PREC_FP32 && p->n != 128 && p->n != 256 && p->n != 512)
     return fail(MHD_ERR_INVALID, "the split-precision tensor-core forms exist for n = 128, 256, 512");
+  if (p->vp != 0 && p->vp != 1) return fail(MHD_ERR_INVALID, "vp must be 0 or 1");
+  if (p->vp && p->precision != MHD_PREC_FP32)
+    return fail(MHD_ERR_INVALID, "volume penalisation runs in the FP32 form only");
   return MHD_OK;
 }
 
@@ -750,15 +784,18 @@ int create_class(const mhd_params* params, int cap, mhd_handle* out) {
   h->device = params->device;
   MHD_CUDA(cudaSetDevice(h->device));
   h->g = make_geom(params->n, params->L);
-  h->sz = sizes_of(h->g);
+  h->ns = slots_of(params->vp != 0);
+  h->sz = sizes_of(h->g, h->ns);
   h->ops.reset(make_ops(params->n));
   if (!h->ops) return fail(MHD_ERR_INVALID, "no plan for n");
   h->ops->prec = params->precision;
+  h->ops->vp_capable = params->vp != 0;
   if ((rc = h->ops->setup(h->g))) return rc;
+  if (params->vp && (rc = h->ops->set_vp(1))) return rc;  // mask only until walls are set
   {
     // a selection the autotuner made earlier for this device and grid size (this process or the
     // tuning file); the defaults otherwise
-    const std::string key = tune_key(h->device, h->g.n, params->precision);
+    const std::string key = tune_key(h->device, h->g.n, params->precision, h->ops->vp);
     std::vector<std::string> names;
     if (!key.empty() && tuned_lookup(key, &names)) h->apply_names(names);
   }
@@ -790,6 +827,13 @@ int create_class(const mhd_params* params, int cap, mhd_handle* out) {
   MHD_CUDA(cudaMemsetAsync(h->sol, 0, c * s.state * sizeof(float2), h->stream));
   MHD_CUDA(cudaMemsetAsync(h->xs, 0, c * s.state * sizeof(float2), h->stream));
   MHD_CUDA(cudaMemsetAsync(h->acc, 0, c * s.state * sizeof(float2), h->stream));
+  if (params->vp) {
+    MHD_CUDA(cudaMalloc(&h->vchi, c * s.phys * sizeof(float)));
+    MHD_CUDA(cudaMalloc(&h->vwall, 6 * c * s.phys * sizeof(float)));
+    MHD_CUDA(cudaMemsetAsync(h->vchi, 0, c * s.phys * sizeof(float), h->stream));
+    MHD_CUDA(cudaMemsetAsync(h->vwall, 0, 6 * c * s.phys * sizeof(float), h->stream));
+  }
+  h->walls.assign(cap, 0);
   h->build_tma();
   h->hparams.assign(cap, SlotParams{0.f, 0.f, 0.f, 0.f});
   h->used.assign(cap, 0);
@@ -839,7 +883,7 @@ int mhd_footprint_bytes(const mhd_params* params, long long* bytes) {
   int rc = validate(params);
   if (rc) return rc;
   if (!bytes) return fail(MHD_ERR_INVALID, "null output");
-  *bytes = footprint(make_geom(params->n, params->L), 1);
+  *bytes = footprint(make_geom(params->n, params->L), 1, params->vp != 0);
   return MHD_OK;
 }
 
@@ -847,7 +891,7 @@ int mhd_slot_bytes(const mhd_params* params, long long* per_slot, long long* per
   int rc = validate(params);
   if (rc) return rc;
   const Geom g = make_geom(params->n, params->L);
-  if (per_slot) *per_slot = slot_bytes(g);
+  if (per_slot) *per_slot = slot_bytes(g, params->vp != 0);
   if (per_class) *per_class = class_bytes(g);
   return MHD_OK;
 }
@@ -1074,6 +1118,65 @@ int mhd_set_forcing(mhd_handle h, double P, double kf, double sigma, double b, u
   return mhd_slot_set_forcing(h, 0, P, kf, sigma, b, seed);
 }
 
+int mhd_slot_set_vp(mhd_handle h, int slot, const float* chi, const float* U0, const float* B0) {
+  int rc = check_slot(h, slot);
+  if (rc) return rc;
+  if (!h->p.vp) return fail(MHD_ERR_STATE, "volume penalisation is off for this handle (mhd_params.vp = 0)");
+  const long long n3 = h->sz.phys;
+  const size_t fb = (size_t)n3 * sizeof(float);
+  float* c = h->vchi + slot * n3;
+  float* w = h->vwall + 6 * slot * n3;
+  if (chi) MHD_CUDA(cudaMemcpyAsync(c, chi, fb, cudaMemcpyHostToDevice, h->stream));
+  else MHD_CUDA(cudaMemsetAsync(c, 0, fb, h->stream));
+  const float* src[2] = {U0, B0};
+  for (int k = 0; k < 2; ++k) {
+    if (src[k]) MHD_CUDA(cudaMemcpyAsync(w + 3 * k * n3, src[k], 3 * fb, cudaMemcpyHostToDevice, h->stream));
+    else MHD_CUDA(cudaMemsetAsync(w + 3 * k * n3, 0, 3 * fb, h->stream));
+  }
+  h->walls[slot] = (U0 || B0) ? 1 : 0;
+  bool any = false;
+  for (int s = 0; s < h->cap; ++s) any = any || h->walls[s];
+  const int mode = any ? 2 : 1;
+  if (mode != h->ops->vp) {
+    if ((rc = h->ops->set_vp(mode))) return rc;
+    // a tuned selection of the new form, if one is known
+    const std::string key = tune_key(h->device, h->g.n, h->p.precision, mode);
+    std::vector<std::string> names;
+    if (!key.empty() && tuned_lookup(key, &names)) h->apply_names(names);
+    h->invalidate_graph();
+  }
+  MHD_CUDA(cudaStreamSynchronize(h->stream));
+  return MHD_OK;
+}
+
+int mhd_set_vp(mhd_handle h, const float* chi, const float* U0, const float* B0) {
+  return mhd_slot_set_vp(h, 0, chi, U0, B0);
+}
+
+int mhd_slot_div_correct(mhd_handle h, int slot, int fields) {
+  int rc = check_slot(h, slot);
+  if (rc) return rc;
+  if (fields < 0 || fields > 3) return fail(MHD_ERR_INVALID, "fields must be a mask of MHD_DIV_U and MHD_DIV_B");
+  if (h->p.hydro_only) fields &= MHD_DIV_U;
+  if (fields && (rc = h->div_correct(h->slot_ref(slot), 1, fields))) return rc;
+  MHD_CUDA(cudaStreamSynchronize(h->stream));
+  return MHD_OK;
+}
+
+int mhd_div_correct(mhd_handle h, int fields) { return mhd_slot_div_correct(h, 0, fields); }
+
+int mhd_set_div_correction(mhd_handle h, int on) {
+  int rc = check_handle(h);
+  if (rc) return rc;
+  if (on != 0 && on != 1) return fail(MHD_ERR_INVALID, "on must be 0 or 1");
+  if ((on != 0) != h->divcorr) {
+    MHD_CUDA(cudaStreamSynchronize(h->stream));
+    h->divcorr = on != 0;
+    h->invalidate_graph();
+  }
+  return MHD_OK;
+}
+
 int mhd_get_forcing(mhd_handle h, int slot, double* A, double* kf_used) {
   if (!h) return fail(MHD_ERR_INVALID, "null handle");
   if (!h->valid_slot(slot)) return fail(MHD_ERR_INVALID, "slot " + std::to_string(slot) + " is not active");
@@ -1196,7 +1299,7 @@ void* mhd_get_stream(mhd_handle h) { return h ? (void*)h->stream : nullptr; }
 
 int mhd_memory_bytes(mhd_handle h, long long* bytes) {
   if (!h || !bytes) return fail(MHD_ERR_INVALID, "null argument");
-  *bytes = footprint(h->g, h->cap);
+  *bytes = footprint(h->g, h->cap, h->p.vp != 0);
   return MHD_OK;
 }
 
@@ -1247,13 +1350,16 @@ int mhd_kernel_class_bytes(mhd_handle h, int cls, double* bytes) {
   double b = 0;
   // state arrays (6 fields each) one epilogue launch touches, averaged over the scheme's stages
   const double arrays = h->p.scheme == MHD_RK4 ? (3 + 5 + 5 + 4) / 4.0 : (3 + 4 * 4) / 5.0;
+  // out-going planes (8 products, 14 with the VP penalty fields) and the VP mask / wall reads
+  const double ns = h->ns;
+  const double vpin = h->p.vp ? (h->ops->vp == 2 ? 7.0 : 1.0) * n * n * n * 4.0 : 0.0;
   switch (cls) {
     case KC_ZINV: b = 6 * (state_field + n * k2 * kx * c); break;
     case KC_YINV: b = 6 * (n * k2 * kx * c + n * n * kx * c); break;
-    case KC_XFUSED: b = (6 + 8) * n * n * kx * c; break;
-    case KC_YFWD: b = 8 * (n * n * kx * c + n * k2 * kx * c); break;
-    case KC_ZFWD: b = 8 * (n * k2 * kx * c + state_field); break;
-    case KC_RKEPI: b = 8 * state_field + arrays * 6 * state_field + 6 * k2 * k2 * c; break;
+    case KC_XFUSED: b = (6 + ns) * n * n * kx * c + vpin; break;
+    case KC_YFWD: b = ns * (n * n * kx * c + n * k2 * kx * c); break;
+    case KC_ZFWD: b = ns * (n * k2 * kx * c + state_field); break;
+    case KC_RKEPI: b = ns * state_field + arrays * 6 * state_field + 6 * k2 * k2 * c; break;
     case KC_HERM: b = 2 * 6 * k2 * k2 * c; break;
     default: b = 0;
   }

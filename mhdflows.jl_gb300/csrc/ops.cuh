@@ -26,7 +26,7 @@ constexpr int kTunedClasses = 5;  // z_inverse .. z_forward
 int report_error(int code, const std::string& msg);
 
 using XFn = void (*)(float2*, Geom, long long, long long, long long, BatchRef, const float2*, const float2*,
-                     unsigned int*);
+                     unsigned int*, VpRef);
 using ColFn = void (*)(ColArgs, Geom, ColWork, BatchRef, const float2*);
 using TmaColFn = void (*)(ColArgs, Geom, ColWork, BatchRef, const float2*, CUtensorMap, TmaCoords, int*);
 
@@ -52,6 +52,8 @@ struct XVariant {
   // precision form: 0 FP32, 1 split FP16 tensor cores, 2 split BF16 tensor cores; the split
   // forms read a per-device constant table (DFT fragments, twiddles) built by build_table
   int prec = 0;
+  // volume penalisation (x_fused_kernel's VPM): 0 none, 1 mask only, 2 mask and wall fields
+  int vp = 0;
   size_t table_words = 0;
   int (*build_table)(uint32_t* table) = nullptr;
   uint32_t* table = nullptr;
@@ -77,12 +79,17 @@ class OpsBase {
   void col(int cls, const ColArgs& a, const Geom& g, int outer, int nf, BatchRef br, int cap, cudaStream_t s,
            const TmaPass* tp = nullptr) const;
   void x_fused(float2* pool, const Geom& g, long long rowstride, long long slot, long long istride, BatchRef br,
-               int cap, unsigned int* vmax, cudaStream_t s) const;
+               int cap, unsigned int* vmax, VpRef vp, cudaStream_t s) const;
   void x_c2r(const float2* src, float* dst, const Geom& g, long long srow, float scale, cudaStream_t s) const;
   void x_r2c(const float* src, float2* dst, const Geom& g, long long drow, cudaStream_t s) const;
 
   int n = 0;
   int prec = 0;  // precision form of the x rows (mhd_params.precision)
+  int vp = 0;    // volume-penalisation form of the x rows (XVariant::vp)
+  bool vp_capable = false;  // set before setup: prepare the penalty forms too
+  // switch the volume-penalisation form; the x-row class falls back to its first variant of the
+  // new form (MHD_OK, or MHD_ERR_INVALID when this grid size has none)
+  int set_vp(int mode);
   std::vector<XVariant> xv;
   std::vector<ColVariant> cv;
   int sel[kTunedClasses] = {0, 0, 0, 0, 0};  // selected variant of each tuned class
@@ -163,6 +170,30 @@ class Ops : public OpsBase {
     v.group_words = &XC::group_words;
     v.tw = twiddles<R>();
     v.twr = twiddles<typename Reverse<R>::type>();
+    xv.push_back(v);
+  }
+
+  // x rows with the volume-penalisation pairs: the mask-only and the mask-and-walls forms of a
+  // plan, one forward transform per exchange round
+  template <class R, int GROUPS, int NTI, int MINB>
+  void add_x_vp() {
+    add_x_vp_one<R, GROUPS, NTI, MINB, 1>();
+    add_x_vp_one<R, GROUPS, NTI, MINB, 2>();
+  }
+  template <class R, int GROUPS, int NTI, int MINB, int VPM>
+  void add_x_vp_one() {
+    using XC = XCfg<R, NTI>;
+    XVariant v;
+    v.name = "xvp" + std::to_string(VPM) + ":" + plan_name<R>() + "/nt" + std::to_string(NTI) + "1/c" +
+             std::to_string(GROUPS) + "/b" + std::to_string(MINB);
+    v.fn = x_fused_kernel<R, GROUPS, NTI, 1, MINB, VPM>;
+    v.threads = GROUPS * XC::TPG;
+    v.rpg = XC::RPG;
+    v.groups = GROUPS;
+    v.group_words = &XC::group_words;
+    v.tw = twiddles<R>();
+    v.twr = twiddles<typename Reverse<R>::type>();
+    v.vp = VPM;
     xv.push_back(v);
   }
 

@@ -51,6 +51,7 @@ int OpsBase::setup(const Geom& g) {
     x.smem = sizeof(float2) * (size_t)x.groups * x.group_words(g.kxp);
     x.ctas = 0;
     if (x.prec != prec || (int)x.smem > smem_max) continue;  // only this problem's precision form
+    if (x.vp && !vp_capable) continue;                       // penalty forms only with VP on
     if (x.build_table) {
       e = cudaMalloc(&x.table, x.table_words * sizeof(uint32_t));
       if (e != cudaSuccess) return report_error(MHD_ERR_OOM, std::string("tensor-core tables: ") + cudaGetErrorString(e));
@@ -85,6 +86,16 @@ int OpsBase::setup(const Geom& g) {
   return MHD_OK;
 }
 
+int OpsBase::set_vp(int mode) {
+  if (mode == vp) return MHD_OK;
+  const int old = vp;
+  vp = mode;
+  for (int i = 0; i < (int)xv.size(); ++i)
+    if (variant_ok(KC_XFUSED, i)) { sel[KC_XFUSED] = i; return MHD_OK; }
+  vp = old;
+  return report_error(MHD_ERR_INVALID, "no x-row kernel of this volume-penalisation form for this grid size");
+}
+
 int OpsBase::variant_count(int cls) const {
   if (cls == KC_XFUSED) return (int)xv.size();
   return is_col(cls) ? (int)cv.size() : 0;
@@ -92,7 +103,7 @@ int OpsBase::variant_count(int cls) const {
 
 bool OpsBase::variant_ok(int cls, int i) const {
   if (i < 0 || i >= variant_count(cls)) return false;
-  if (cls == KC_XFUSED) return xv[i].ctas > 0 && xv[i].prec == prec;
+  if (cls == KC_XFUSED) return xv[i].ctas > 0 && xv[i].prec == prec && xv[i].vp == vp;
   return is_inv(cls) ? cv[i].ctas_inv > 0 : cv[i].ctas_fwd > 0;
 }
 
@@ -138,14 +149,14 @@ void OpsBase::col(int cls, const ColArgs& a, const Geom& g, int outer, int nf, B
 }
 
 void OpsBase::x_fused(float2* pool, const Geom& g, long long rowstride, long long slot, long long istride,
-                      BatchRef br, int cap, unsigned int* vmax, cudaStream_t s) const {
+                      BatchRef br, int cap, unsigned int* vmax, VpRef vp, cudaStream_t s) const {
   const XVariant& x = xv[sel[KC_XFUSED]];
   const long long groups = (long long)cap * n * n / x.rpg;
   const long long need = (groups + x.groups - 1) / x.groups;
   const int grid = (int)(need < x.ctas ? need : x.ctas);
   const float2* t1 = x.table ? reinterpret_cast<const float2*>(x.table) : tw_dev + x.tw;
   const float2* t2 = x.table ? nullptr : tw_dev + x.twr;
-  x.fn<<<grid, x.threads, x.smem, s>>>(pool, g, rowstride, slot, istride, br, t1, t2, vmax);
+  x.fn<<<grid, x.threads, x.smem, s>>>(pool, g, rowstride, slot, istride, br, t1, t2, vmax, vp);
 }
 
 void OpsBase::x_c2r(const float2* src, float* dst, const Geom& g, long long srow, float scale, cudaStream_t s) const {

@@ -4,7 +4,8 @@
 //   state   S[f][kz'][ky'][kx]          retained band only (kx < Kx, ky', kz' kept indices)
 //   colbuf  A[z][ky'][slot][kx]         after the z pass (inverse) / before it (forward)
 //   rowbuf  B[z][y][slot][kx]           after the y pass (inverse) / before it (forward)
-// 8 slots per (z, ky') and (z, y): fields 0..5 on the way in, products 0..7 on the way out.
+// 8 slots per (z, ky') and (z, y): fields 0..5 on the way in, products 0..7 on the way out; with
+// volume penalisation 14 slots, the six penalty fields in slots 8..13 on the way out.
 // A kept index j maps to frequency index j (j < Kp) or j + n - K2 (negative wavenumbers).
 #pragma once
 #include <cuda.h>
@@ -68,6 +69,15 @@ struct RowSync {
 struct BatchRef {
   const int* list;   // active slots
   const int* count;  // number of active slots
+};
+
+// Volume-penalisation inputs of the x rows (src/Solver/VPSolver.jl): per slot the mask chi
+// (n^3 floats) and the wall fields U0x U0y U0z B0x B0y B0z (6 n^3 floats), all in the reference's
+// (x, y, z) order, x fastest: the row of physical (y, z) starts at (z n + y) n.
+struct VpRef {
+  const float* chi;
+  const float* wall;
+  long long cs;  // n^3: field stride; slot strides cs (chi) and 6 cs (wall)
 };
 
 struct SlotParams {
@@ -542,16 +552,22 @@ struct XCfg {
 // Variants (chosen per grid size by the autotuner): NTI inverse transforms (1 or 3) and NTF
 // forward transforms (1, 2 or 4) go through the stages together, sharing the twiddle loads and
 // the barriers and giving each thread more independent work; MINB is the occupancy bound.
-template <class P, int GROUPS, int NTI, int NTF, int MINB>
+//
+// VPM (volume penalisation, VP_UᵢUpdate! / VP_BᵢUpdate! of src/Solver/VPSolver.jl:20-58): 0 off;
+// 1 adds the penalty fields chi u and chi B (walls U0 = B0 = 0); 2 adds chi (u - U0), chi (B - B0).
+// They leave as three more forward pairs in slots 8..13; the epilogue scales and projects them.
+template <class P, int GROUPS, int NTI, int NTF, int MINB, int VPM = 0>
 __global__ void __launch_bounds__(GROUPS * XCfg<P>::TPG, MINB)
     x_fused_kernel(float2* pool, Geom geo, long long rowstride, long long slot, long long istride, BatchRef br,
-                   const float2* __restrict__ tw, const float2* __restrict__ twr, unsigned int* vmax) {
+                   const float2* __restrict__ tw, const float2* __restrict__ twr, unsigned int* vmax, VpRef vp) {
   using PR = typename Reverse<P>::type;
   constexpr int NTS = NTI > NTF ? NTI : NTF;
   using XC = XCfg<P, NTS>;
   static_assert(NTI == 1 || NTI == 3, "inverse transforms go one or three at a time");
   static_assert(NTF == 1 || NTF == 2 || NTF == 4, "forward transforms go one, two or four at a time");
   static_assert(NTF == 1 || P::G <= 32, "batched forward transforms need the row inside one warp");
+  static_assert(VPM == 0 || NTF == 1, "the penalty pairs go one at a time");
+  constexpr int NPAIR = VPM ? 7 : 4;  // forward transform pairs per row
   constexpr int G = P::G, V = P::V, N = P::N, RPG = XC::RPG, TPG = XC::TPG, TS = XC::TS;
   constexpr int KX = kept_kx_of(N);  // the host checks geo.kx == KX
   extern __shared__ float2 smem[];
@@ -628,10 +644,25 @@ __global__ void __launch_bounds__(GROUPS * XCfg<P>::TPG, MINB)
       }
     }
     float2* rowp = group_rows(q) + rr * rowstride;
+    // the penalty inputs of this row at the physical points this thread holds: x = lF + LF e for
+    // register d RF + e (the inverse plan's output layout)
+    float chi[VPM ? V : 1];
+    const float* wrow = nullptr;
+    if constexpr (VPM > 0) {
+      const int inst = (int)(q / GPI);
+      const long long s = br.list[inst];
+      const long long r = (q - (long long)inst * GPI) * RPG + rr;  // z n + y
+      const float* crow = vp.chi + s * vp.cs + r * N;
+      if constexpr (VPM == 2) wrow = vp.wall + 6 * s * vp.cs + r * N;
+#pragma unroll
+      for (int d = 0; d < P::DF; ++d)
+#pragma unroll
+        for (int e = 0; e < P::RF; ++e) chi[d * P::RF + e] = __ldg(crow + g + G * d + P::LF * e);
+    }
     // NTF product pairs at a time: the six fields stay live, each pair is formed just before its
     // forward transform (fewer live registers than all eight products at once)
 #pragma unroll
-    for (int t0 = 0; t0 < 4; t0 += NTF) {
+    for (int t0 = 0; t0 < NPAIR; t0 += NTF) {
       float2 w[NTF][V];
 #pragma unroll
       for (int j = 0; j < NTF; ++j) {
@@ -640,7 +671,19 @@ __global__ void __launch_bounds__(GROUPS * XCfg<P>::TPG, MINB)
         for (int i = 0; i < V; ++i) {
           const float ux = v[0][i].x, uy = v[0][i].y, uz = v[1][i].x;
           const float bx = v[1][i].y, by = v[2][i].x, bz = v[2][i].y;
-          if (t == 0) {
+          if (t >= 4) {  // penalty pair t - 4: (u x, u y), (u z, B x), (B y, B z) of the field pairs
+            if constexpr (VPM > 0) {
+              float2 f = v[t - 4][i];
+              if constexpr (VPM == 2) {  // the fields are n^3 times physical: so are the walls
+                constexpr float n3 = (float)N * (float)N * (float)N;
+                const int x = g + G * (i / P::RF) + P::LF * (i % P::RF);
+                const long long c0 = (long long)(2 * (t - 4)) * vp.cs;
+                f.x = fmaf(-n3, __ldg(wrow + c0 + x), f.x);
+                f.y = fmaf(-n3, __ldg(wrow + c0 + vp.cs + x), f.y);
+              }
+              w[j][i] = make_float2(chi[i] * f.x, chi[i] * f.y);
+            }
+          } else if (t == 0) {
             const float tzz = bz * bz - uz * uz;
             w[j][i] = make_float2((bx * bx - ux * ux) - tzz, (by * by - uy * uy) - tzz);
           } else if (t == 1) {

@@ -24,7 +24,7 @@ enum StageOp : int {
 // projection removes).  Induction: R_b = i k x E - eta k^2 X_b with E = (Ayz, -Axz, Axy) = u x B.
 // ------------------------------------------------------------------------------------------
 struct RkArgs {
-  const float2* prod;   // 8 compact planes (slot stride prodI)
+  const float2* prod;   // 8 compact product planes, then 6 penalty planes with VP (slot stride prodI)
   const float2* X;      // stage state (6 fields, slot stride stI)
   const float2* H;      // Hermitian part of X on the kx = 0 plane, [f][kz'][ky'] (slot stride hI)
   float2* sol;          // RK4 step-start state
@@ -40,6 +40,7 @@ struct RkArgs {
   const long long* step; // per-slot step counters (random forcing: call = 8 * step + stage)
   int stage;             // right-hand-side evaluation within the step (7: outside a step)
   int hydro;             // hydrodynamics: the induction right-hand side is zero, B stays zero
+  float vscale;          // 1/n^3: the penalty planes are n^3 times the reference's rfft
 };
 
 // ------------------------------------------------------------------------------------------
@@ -120,7 +121,7 @@ __device__ __forceinline__ void rk_apply(const RkSlot& a, long long o, float2 x,
 }
 
 // grid (ceil(kx / blockDim.x), k2, k2): one thread per retained mode, no index division.
-template <int OP, bool FORCED>
+template <int OP, bool FORCED, bool VPEN>
 __global__ void __launch_bounds__(256) rk_epilogue_kernel(RkArgs a, Geom geo, BatchRef br) {
   const int x = blockIdx.x * blockDim.x + threadIdx.x;
   if (x >= geo.kx) return;
@@ -177,6 +178,23 @@ __global__ void __launch_bounds__(256) rk_epilogue_kernel(RkArgs a, Geom geo, Ba
   for (int c = 0; c < 6; ++c) {
     const float dk = c < 3 ? du : db;
     R[c] = make_float2(nl[c].x + dk * xd[c].x, nl[c].y + dk * xd[c].y);
+  }
+  if constexpr (VPEN) {
+    // VP_UᵢUpdate! / VP_BᵢUpdate! (src/Solver/VPSolver.jl:20-58): N_a += -(δ_aj - k_a k_j / k^2) F_j
+    // with F = rfft(chi / eta (u - U0)) (and chi / eta (B - B0)), eta = 13 dt / 7, 1/k^2 = 0 at k = 0
+    const float sc = -a.vscale * 7.f / (13.f * sp.dt);
+    float2 F[6];
+#pragma unroll
+    for (int q = 0; q < 6; ++q) F[q] = cscale(__ldcs(prod + (8 + q) * fs + i), sc);
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const float2 f0 = F[3 * h], f1 = F[3 * h + 1], f2 = F[3 * h + 2];
+      const float px = (kxv * f0.x + kyv * f1.x + kzv * f2.x) * ik2;
+      const float py = (kxv * f0.y + kyv * f1.y + kzv * f2.y) * ik2;
+      R[3 * h] = make_float2(R[3 * h].x + f0.x - kxv * px, R[3 * h].y + f0.y - kxv * py);
+      R[3 * h + 1] = make_float2(R[3 * h + 1].x + f1.x - kyv * px, R[3 * h + 1].y + f1.y - kyv * py);
+      R[3 * h + 2] = make_float2(R[3 * h + 2].x + f2.x - kzv * px, R[3 * h + 2].y + f2.y - kzv * py);
+    }
   }
   if (FORCED && sp.fA != 0.f) {  // addforcing!: N[u] += F, then the kx = 0 plane keeps its real part
     const unsigned long long call = 8ull * (unsigned long long)a.step[slot] + (unsigned long long)a.stage;
@@ -416,6 +434,35 @@ __global__ void divb_spectrum_kernel(const float2* __restrict__ S, float2* __res
     const float re = kx * bx.x + ky * by.x + kz * bz.x;
     const float im = kx * bx.y + ky * by.y + kz * bz.y;
     out[i] = x < geo.kx ? make_float2(-im, re) : make_float2(0.f, 0.f);
+  }
+}
+
+// DivVCorrection! / DivBCorrection! (src/Solver/VPSolver.jl:60-138): u (mask bit 0) and B (bit 1)
+// of every active slot lose their gradient part, X -= k (k.X) / k^2 with 1/k^2 = 0 at k = 0.
+// grid (ceil(kx / blockDim.x), k2, k2 * cap): one thread per retained mode.
+__global__ void div_correct_kernel(float2* __restrict__ pool, Geom geo, long long fs, long long stI, BatchRef br,
+                                   int mask) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  if (x >= geo.kx) return;
+  const int inst = blockIdx.z / geo.k2;
+  if (inst >= *br.count) return;
+  const int jy = blockIdx.y, jz = blockIdx.z - inst * geo.k2;
+  float2* X = pool + br.list[inst] * stI + ((long long)jz * geo.k2 + jy) * geo.kxp + x;
+  const float kx = geo.kscale * (float)x;
+  const float ky = geo.kscale * (float)signed_of_kept(geo, jy);
+  const float kz = geo.kscale * (float)signed_of_kept(geo, jz);
+  const float k2 = kx * kx + ky * ky + kz * kz;
+  const float ik2 = k2 > 0.f ? 1.0f / k2 : 0.f;
+#pragma unroll
+  for (int h = 0; h < 2; ++h) {
+    if (!(mask & (1 << h))) continue;
+    float2* F = X + 3 * h * fs;
+    const float2 a = F[0], b = F[fs], c = F[2 * fs];
+    const float pr = (kx * a.x + ky * b.x + kz * c.x) * ik2;
+    const float pi = (kx * a.y + ky * b.y + kz * c.y) * ik2;
+    F[0] = make_float2(a.x - kx * pr, a.y - kx * pi);
+    F[fs] = make_float2(b.x - ky * pr, b.y - ky * pi);
+    F[2 * fs] = make_float2(c.x - kz * pr, c.y - kz * pi);
   }
 }
 

@@ -485,7 +485,8 @@ __device__ __forceinline__ void tc_forward(Prod prod, float s, float2* buf, cons
 template <int N, int KIND, int GROUPS, int MINB>
 __global__ void __launch_bounds__(GROUPS * 32, MINB)
     x_fused_tc_kernel(float2* pool, Geom geo, long long rowstride, long long slot, long long istride, BatchRef br,
-                      const float2* __restrict__ tabf, const float2* __restrict__ unused, unsigned int* vmax) {
+                      const float2* __restrict__ tabf, const float2* __restrict__ unused, unsigned int* vmax,
+                      VpRef) {
   constexpr int Q = N / 16, NT = Q / 8;
   constexpr int KX = kept_kx_of(N);
   const uint32_t* __restrict__ tab = reinterpret_cast<const uint32_t*>(tabf);

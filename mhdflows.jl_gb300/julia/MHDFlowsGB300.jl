@@ -14,7 +14,7 @@ using FourierFlows
 import FourierFlows: stepforward!
 
 export GB300TimeStepper, gb300_updatevars!, sync_sol!, push_sol!, gb300_diagnostics, gb300_autotune!,
-       gb300_SetUpFk!
+       gb300_SetUpFk!, gb300_set_vp!, gb300_DivVCorrection!, gb300_DivBCorrection!, gb300_div_correction!
 
 const libmhdgb = get(ENV, "MHDGB_LIB", joinpath(@__DIR__, "..", "lib", "libmhdgb.so"))
 
@@ -30,6 +30,7 @@ struct MhdParams
   precision::Cint
   device::Cint
   hydro_only::Cint
+  vp::Cint
 end
 
 check(rc) = rc == 0 ? nothing : error(unsafe_string(ccall((:mhd_last_error, libmhdgb), Cstring, ())))
@@ -40,14 +41,14 @@ mutable struct GB300TimeStepper{T} <: FourierFlows.AbstractTimeStepper{T}
 end
 
 function GB300TimeStepper(grid, params, dt; scheme::Symbol = :RK4, device::Integer = 0,
-                          B_field::Bool = true, precision::Symbol = :FP32)
+                          B_field::Bool = true, precision::Symbol = :FP32, VP_method::Bool = false)
   grid.nx == grid.ny == grid.nz || error("GB300TimeStepper needs a cubic grid")
   prec = precision == :FP32 ? 0 : precision == :SPLIT_FP16 ? 1 : precision == :SPLIT_BF16 ? 2 :
          error("precision must be :FP32, :SPLIT_FP16 or :SPLIT_BF16")
   eta = B_field ? params.η : 0.0
   neta = B_field ? params.nη : 0
   p = MhdParams(grid.nx, grid.Lx, params.ν, eta, params.nν, neta, dt,
-                scheme == :RK4 ? 0 : 1, prec, device, B_field ? 0 : 1)
+                scheme == :RK4 ? 0 : 1, prec, device, B_field ? 0 : 1, VP_method ? 1 : 0)
   h = Ref{Ptr{Cvoid}}(C_NULL)
   check(ccall((:mhd_create, libmhdgb), Cint, (Ref{MhdParams}, Ref{Ptr{Cvoid}}), p, h))
   ts = GB300TimeStepper{Array{ComplexF32,4}}(h[], grid.nx)
@@ -107,5 +108,33 @@ gb300_autotune!(ts::GB300TimeStepper; force::Bool = false) =
 gb300_SetUpFk!(ts::GB300TimeStepper; kf = 2.0, P = 1.0, σ = 1.0, b = 1.0, seed::Integer = 0) =
   check(ccall((:mhd_set_forcing, libmhdgb), Cint,
               (Ptr{Cvoid}, Cdouble, Cdouble, Cdouble, Cdouble, Culonglong), ts.handle, P, kf, σ, b, seed))
+
+# Volume penalisation (VP_method = true): the library's copy of params.χ, params.U₀x..U₀z and
+# params.B₀x..B₀z (src/Structure/datastructure.jl:79-95).  Call after filling them, and again
+# whenever they change; U₀ / B₀ = nothing means zero walls.
+function gb300_set_vp!(ts::GB300TimeStepper, χ; U₀ = nothing, B₀ = nothing)
+  walls(t) = t === nothing ? C_NULL : vcat(vec(Array{Float32}(t[1])), vec(Array{Float32}(t[2])), vec(Array{Float32}(t[3])))
+  u, b = walls(U₀), walls(B₀)
+  GC.@preserve u b begin
+    check(ccall((:mhd_set_vp, libmhdgb), Cint, (Ptr{Cvoid}, Ptr{Float32}, Ptr{Float32}, Ptr{Float32}),
+                ts.handle, Array{Float32}(χ), u === C_NULL ? C_NULL : pointer(u), b === C_NULL ? C_NULL : pointer(b)))
+  end
+end
+gb300_set_vp!(prob) = gb300_set_vp!(prob.timestepper, prob.params.χ;
+                                    U₀ = (prob.params.U₀x, prob.params.U₀y, prob.params.U₀z),
+                                    B₀ = hasproperty(prob.params, :B₀x) ?
+                                         (prob.params.B₀x, prob.params.B₀y, prob.params.B₀z) : nothing)
+
+# DivVCorrection!(prob) / DivBCorrection!(prob) (src/Solver/VPSolver.jl:60-138) on the device state
+gb300_DivVCorrection!(ts::GB300TimeStepper) =
+  check(ccall((:mhd_div_correct, libmhdgb), Cint, (Ptr{Cvoid}, Cint), ts.handle, 1))
+gb300_DivBCorrection!(ts::GB300TimeStepper) =
+  check(ccall((:mhd_div_correct, libmhdgb), Cint, (Ptr{Cvoid}, Cint), ts.handle, 2))
+
+# Per-step corrections inside the library, as TimeIntegrator! does with VP after every
+# stepforward! (src/integrator.jl:118-122); a TimeIntegrator! that already calls
+# DivVCorrection! / DivBCorrection! itself leaves this off.
+gb300_div_correction!(ts::GB300TimeStepper, on::Bool) =
+  check(ccall((:mhd_set_div_correction, libmhdgb), Cint, (Ptr{Cvoid}, Cint), ts.handle, on ? 1 : 0))
 
 end # module

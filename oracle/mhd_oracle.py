@@ -147,8 +147,9 @@ def _delta(a, b):
     return 1 if a == b else 0
 
 
-def calcN_literal(N, sol, grid: Grid, nu, eta, nnu=0, neta=0, vars_out=None):
-    """Literal restatement of MHDcalcN! (src/pgen.jl:153-162); dealiases ``sol`` in place."""
+def calcN_literal(N, sol, grid: Grid, nu, eta, nnu=0, neta=0, vars_out=None, vp=None):
+    """Literal restatement of MHDcalcN! (src/pgen.jl:153-162); dealiases ``sol`` in place.
+    ``vp``: None or the volume-penalisation inputs (``add_vp``)."""
     g = grid
     g.dealias(sol)
     # MHDcalcN_advection! (src/Solver/MHDSolver.jl:333-338): vars <- ldiv!(rfftplan, copy(sol[f]))
@@ -174,6 +175,8 @@ def calcN_literal(N, sol, grid: Grid, nu, eta, nnu=0, neta=0, vars_out=None):
                     out += 1j * ks[i] * (_delta(a, j) - ka * ks[j] * g.invKrsq) * nlh
                     if i != j:
                         out += 1j * ks[j] * (_delta(a, i) - ka * ks[i] * g.invKrsq) * nlh
+        if vp is not None:  # src/Solver/MHDSolver.jl:85-88
+            vp_update(out, a, u, vp["chi"], vp.get("U0"), vp["dt"], g)
         uh = g.rfft(u[a])
         out += (-g.Krsq * nu_s * uh).astype(out.dtype)
         if nnu > 1:
@@ -187,11 +190,48 @@ def calcN_literal(N, sol, grid: Grid, nu, eta, nnu=0, neta=0, vars_out=None):
                 nl = u[a] * b[j] - b[a] * u[j]
                 nlh = g.rfft(nl)
                 out += 1j * ks[j] * nlh
+        if vp is not None:  # src/Solver/MHDSolver.jl:160-163
+            vp_update(out, a, b, vp["chi"], vp.get("B0"), vp["dt"], g)
         bh = g.rfft(b[a])
         out += (-g.Krsq * eta_s * bh).astype(out.dtype)
         if neta > 1:
             out += (-g.Krsq ** neta * eta_s * bh).astype(out.dtype)
     return N
+
+
+def vp_update(out, a, fields, chi, walls, dt, grid: Grid):
+    """VP_UᵢUpdate! / VP_BᵢUpdate! (src/Solver/VPSolver.jl:20-58) for component a:
+    out += -(δ_aj - k_j k_a / k^2) rfft(chi / eta (f_j - W_j)), eta = dt 13 / 7, summed over j.
+    ``walls`` is None (zero) or the three wall fields; physical arrays are (nz, ny, nx)."""
+    g = grid
+    eta_vp = dt * 13 / 7
+    ks = g.ks
+    for j in range(3):
+        w = 0.0 if walls is None else walls[j]
+        F = g.rfft(chi / eta_vp * (fields[j] - w))
+        out += (-(_delta(a, j) - ks[j] * ks[a] * g.invKrsq) * F).astype(out.dtype)
+
+
+def add_vp(N, sol_dealiased, grid: Grid, vp: dict):
+    """The penalty terms of both equations added to a right-hand side N, from the physical fields
+    of a dealiased state (``vp``: chi, dt and optional U0, B0)."""
+    v = [grid.irfft(sol_dealiased[f]) for f in range(6)]
+    for a in range(3):
+        vp_update(N[a], a, v[0:3], vp["chi"], vp.get("U0"), vp["dt"], grid)
+        vp_update(N[3 + a], a, v[3:6], vp["chi"], vp.get("B0"), vp["dt"], grid)
+    return N
+
+
+def div_correct(grid: Grid, sol, fields: int = 3):
+    """DivVCorrection! (fields & 1) and DivBCorrection! (fields & 2), src/Solver/VPSolver.jl:60-138:
+    phi = -i (k.X) / k^2, X -= i k phi, i.e. X loses k (k.X) / k^2 (1/k^2 = 0 at k = 0)."""
+    ks = grid.ks
+    for bit, off in ((1, 0), (2, 3)):
+        if fields & bit:
+            phi = (ks[0] * sol[off] + ks[1] * sol[off + 1] + ks[2] * sol[off + 2]) * grid.invKrsq
+            for a in range(3):
+                sol[off + a] -= ks[a] * phi
+    return sol
 
 
 def hermitian_kx0(grid: Grid, X):
@@ -210,7 +250,7 @@ def hermitian_kx0(grid: Grid, X):
     return Y
 
 
-def calcN_fast(N, sol, grid: Grid, nu, eta):
+def calcN_fast(N, sol, grid: Grid, nu, eta, vp=None):
     """Same RHS as ``calcN_literal`` with the six unique stress products transformed once.
 
     Used for larger FP64 checks; mathematically identical to the literal form (the diffusion
@@ -242,6 +282,8 @@ def calcN_fast(N, sol, grid: Grid, nu, eta):
             if j != a:
                 acc = acc + ks[j] * E[(a, j)]
         N[3 + a] = 1j * acc - g.Krsq * eta * H[3 + a]
+    if vp is not None:
+        add_vp(N, sol, g, vp)
     return N
 
 
@@ -270,12 +312,15 @@ class Stepper:
 
     # A99 forcing (add_a99_forcing): None or dict(A, kf_used, sigma2, b, seed)
     forcing = None
+    # volume penalisation (add_vp): None or dict(chi, U0=None, B0=None); eta uses the step's dt
+    vp = None
 
     def calcN(self, N, X, stage=0):
+        vp = None if self.vp is None else dict(self.vp, dt=self.dt)
         if self.literal:
-            calcN_literal(N, X, self.g, self.nu, self.eta, self.nnu, self.neta, self.vars)
+            calcN_literal(N, X, self.g, self.nu, self.eta, self.nnu, self.neta, self.vars, vp=vp)
         else:
-            calcN_fast(N, X, self.g, self.nu, self.eta)
+            calcN_fast(N, X, self.g, self.nu, self.eta, vp=vp)
         if self.forcing is not None:
             add_a99_forcing(N, self.g, self.forcing, 8 * self.step + stage)
         return N
