@@ -20,7 +20,7 @@ LIB_DIR = os.path.join(PKG_DIR, "lib")
 LIB_PATH = os.path.join(LIB_DIR, "libmhdgb.so")
 
 ARCH_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a"]
-NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-O2"]
+NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-O2,-pthread"]
 
 
 def _sources():
@@ -76,7 +76,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
                 print(res.stdout + res.stderr)
             objs.append(obj)
     tmp = LIB_PATH + ".tmp"
-    cmd = [nvcc, *ARCH_FLAGS, "-shared", "-o", tmp, *objs]
+    cmd = [nvcc, *ARCH_FLAGS, "-shared", "-o", tmp, *objs, "-Xcompiler", "-pthread"]
     res = subprocess.run(cmd, capture_output=True, text=True)
     if res.returncode != 0:
         raise RuntimeError("nvcc link failed:\n" + " ".join(cmd) + "\n" + res.stdout + res.stderr)

@@ -25,6 +25,8 @@
 #include <mutex>
 #include <new>
 #include <string>
+#include <thread>
+#include <utility>
 #include <vector>
 
 #include "../../include/mhdgb.h"
@@ -966,6 +968,35 @@ void* mapped_host(const void* p, size_t bytes) {
   return a0.devicePointer;
 }
 
+// Zero every element of a reference-layout state (nf, n, n, nkr) outside the retained band (the
+// complement of scatter_retained_kernel), on up to 16 host threads, plane by plane.  The alias
+// band of an axis is the contiguous frequency range [kp, n - kn): a plane with kz in it is all
+// zero; a kept plane has one block of alias rows and, in each kept row, the tail kx >= Kx.
+void zero_outside_retained(float2* ref, const Geom& g, int nf) {
+  const size_t nkr = g.n / 2 + 1, row = nkr * sizeof(float2), plane = (size_t)g.n * row;
+  const size_t za = (size_t)(g.n - g.kp - g.kn), tail = (nkr - g.kx) * sizeof(float2);
+  const int planes = nf * g.n;
+  auto zero_plane = [&](int q) {
+    char* p = reinterpret_cast<char*>(ref) + (size_t)q * plane;
+    const int fz = q % g.n;
+    if (kept_of_freq(g, fz) < 0) { std::memset(p, 0, plane); return; }
+    std::memset(p + (size_t)g.kp * row, 0, za * row);
+    for (int j = 0; j < g.k2; ++j) std::memset(p + (size_t)freq_of_kept(g, j) * row + g.kx * sizeof(float2), 0, tail);
+  };
+  // one thread per 16 MB to zero, at most 16 and at most the hardware threads
+  const size_t zero_bytes = (size_t)nf * g.n * plane - (size_t)nf * g.k2 * g.k2 * g.kx * sizeof(float2);
+  const unsigned hw = std::thread::hardware_concurrency();
+  const size_t want = std::max<size_t>(1, std::min<size_t>(16, zero_bytes >> 24));
+  const int nt = (int)std::min<size_t>(want, hw ? hw : 1);
+  auto work = [&](int t) {
+    for (int q = t; q < planes; q += nt) zero_plane(q);
+  };
+  std::vector<std::thread> pool;
+  for (int t = 1; t < nt; ++t) pool.emplace_back(work, t);
+  work(0);
+  for (auto& th : pool) th.join();
+}
+
 }  // namespace
 
 extern "C" {
@@ -994,12 +1025,28 @@ int mhd_slot_get_state(mhd_handle h, int slot, float* sol) {
   if (!sol) return fail(MHD_ERR_INVALID, "null sol");
   const float2* src = h->sol + slot * h->sz.state;
   const size_t bytes = h->ref_elems() * sizeof(float2);
-  float2* out = static_cast<float2*>(mapped_host(sol, bytes));  // scatter straight into mapped memory
-  if ((rc = h->launch(KC_OTHER, [&] {
-         scatter_state_kernel<<<1216, 256, 0, h->stream>>>(src, out ? out : h->ref, h->g, h->nfields());
-       })))
-    return rc;
-  if (!out) MHD_CUDA(cudaMemcpyAsync(sol, h->ref, bytes, cudaMemcpyDeviceToHost, h->stream));
+  float2* out = static_cast<float2*>(mapped_host(sol, bytes));
+  if (out && bytes < (size_t(16) << 20)) {
+    // small mapped buffers: the device writes every element
+    if ((rc = h->launch(KC_OTHER, [&] {
+           scatter_state_kernel<<<1216, 256, 0, h->stream>>>(src, out, h->g, h->nfields());
+         })))
+      return rc;
+  } else if (out) {
+    // mapped memory: the device writes the retained elements straight into it (29% of the bytes
+    // at any n) while host threads zero the rest, overlapping with whatever the stream still runs
+    if ((rc = h->launch(KC_OTHER, [&] {
+           scatter_retained_kernel<<<1216, 256, 0, h->stream>>>(src, out, h->g, h->nfields());
+         })))
+      return rc;
+    zero_outside_retained(reinterpret_cast<float2*>(sol), h->g, h->nfields());
+  } else {
+    if ((rc = h->launch(KC_OTHER, [&] {
+           scatter_state_kernel<<<1216, 256, 0, h->stream>>>(src, h->ref, h->g, h->nfields());
+         })))
+      return rc;
+    MHD_CUDA(cudaMemcpyAsync(sol, h->ref, bytes, cudaMemcpyDeviceToHost, h->stream));
+  }
   MHD_CUDA(cudaStreamSynchronize(h->stream));
   return MHD_OK;
 }

@@ -340,6 +340,22 @@ __global__ void scatter_state_kernel(const float2* __restrict__ S, float2* __res
   }
 }
 
+// Compact state -> the retained elements of the reference layout (kx < Kx, ky and kz kept),
+// 8-byte stores; every other element is zero and the caller fills it.
+__global__ void scatter_retained_kernel(const float2* __restrict__ S, float2* __restrict__ ref, Geom geo, int nf) {
+  const int nkr = geo.n / 2 + 1;
+  const long long total = (long long)nf * geo.k2 * geo.k2 * geo.kx;
+  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < total; p += (long long)gridDim.x * blockDim.x) {
+    const int x = (int)(p % geo.kx);
+    long long r = p / geo.kx;
+    const int jy = (int)(r % geo.k2); r /= geo.k2;
+    const int jz = (int)(r % geo.k2);
+    const int f = (int)(r / geo.k2);
+    const long long row = ((long long)f * geo.n + freq_of_kept(geo, jz)) * geo.n + freq_of_kept(geo, jy);
+    ref[row * nkr + x] = S[(((long long)f * geo.k2 + jz) * geo.k2 + jy) * geo.kxp + x];
+  }
+}
+
 // ------------------------------------------------------------------------------------------
 // Diagnostics.
 // ------------------------------------------------------------------------------------------

@@ -1,6 +1,8 @@
 """State transfer through page-locked host buffers (mhd_host_alloc): the gather / scatter kernels
 read and write the mapped buffer directly.  Results must equal the pageable-memory path bit for
-bit; a pageable buffer goes through the staging copy."""
+bit; a pageable buffer goes through the staging copy.  From 16 MB up, get_state into mapped
+memory writes only the retained band from the device and zeroes the rest on host threads
+(n = 96 and the HD n = 128 case); smaller buffers are written whole by the device (n = 32)."""
 import ctypes as C
 import math
 
@@ -51,3 +53,25 @@ def test_pageable_buffer_uses_staging(pkg, mo, lib):
     with pkg.Problem(pkg.GPU(0), nx=n, Lx=2 * math.pi, nu=1e-3, eta=1e-3, dt=1e-3) as prob:
         pkg._lib.check(lib.mhd_set_state(prob.handle, buf.ctypes.data))
         assert np.array_equal(prob.sol_c(), g.dealias(s.copy()))
+
+
+def test_pinned_hydrodynamic_state_overwrites_every_element(pkg, mo, lib):
+    """get_state into mapped memory: the device writes the rows with kept ky and kz, host threads
+    zero the rest; a (nkr, n, n, 3) HD buffer full of garbage comes back exact."""
+    n = 128
+    g = mo.Grid(n)
+    s = np.ascontiguousarray(mo.random_spectrum_state(g, seed=53).astype(np.complex64)[:3])
+    nbytes = s.nbytes
+    pin = _pinned(lib, pkg, nbytes)
+    try:
+        with pkg.Problem(pkg.GPU(0), nx=n, nu=1e-3, dt=1e-3, B_field=False) as prob:
+            prob.set_sol(s.T)
+            C.memset(pin, 0x7f, nbytes)
+            pkg._lib.check(lib.mhd_get_state(prob.handle, pin))
+            got = np.frombuffer((C.c_char * nbytes).from_address(pin.value), dtype=np.complex64).reshape(s.shape).copy()
+            assert np.array_equal(got, prob.sol_c())
+        full = np.zeros((6,) + s.shape[1:], np.complex64)
+        full[:3] = s
+        assert np.array_equal(got, g.dealias(full)[:3])
+    finally:
+        lib.mhd_host_free(pin)
