@@ -360,6 +360,24 @@ def run_gpu(args, rank, world, local, dist: Dist):
     el = time.perf_counter() - t0
     el_max = dist.max(el)
     e2e_value = dist.sum(float(n) ** 3 * ke) / el_max
+
+    # the e2e step's pieces, each call timed on its own (host clock, synchronised): set_state,
+    # step, get_state after an idle device, and step + get_state back to back
+    def piece(f, k=5):
+        f()
+        chk(lib.mhd_synchronize(h))
+        a = time.perf_counter()
+        for _ in range(k):
+            f()
+        chk(lib.mhd_synchronize(h))
+        return round((time.perf_counter() - a) / k * 1e3, 3)
+
+    e2e_pieces = {
+        "set_state_ms": piece(lambda: chk(lib.mhd_set_state(h, pin_in))),
+        "step_ms": piece(lambda: chk(lib.mhd_step(h, 1))),
+        "get_state_ms": piece(lambda: chk(lib.mhd_get_state(h, pin_out))),
+        "step_then_get_state_ms": piece(lambda: (chk(lib.mhd_step(h, 1)), chk(lib.mhd_get_state(h, pin_out)))),
+    }
     out_arr = np.frombuffer((C.c_char * nbytes).from_address(pin_out.value), dtype=np.complex64)
     finite = bool(np.isfinite(out_arr).all())
     chk(lib.mhd_host_free(pin_in))
@@ -385,7 +403,7 @@ def run_gpu(args, rank, world, local, dist: Dist):
     return {
         "value": value, "ms_per_step": ms_per_step, "p50_ms": p50, "p99_ms": p99, "launches": launches,
         "clocks": clocks, "top": top, "achieved": achieved, "bytes": b.value, "peak": peak, "peak_kind": peak_kind,
-        "kernels": kernels, "e2e": e2e_value, "e2e_bytes": nbytes, "e2e_steps": ke, "finite": finite,
+        "kernels": kernels, "e2e": e2e_value, "e2e_bytes": nbytes, "e2e_steps": ke, "e2e_pieces": e2e_pieces, "finite": finite,
         "secondary": secondary, "prof_ms": prof_ms, "variants": variants,
     }
 
@@ -490,7 +508,8 @@ def main():
                        "reasons": r["clocks"]["reasons"], "samples": r["clocks"]["samples"]},
             "e2e": {"value": r["e2e"], "unit": UNIT, "h2d_bytes_per_step": r["e2e_bytes"],
                     "d2h_bytes_per_step": r["e2e_bytes"], "steps": r["e2e_steps"],
-                    "path": "mhd_set_state(pinned host) + mhd_step(1) + mhd_get_state(pinned host)"},
+                    "path": "mhd_set_state(pinned host) + mhd_step(1) + mhd_get_state(pinned host)",
+                    "pieces": r["e2e_pieces"]},
             "gpu_launches": r["launches"],
             "roofline": {"bound": "hbm", "kernel": r["top"], "achieved": r["achieved"], "peak": r["peak"],
                          "unit": "GB/s", "frac": r["achieved"] / r["peak"], "peak_kind": r["peak_kind"],
