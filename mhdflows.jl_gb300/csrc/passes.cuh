@@ -162,25 +162,27 @@ __global__ void __launch_bounds__(TX * P0::G, MINB)
   constexpr int KP = kept_kx_of(N), KN = kept_kn_of(N);
   const int dR = (int)a.dR;  // row offsets inside one buffer fit 32 bits for n <= 512
   const int shift = (N - KP - KN) * dR;
-  // Tile index t = tx_t + tiles_x*(o + outer*(f + nf*inst)).  The grid-stride walk advances it
-  // by gridDim.x with a carrying mixed-radix add, so divisions happen once per CTA.
+  // Tile index t = tx_t + tiles_x*(f + nf*(o + outer*inst)): the outer index (z of the y passes)
+  // varies slowest, so the last tiles of a pass write the last outer planes, the part of its
+  // output still in L2 when the next pass starts.  The grid-stride walk advances t by gridDim.x
+  // with a carrying mixed-radix add, so divisions happen once per CTA.
   struct Cur { int tx, o, f, inst; };
   auto decompose = [&](int t) {
     Cur c;
     c.tx = t % w.tiles_x;
     int r = t / w.tiles_x;
-    c.o = r % w.outer;
-    r /= w.outer;
     c.f = r % w.nf;
-    c.inst = r / w.nf;
+    r /= w.nf;
+    c.o = r % w.outer;
+    c.inst = r / w.outer;
     return c;
   };
   const Cur gstep = decompose(gridDim.x);
   auto advance = [&](Cur c) {
     int carry;
     c.tx += gstep.tx; carry = c.tx >= w.tiles_x; if (carry) c.tx -= w.tiles_x;
-    c.o += gstep.o + carry; carry = c.o >= w.outer; if (carry) c.o -= w.outer;
     c.f += gstep.f + carry; carry = c.f >= w.nf; if (carry) c.f -= w.nf;
+    c.o += gstep.o + carry; carry = c.o >= w.outer; if (carry) c.o -= w.outer;
     c.inst += gstep.inst + carry;
     return c;
   };
@@ -328,18 +330,18 @@ __global__ void __launch_bounds__(TX * P0::G, MINB)
     Cur c;
     c.tx = t % w.tiles_x;
     int r = t / w.tiles_x;
-    c.o = r % w.outer;
-    r /= w.outer;
     c.f = r % w.nf;
-    c.inst = r / w.nf;
+    r /= w.nf;
+    c.o = r % w.outer;
+    c.inst = r / w.outer;
     return c;
   };
   const Cur gstep = decompose(gridDim.x);
   auto advance = [&](Cur c) {
     int carry;
     c.tx += gstep.tx; carry = c.tx >= w.tiles_x; if (carry) c.tx -= w.tiles_x;
-    c.o += gstep.o + carry; carry = c.o >= w.outer; if (carry) c.o -= w.outer;
     c.f += gstep.f + carry; carry = c.f >= w.nf; if (carry) c.f -= w.nf;
+    c.o += gstep.o + carry; carry = c.o >= w.outer; if (carry) c.o -= w.outer;
     c.inst += gstep.inst + carry;
     return c;
   };
@@ -582,8 +584,11 @@ __global__ void __launch_bounds__(GROUPS * XCfg<P>::TPG, MINB)
   constexpr int GPI = N * N / RPG;  // row groups per instance
   const long long ngroups = (long long)(*br.count) * GPI;
   const int chunks_row = 3 * kxp;  // 16-byte chunks of the six contiguous field rows (slot == kxp)
-  // first row of row group q, inside its instance's rowbuf
+  // first row of row group q, inside its instance's rowbuf.  Groups are taken from the last one
+  // down: the y pass before this kernel wrote the last z planes last (still in L2), and the y
+  // pass after it reads the first z planes first (written here last).
   auto group_rows = [&](long long q) {
+    q = ngroups - 1 - q;
     const int inst = (int)(q / GPI);
     return pool + br.list[inst] * istride + (q - (long long)inst * GPI) * RPG * rowstride;
   };
@@ -638,7 +643,7 @@ __global__ void __launch_bounds__(GROUPS * XCfg<P>::TPG, MINB)
         bb = max(bb, __shfl_xor_sync(0xffffffffu, bb, o));
       }
       if ((threadIdx.x & 31) == 0) {
-        const int inst = (int)(q / GPI);
+        const int inst = (int)((ngroups - 1 - q) / GPI);  // the instance of group_rows(q)
         atomicMax(vmax + 2 * br.list[inst], bu);
         atomicMax(vmax + 2 * br.list[inst] + 1, bb);
       }
@@ -649,9 +654,10 @@ __global__ void __launch_bounds__(GROUPS * XCfg<P>::TPG, MINB)
     float chi[VPM ? V : 1];
     const float* wrow = nullptr;
     if constexpr (VPM > 0) {
-      const int inst = (int)(q / GPI);
+      const long long qr = ngroups - 1 - q;  // the group group_rows(q) addresses
+      const int inst = (int)(qr / GPI);
       const long long s = br.list[inst];
-      const long long r = (q - (long long)inst * GPI) * RPG + rr;  // z n + y
+      const long long r = (qr - (long long)inst * GPI) * RPG + rr;  // z n + y
       const float* crow = vp.chi + s * vp.cs + r * N;
       if constexpr (VPM == 2) wrow = vp.wall + 6 * s * vp.cs + r * N;
 #pragma unroll
