@@ -197,13 +197,13 @@ std::string tune_file() {
   return "";
 }
 
-std::string tune_key(int device, int n, int prec, int vp) {
+std::string tune_key(int device, int n, int prec, int vp, int hd = 0) {
   cudaDeviceProp prop;
   if (cudaGetDeviceProperties(&prop, device) != cudaSuccess) return "";
   std::string name(prop.name);
   for (auto& c : name) if (c == '|' || c == '\n') c = ' ';
   return name + "|" + std::to_string(prop.multiProcessorCount) + "|" + std::to_string(n) + (prec ? "p" + std::to_string(prec) : "") +
-         (vp ? "v" + std::to_string(vp) : "");
+         (vp ? "v" + std::to_string(vp) : "") + (hd ? "h" : "");
 }
 
 std::vector<std::string> split_bar(const std::string& line) {
@@ -471,22 +471,23 @@ struct mhd_problem {
     // UᵢUpdate! starts by zeroing the velocity right-hand side: a hydrodynamic problem is unforced
     const bool f = forcing && !p.hydro_only, v = p.vp != 0;
     return launch(KC_RKEPI, [&] {
-      if (f && v) launch_epilogue<true, true>(op, grid, bx, a, br);
+      if (hd_form()) launch_epilogue<false, false, true>(op, grid, bx, a, br);
+      else if (f && v) launch_epilogue<true, true>(op, grid, bx, a, br);
       else if (f) launch_epilogue<true, false>(op, grid, bx, a, br);
       else if (v) launch_epilogue<false, true>(op, grid, bx, a, br);
       else launch_epilogue<false, false>(op, grid, bx, a, br);
     });
   }
   // record: the stage whose physical fields getCFL! reads (the last one of a step)
-  template <bool F, bool V>
+  template <bool F, bool V, bool H = false>
   void launch_epilogue(int op, dim3 grid, int bx, const RkArgs& a, BatchRef br) {
     switch (op) {
-      case OP_RHS: rk_epilogue_kernel<OP_RHS, F, V><<<grid, bx, 0, stream>>>(a, g, br); break;
-      case OP_RK4_FIRST: rk_epilogue_kernel<OP_RK4_FIRST, F, V><<<grid, bx, 0, stream>>>(a, g, br); break;
-      case OP_RK4_MID: rk_epilogue_kernel<OP_RK4_MID, F, V><<<grid, bx, 0, stream>>>(a, g, br); break;
-      case OP_RK4_LAST: rk_epilogue_kernel<OP_RK4_LAST, F, V><<<grid, bx, 0, stream>>>(a, g, br); break;
-      case OP_LS_FIRST: rk_epilogue_kernel<OP_LS_FIRST, F, V><<<grid, bx, 0, stream>>>(a, g, br); break;
-      default: rk_epilogue_kernel<OP_LS, F, V><<<grid, bx, 0, stream>>>(a, g, br); break;
+      case OP_RHS: rk_epilogue_kernel<OP_RHS, F, V, H><<<grid, bx, 0, stream>>>(a, g, br); break;
+      case OP_RK4_FIRST: rk_epilogue_kernel<OP_RK4_FIRST, F, V, H><<<grid, bx, 0, stream>>>(a, g, br); break;
+      case OP_RK4_MID: rk_epilogue_kernel<OP_RK4_MID, F, V, H><<<grid, bx, 0, stream>>>(a, g, br); break;
+      case OP_RK4_LAST: rk_epilogue_kernel<OP_RK4_LAST, F, V, H><<<grid, bx, 0, stream>>>(a, g, br); break;
+      case OP_LS_FIRST: rk_epilogue_kernel<OP_LS_FIRST, F, V, H><<<grid, bx, 0, stream>>>(a, g, br); break;
+      default: rk_epilogue_kernel<OP_LS, F, V, H><<<grid, bx, 0, stream>>>(a, g, br); break;
     }
   }
   // DivVCorrection! / DivBCorrection! of the slots in br (mask: 1 u, 2 B)
@@ -498,11 +499,12 @@ struct mhd_problem {
   // stage: right-hand-side evaluation within the step (7 outside a step)
   int rhs(const float2* X, int op, float hf, float ca, float cb, BatchRef br, int stage, bool record = false) {
     int rc;
-    if ((rc = z_inverse(X, ST(), 6, br))) return rc;
-    if ((rc = y_inverse(6, br))) return rc;
+    const int nin = hd_form() ? 3 : 6, nout = hd_form() ? 5 : ns;
+    if ((rc = z_inverse(X, ST(), nin, br))) return rc;
+    if ((rc = y_inverse(nin, br))) return rc;
     if ((rc = x_fused(br, (record && cfl) ? dvmax : nullptr))) return rc;
-    if ((rc = y_forward(ns, br))) return rc;
-    if ((rc = z_forward(rowbuf, sz.rowbuf, ns, br))) return rc;
+    if ((rc = y_forward(nout, br))) return rc;
+    if ((rc = z_forward(rowbuf, sz.rowbuf, nout, br))) return rc;
     return epilogue(X, op, hf, ca, cb, br, stage);
   }
   // One step of every active slot (launches only; see run_steps for graphs and clocks).
@@ -610,7 +612,7 @@ struct mhd_problem {
     if (profiling) return fail(MHD_ERR_STATE, "autotune does not run with per-kernel profiling enabled");
     int rc;
     if ((rc = sync_lists())) return rc;
-    const std::string key = tune_key(device, g.n, p.precision, ops->vp);
+    const std::string key = tune_key(device, g.n, p.precision, ops->vp, ops->hd);
     std::vector<std::string> names;
     if (!force && !key.empty() && tuned_lookup(key, &names) && apply_names(names) == MHD_OK) return MHD_OK;
     if (active.empty()) return fail(MHD_ERR_STATE, "autotune needs at least one active slot");
@@ -730,6 +732,9 @@ struct mhd_problem {
   // products enter the momentum at ~1e-14 relative).  Only the three velocity fields cross the
   // boundary.
   int nfields() const { return p.hydro_only ? 3 : 6; }
+  // the dedicated hydrodynamic passes (three fields in, five products out); hydrodynamics with
+  // volume penalisation runs the MHD passes with B = 0
+  bool hd_form() const { return p.hydro_only && !p.vp; }
   long long ref_elems() const { return sz.ref / 6 * nfields(); }
 };
 
@@ -792,12 +797,13 @@ int create_class(const mhd_params* params, int cap, mhd_handle* out) {
   if (!h->ops) return fail(MHD_ERR_INVALID, "no plan for n");
   h->ops->prec = params->precision;
   h->ops->vp_capable = params->vp != 0;
+  h->ops->hd = h->hd_form() ? 1 : 0;
   if ((rc = h->ops->setup(h->g))) return rc;
   if (params->vp && (rc = h->ops->set_vp(1))) return rc;  // mask only until walls are set
   {
     // a selection the autotuner made earlier for this device and grid size (this process or the
     // tuning file); the defaults otherwise
-    const std::string key = tune_key(h->device, h->g.n, params->precision, h->ops->vp);
+    const std::string key = tune_key(h->device, h->g.n, params->precision, h->ops->vp, h->ops->hd);
     std::vector<std::string> names;
     if (!key.empty() && tuned_lookup(key, &names)) h->apply_names(names);
   }
@@ -1398,15 +1404,17 @@ int mhd_kernel_class_bytes(mhd_handle h, int cls, double* bytes) {
   // state arrays (6 fields each) one epilogue launch touches, averaged over the scheme's stages
   const double arrays = h->p.scheme == MHD_RK4 ? (3 + 5 + 5 + 4) / 4.0 : (3 + 4 * 4) / 5.0;
   // out-going planes (8 products, 14 with the VP penalty fields) and the VP mask / wall reads
-  const double ns = h->ns;
+  // the hydrodynamic form moves 3 fields in and 5 products out (6 product slots leave x_fused)
+  const bool hd = h->hd_form();
+  const double ns = hd ? 5 : h->ns, nin = hd ? 3 : 6, xout = hd ? 6 : ns;
   const double vpin = h->p.vp ? (h->ops->vp == 2 ? 7.0 : 1.0) * n * n * n * 4.0 : 0.0;
   switch (cls) {
-    case KC_ZINV: b = 6 * (state_field + n * k2 * kx * c); break;
-    case KC_YINV: b = 6 * (n * k2 * kx * c + n * n * kx * c); break;
-    case KC_XFUSED: b = (6 + ns) * n * n * kx * c + vpin; break;
+    case KC_ZINV: b = nin * (state_field + n * k2 * kx * c); break;
+    case KC_YINV: b = nin * (n * k2 * kx * c + n * n * kx * c); break;
+    case KC_XFUSED: b = (nin + xout) * n * n * kx * c + vpin; break;
     case KC_YFWD: b = ns * (n * n * kx * c + n * k2 * kx * c); break;
     case KC_ZFWD: b = ns * (n * k2 * kx * c + state_field); break;
-    case KC_RKEPI: b = ns * state_field + arrays * 6 * state_field + 6 * k2 * k2 * c; break;
+    case KC_RKEPI: b = ns * state_field + arrays * nin * state_field + nin * k2 * k2 * c; break;
     case KC_HERM: b = 2 * 6 * k2 * k2 * c; break;
     default: b = 0;
   }

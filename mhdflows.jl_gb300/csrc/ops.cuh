@@ -54,6 +54,8 @@ struct XVariant {
   int prec = 0;
   // volume penalisation (x_fused_kernel's VPM): 0 none, 1 mask only, 2 mask and wall fields
   int vp = 0;
+  // hydrodynamic form (x_fused_kernel's HDX): three fields in, five products out
+  int hd = 0;
   size_t table_words = 0;
   int (*build_table)(uint32_t* table) = nullptr;
   uint32_t* table = nullptr;
@@ -87,6 +89,7 @@ class OpsBase {
   int prec = 0;  // precision form of the x rows (mhd_params.precision)
   int vp = 0;    // volume-penalisation form of the x rows (XVariant::vp)
   bool vp_capable = false;  // set before setup: prepare the penalty forms too
+  int hd = 0;    // set before setup: 1 selects the hydrodynamic x-row form (XVariant::hd)
   // switch the volume-penalisation form; the x-row class falls back to its first variant of the
   // new form (MHD_OK, or MHD_ERR_INVALID when this grid size has none)
   int set_vp(int mode);
@@ -194,6 +197,23 @@ class Ops : public OpsBase {
     v.tw = twiddles<R>();
     v.twr = twiddles<typename Reverse<R>::type>();
     v.vp = VPM;
+    xv.push_back(v);
+  }
+
+  // x rows of the hydrodynamic form (one transform per exchange round)
+  template <class R, int GROUPS, int MINB>
+  void add_x_hd() {
+    using XC = XCfg<R, 1>;
+    XVariant v;
+    v.name = "xhd:" + plan_name<R>() + "/nt11/c" + std::to_string(GROUPS) + "/b" + std::to_string(MINB);
+    v.fn = x_fused_kernel<R, GROUPS, 1, 1, MINB, 0, true>;
+    v.threads = GROUPS * XC::TPG;
+    v.rpg = XC::RPG;
+    v.groups = GROUPS;
+    v.group_words = &XC::group_words;
+    v.tw = twiddles<R>();
+    v.twr = twiddles<typename Reverse<R>::type>();
+    v.hd = 1;
     xv.push_back(v);
   }
 

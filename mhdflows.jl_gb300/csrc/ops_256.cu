@@ -23,6 +23,8 @@ OpsBase* make_ops_256() {
   o->add_x<Plan<256, 32, 8, 8, 4>, 8, 1, 1, 2>();
   o->add_x<Plan<256, 32, 8, 8, 4>, 2, 1, 1, 8>();
   o->add_x_vp<Plan<256, 32, 8, 8, 4>, 4, 1, 3>();
+  o->add_x_hd<Plan<256, 32, 8, 8, 4>, 8, 2>();
+  o->add_x_hd<Plan<256, 32, 8, 8, 4>, 4, 4>();
   o->add_x_tc<SPLIT_F16, 4, 2>();
   o->add_x_tc<SPLIT_BF16, 4, 2>();
   o->set_rows<Plan<256, 32, 8, 8, 4>, 4>();

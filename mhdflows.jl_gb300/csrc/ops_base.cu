@@ -52,6 +52,7 @@ int OpsBase::setup(const Geom& g) {
     x.ctas = 0;
     if (x.prec != prec || (int)x.smem > smem_max) continue;  // only this problem's precision form
     if (x.vp && !vp_capable) continue;                       // penalty forms only with VP on
+    if (x.hd != hd) continue;                                // this problem's field set only
     if (x.build_table) {
       e = cudaMalloc(&x.table, x.table_words * sizeof(uint32_t));
       if (e != cudaSuccess) return report_error(MHD_ERR_OOM, std::string("tensor-core tables: ") + cudaGetErrorString(e));
@@ -103,7 +104,7 @@ int OpsBase::variant_count(int cls) const {
 
 bool OpsBase::variant_ok(int cls, int i) const {
   if (i < 0 || i >= variant_count(cls)) return false;
-  if (cls == KC_XFUSED) return xv[i].ctas > 0 && xv[i].prec == prec && xv[i].vp == vp;
+  if (cls == KC_XFUSED) return xv[i].ctas > 0 && xv[i].prec == prec && xv[i].vp == vp && xv[i].hd == hd;
   return is_inv(cls) ? cv[i].ctas_inv > 0 : cv[i].ctas_fwd > 0;
 }
 

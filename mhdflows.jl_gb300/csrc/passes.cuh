@@ -455,7 +455,8 @@ __global__ void __launch_bounds__(TX * P0::G, MINB)
 // which is what a c2r transform does with a non-Hermitian kx = 0 plane.  Elements whose index
 // lies in the alias band for every lane are compile-time zeros, so the first stage of the
 // transform is pruned by constant folding.
-template <class P, int KX>
+// ZB: the second field is zero (f2 is not read).
+template <class P, int KX, bool ZB = false>
 __device__ __forceinline__ void load_herm_pair(float2 (&v)[P::V], const float2* __restrict__ f1,
                                                const float2* __restrict__ f2, int g) {
 #pragma unroll
@@ -467,12 +468,12 @@ __device__ __forceinline__ void load_herm_pair(float2 (&v)[P::V], const float2* 
       if (nmin < KX || nmin + P::G - 1 > P::N - KX) {  // some lane holds a kept mode
         const int n = g + nmin;
         if (n < KX) {
-          float2 a = f1[n], b = f2[n];
+          float2 a = f1[n], b = ZB ? make_float2(0.f, 0.f) : f2[n];
           if (n == 0) { a.y = 0.f; b.y = 0.f; }
           z = make_float2(a.x - b.y, a.y + b.x);
         } else if (n > P::N - KX) {
           const int m = P::N - n;
-          float2 a = f1[m], b = f2[m];
+          float2 a = f1[m], b = ZB ? make_float2(0.f, 0.f) : f2[m];
           z = make_float2(a.x + b.y, b.x - a.y);
         }
       }
@@ -558,7 +559,10 @@ struct XCfg {
 // VPM (volume penalisation, VP_UᵢUpdate! / VP_BᵢUpdate! of src/Solver/VPSolver.jl:20-58): 0 off;
 // 1 adds the penalty fields chi u and chi B (walls U0 = B0 = 0); 2 adds chi (u - U0), chi (B - B0).
 // They leave as three more forward pairs in slots 8..13; the epilogue scales and projects them.
-template <class P, int GROUPS, int NTI, int NTF, int MINB, int VPM = 0>
+// HDX (hydrodynamics, HDcalcN!): three fields in (ux uy | uz), B = 0 folded at compile time, two
+// inverse and three forward transforms; the products are the first five of the MHD set (the
+// sixth slot written is zero).
+template <class P, int GROUPS, int NTI, int NTF, int MINB, int VPM = 0, bool HDX = false>
 __global__ void __launch_bounds__(GROUPS * XCfg<P>::TPG, MINB)
     x_fused_kernel(float2* pool, Geom geo, long long rowstride, long long slot, long long istride, BatchRef br,
                    const float2* __restrict__ tw, const float2* __restrict__ twr, unsigned int* vmax, VpRef vp) {
@@ -569,7 +573,9 @@ __global__ void __launch_bounds__(GROUPS * XCfg<P>::TPG, MINB)
   static_assert(NTF == 1 || NTF == 2 || NTF == 4, "forward transforms go one, two or four at a time");
   static_assert(NTF == 1 || P::G <= 32, "batched forward transforms need the row inside one warp");
   static_assert(VPM == 0 || NTF == 1, "the penalty pairs go one at a time");
-  constexpr int NPAIR = VPM ? 7 : 4;  // forward transform pairs per row
+  static_assert(!HDX || (VPM == 0 && NTI == 1 && NTF == 1), "the hydrodynamic form is plain and one at a time");
+  constexpr int NPAIR = HDX ? 3 : VPM ? 7 : 4;  // forward transform pairs per row
+  constexpr int NINV = HDX ? 2 : 3;             // inverse transforms (field pairs) per row
   constexpr int G = P::G, V = P::V, N = P::N, RPG = XC::RPG, TPG = XC::TPG, TS = XC::TS;
   constexpr int KX = kept_kx_of(N);  // the host checks geo.kx == KX
   extern __shared__ float2 smem[];
@@ -583,7 +589,7 @@ __global__ void __launch_bounds__(GROUPS * XCfg<P>::TPG, MINB)
   const RowSync<G> sync{1 + grp};
   constexpr int GPI = N * N / RPG;  // row groups per instance
   const long long ngroups = (long long)(*br.count) * GPI;
-  const int chunks_row = 3 * kxp;  // 16-byte chunks of the six contiguous field rows (slot == kxp)
+  const int chunks_row = (HDX ? 3 : 6) * kxp / 2;  // 16-byte chunks of the contiguous field rows (slot == kxp)
   // first row of row group q, inside its instance's rowbuf.  Groups are taken from the last one
   // down: the y pass before this kernel wrote the last z planes last (still in L2), and the y
   // pass after it reads the first z planes first (written here last).
@@ -616,15 +622,25 @@ __global__ void __launch_bounds__(GROUPS * XCfg<P>::TPG, MINB)
     const float2* rin = cur + rr * 6 * kxp;
     float2 v[3][V];
 #pragma unroll
-    for (int t = 0; t < 3; ++t) load_herm_pair<P, KX>(v[t], rin + (2 * t) * kxp, rin + (2 * t + 1) * kxp, g);
+    for (int t = 0; t < NINV; ++t) {
+      if (HDX && t == 1) load_herm_pair<P, KX, true>(v[t], rin + (2 * t) * kxp, nullptr, g);
+      else load_herm_pair<P, KX>(v[t], rin + (2 * t) * kxp, rin + (2 * t + 1) * kxp, g);
+    }
     if constexpr (NTI == 3) {
       fft_run<P, +1, 3, TS, 1>(v, sb, 0, g, tw, sync);
       sync();
     } else {
 #pragma unroll
-      for (int t = 0; t < 3; ++t) {
+      for (int t = 0; t < NINV; ++t) {
         fft_run<P, +1, 1, TS, 1>(reinterpret_cast<float2(&)[1][V]>(v[t]), sb, 0, g, tw, sync);
         sync();
+      }
+    }
+    if constexpr (HDX) {  // B = 0: the second half of pair 1 is zero up to roundoff, pair 2 unused
+#pragma unroll
+      for (int i = 0; i < V; ++i) {
+        v[1][i].y = 0.f;
+        v[2][i] = make_float2(0.f, 0.f);
       }
     }
     if (vmax) {

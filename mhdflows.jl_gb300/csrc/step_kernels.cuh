@@ -121,8 +121,10 @@ __device__ __forceinline__ void rk_apply(const RkSlot& a, long long o, float2 x,
 }
 
 // grid (ceil(kx / blockDim.x), k2, k2): one thread per retained mode, no index division.
-template <int OP, bool FORCED, bool VPEN>
+// HD: the hydrodynamic form (three fields, five product planes; B is neither read nor written).
+template <int OP, bool FORCED, bool VPEN, bool HD = false>
 __global__ void __launch_bounds__(256) rk_epilogue_kernel(RkArgs a, Geom geo, BatchRef br) {
+  constexpr int NF = HD ? 3 : 6;
   const int x = blockIdx.x * blockDim.x + threadIdx.x;
   if (x >= geo.kx) return;
   const int inst = blockIdx.z / geo.k2;
@@ -142,15 +144,15 @@ __global__ void __launch_bounds__(256) rk_epilogue_kernel(RkArgs a, Geom geo, Ba
   const float k2 = kxv * kxv + kyv * kyv + kzv * kzv;
   float2 p[8];
 #pragma unroll
-  for (int q = 0; q < 8; ++q) p[q] = cscale(__ldcs(prod + q * fs + i), a.pscale);
+  for (int q = 0; q < 8; ++q) p[q] = (HD && q >= 5) ? make_float2(0.f, 0.f) : cscale(__ldcs(prod + q * fs + i), a.pscale);
   float2 xv[6], xd[6];
 #pragma unroll
-  for (int c = 0; c < 6; ++c) xv[c] = xd[c] = X[c * fs + i];
+  for (int c = 0; c < 6; ++c) xv[c] = xd[c] = c < NF ? X[c * fs + i] : make_float2(0.f, 0.f);
   if (x == 0) {
     const long long p = (long long)jz * geo.k2 + jy, pl = (long long)geo.k2 * geo.k2;
     const float2* H = a.H + slot * a.hI;
 #pragma unroll
-    for (int c = 0; c < 6; ++c) xd[c] = H[c * pl + p];
+    for (int c = 0; c < NF; ++c) xd[c] = H[c * pl + p];
   }
   const float2 dxz = p[0], dyz = p[1], txy = p[2], txz = p[3], tyz = p[4];
   const float2 axy = p[5], axz = p[6], ayz = p[7];
@@ -211,12 +213,12 @@ __global__ void __launch_bounds__(256) rk_epilogue_kernel(RkArgs a, Geom geo, Ba
       if (x == 0) R[c].y = 0.f;
     }
   }
-  if (a.hydro) {  // B = 0: only roundoff of the paired x-row transforms would feed it
+  if (!HD && a.hydro) {  // B = 0: only roundoff of the paired x-row transforms would feed it
 #pragma unroll
     for (int c = 3; c < 6; ++c) R[c] = make_float2(0.f, 0.f);
   }
 #pragma unroll
-  for (int c = 0; c < 6; ++c) rk_apply<OP>(rs, c * fs + i, xv[c], R[c]);
+  for (int c = 0; c < NF; ++c) rk_apply<OP>(rs, c * fs + i, xv[c], R[c]);
 }
 
 // Hermitian part of the kx = 0 plane of the six fields: H(k) = (X(k) + conj X(-k)) / 2, with

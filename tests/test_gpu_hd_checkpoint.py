@@ -55,6 +55,30 @@ def test_hd_steps_keep_b_zero_and_match_oracle(pkg, mo):
     assert d.E_B == 0.0 and d.H_c == 0.0 and d.max_kdotb == 0.0
 
 
+@pytest.mark.parametrize("n,scheme", [(128, "RK4"), (96, "LSRK4")])
+def test_hd_dedicated_passes_match_oracle(pkg, mo, n, scheme):
+    """The hydrodynamic passes (three fields in, five products out) at larger sizes: the RHS and
+    one step against the FP64 oracle with B = 0."""
+    g = mo.Grid(n)
+    s = _hd_state(mo, g, 33)
+    with pkg.Problem(pkg.GPU(0), nx=n, nu=1e-3, dt=5e-4, B_field=False, stepper=scheme) as prob:
+        prob.set_sol(s[:3].astype(np.complex64).T)
+        rhs = prob.rhs_c()
+        pkg.stepforward(prob, 1)
+        got = prob.sol_c()
+    m = g.retained_mask()
+    N = np.zeros_like(s)
+    mo.calcN_fast(N, s.astype(np.complex64).astype(np.complex128), g, 1e-3, 0.0)
+    e_rhs = mo.rel_l2(rhs, N[:3], m)
+    st = mo.Stepper(g, 1e-3, 0.0, 5e-4, scheme, literal=False)
+    ref = s.astype(np.complex64).astype(np.complex128)
+    st.stepforward(ref)
+    g.dealias(ref)
+    e_step = mo.rel_l2(got, ref[:3], m)
+    print(f"HD n={n} {scheme}: RHS {e_rhs:.3e}, one step {e_step:.3e} rel L2 vs FP64 oracle")
+    assert e_rhs < 1e-5 and e_step < 1e-5
+
+
 def test_hd_rejects_magnetic_fields(pkg):
     with pkg.Problem(pkg.GPU(0), nx=16, nu=1e-3, dt=1e-3, B_field=False) as prob:
         with pytest.raises(pkg.MHDError):
