@@ -224,7 +224,8 @@ def run_ensemble(args):
             "value": batched, "unit": UNIT, "steps": K, "warmup": args.warmup, "higher_is_better": True,
             "ms_per_ensemble_step": el / K * 1e3, "plain_one_at_a_time": seq, "speedup_vs_plain": batched / seq,
             "boxes": len(boxes), "grid_points": pts, "finite": finite, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": "batched ensemble (configs[3])", "scheme": "LSRK4", "dt": "0.2*dx/u_rms"}}
+            "config": {"workload": "batched ensemble: 24x32^3 + 20x48^3 + 12x64^3 + 8x96^3 boxes, one graph per step",
+                       "scheme": "LSRK4", "dt": "0.2*dx/u_rms"}}
 
 
 def run_serve(args):
@@ -257,7 +258,8 @@ def run_serve(args):
                                     "makespan_s": seq["makespan_s"]},
             "speedup_vs_plain": rep["grid_pt_steps_per_s"] / seq["grid_pt_steps_per_s"],
             "dtype": "f32", "data": "synthetic",
-            "config": {"workload": "serving loop (configs[4]), scaled", "requests": args.serve_count,
+            "config": {"workload": "serving loop: Poisson requests for N in {32,48,64,128,256}, continuous batching",
+                       "requests": args.serve_count,
                        "rate_per_s": 20.0, "steps": [lo, hi], "budget_gb": 150}}
 
 
