@@ -144,9 +144,10 @@ def measured_peaks():
         return 6800.0, "fallback"
 
 
-def ncu_traffic(cls_name: str, n: int):
-    """Per-launch DRAM bytes of a kernel class from a committed ncu summary, if any."""
-    path = os.path.join(ROOT, "profiles", f"{cls_name}_{n}.txt")
+def ncu_traffic(cls_name: str, n: int, form: str = ""):
+    """Per-launch DRAM bytes of a kernel class from a committed ncu summary of the same form
+    (plain MHD FP32: profiles/<class>_<n>.txt; others: profiles/<class>_<n>_<form>.txt), if any."""
+    path = os.path.join(ROOT, "profiles", f"{cls_name}_{n}{'_' + form if form else ''}.txt")
     if not os.path.exists(path):
         return None
     for line in open(path):
@@ -500,6 +501,8 @@ def main():
         cpu = cpu_baseline(args.n)
     if rank == 0:
         pub = args.n ** 3 / PUBLISHED_256_S_PER_STEP if args.n == 256 else None
+        # the ncu summary that matches this run's kernels (forcing changes only the epilogue)
+        form = "hd" if args.hydro and not args.vp else "vp" if args.vp else "" if args.precision == "fp32" else args.precision
         line = {
             "metric": METRIC, "value": r["value"], "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": r["ms_per_step"], "higher_is_better": True, "scaling": "weak",
@@ -515,7 +518,7 @@ def main():
             "gpu_launches": r["launches"],
             "roofline": {"bound": "hbm", "kernel": r["top"], "achieved": r["achieved"], "peak": r["peak"],
                          "unit": "GB/s", "frac": r["achieved"] / r["peak"], "peak_kind": r["peak_kind"],
-                         "traffic": ncu_traffic(r["top"], args.n), "algorithmic_bytes_per_launch": r["bytes"],
+                         "traffic": ncu_traffic(r["top"], args.n, form), "algorithmic_bytes_per_launch": r["bytes"],
                          "window": "CUDA events around every launch over K steps right after the timed region",
                          "window_ms_per_step": r["prof_ms"]},
             "kernels": r["kernels"],
