@@ -436,13 +436,14 @@ struct mhd_problem {
   }
   // Stage epilogue: RHS from the 8 compact product planes (in rowbuf; 14 with the VP penalty
   // fields) and the stage state X.
-  int epilogue(const float2* X, int op, float hf, float ca, float cb, BatchRef br, int stage) {
-    int rc = launch(KC_HERM, [&] {
+  int herm(const float2* X, BatchRef br) {
+    return launch(KC_HERM, [&] {
       const int bxh = g.k2 <= 256 ? (g.k2 + 31) / 32 * 32 : 256;
       const dim3 gh((g.k2 + bxh - 1) / bxh, g.k2, cap);
       herm_kx0_kernel<<<gh, bxh, 0, stream>>>(X, aux, g, FS(), ST(), FS(), br);
     });
-    if (rc) return rc;
+  }
+  RkArgs rk_args(const float2* X, int op, float hf, float ca, float cb, int stage) const {
     RkArgs a{};
     a.prod = rowbuf;
     a.X = X;
@@ -465,11 +466,18 @@ struct mhd_problem {
     const double n3 = (double)g.n * g.n * g.n;
     a.pscale = (float)(1.0 / (n3 * n3));
     a.vscale = (float)(1.0 / n3);
+    return a;
+  }
+  // HDcalcN! (src/pgen.jl:176-182) calls addforcing! before HDcalcN_advection!, whose UᵢUpdate!
+  // starts by zeroing the velocity right-hand side: a hydrodynamic problem is unforced
+  bool forced() const { return forcing && !p.hydro_only; }
+  int epilogue(const float2* X, int op, float hf, float ca, float cb, BatchRef br, int stage) {
+    int rc = herm(X, br);
+    if (rc) return rc;
+    const RkArgs a = rk_args(X, op, hf, ca, cb, stage);
     const int bx = g.kx <= 256 ? (g.kx + 31) / 32 * 32 : 256;
     const dim3 grid((g.kx + bx - 1) / bx, g.k2, g.k2 * cap);
-    // HDcalcN! (src/pgen.jl:176-182) calls addforcing! before HDcalcN_advection!, whose
-    // UᵢUpdate! starts by zeroing the velocity right-hand side: a hydrodynamic problem is unforced
-    const bool f = forcing && !p.hydro_only, v = p.vp != 0;
+    const bool f = forced(), v = p.vp != 0;
     return launch(KC_RKEPI, [&] {
       if (hd_form()) launch_epilogue<false, false, true>(op, grid, bx, a, br);
       else if (f && v) launch_epilogue<true, true>(op, grid, bx, a, br);
