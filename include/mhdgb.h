@@ -211,6 +211,13 @@ int mhd_get_forcing(mhd_handle h, int slot, double* A, double* kf_used);
  * TimeIntegrator! does with VP (src/integrator.jl:84-88,118-122); with the on-device CFL the next
  * dt then comes from the corrected fields, as getCFL! reads the corrected vars there.
  * VP needs precision MHD_PREC_FP32. */
+/* Failure detection: the device waits of the library (the TMA-fed passes' tile waits) are
+ * bounded; a wait that runs out records an error word, the kernel drains its own copies and
+ * returns, and mhd_synchronize reports MHD_ERR_CUDA.  mhd_check_bounded_wait exercises that path
+ * on `device` without a fault: one thread waits limit_ms (0 < limit_ms <= 1000) on an mbarrier
+ * nothing arrives on; *timed_out = 1 and *waited_ms the time it waited.  The context stays usable. */
+int mhd_check_bounded_wait(int device, double limit_ms, int* timed_out, double* waited_ms);
+
 #define MHD_DIV_U 1
 #define MHD_DIV_B 2
 int mhd_set_vp(mhd_handle h, const float* chi, const float* U0, const float* B0);

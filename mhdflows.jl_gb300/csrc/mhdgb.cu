@@ -1238,6 +1238,23 @@ int mhd_set_div_correction(mhd_handle h, int on) {
   return MHD_OK;
 }
 
+int mhd_check_bounded_wait(int device, double limit_ms, int* timed_out, double* waited_ms) {
+  if (!timed_out || !waited_ms) return fail(MHD_ERR_INVALID, "null output");
+  if (!(limit_ms > 0) || limit_ms > 1000) return fail(MHD_ERR_INVALID, "limit_ms must be in (0, 1000]");
+  MHD_CUDA(cudaSetDevice(device));
+  unsigned long long* d = nullptr;
+  MHD_CUDA(cudaMalloc(&d, 2 * sizeof(unsigned long long)));
+  bounded_wait_check_kernel<<<1, 32>>>((unsigned long long)(limit_ms * 1e6), d);
+  unsigned long long hbuf[2] = {0, 0};
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaMemcpy(hbuf, d, sizeof(hbuf), cudaMemcpyDeviceToHost);
+  cudaFree(d);
+  if (e != cudaSuccess) return fail(MHD_ERR_CUDA, std::string("bounded wait check: ") + cudaGetErrorString(e));
+  *timed_out = (int)hbuf[0];
+  *waited_ms = (double)hbuf[1] * 1e-6;
+  return MHD_OK;
+}
+
 int mhd_get_forcing(mhd_handle h, int slot, double* A, double* kf_used) {
   if (!h) return fail(MHD_ERR_INVALID, "null handle");
   if (!h->valid_slot(slot)) return fail(MHD_ERR_INVALID, "slot " + std::to_string(slot) + " is not active");

@@ -273,8 +273,9 @@ __device__ __forceinline__ unsigned long long global_ns() {
   asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
   return t;
 }
-// true when the barrier's phase `parity` completed within about a second
-__device__ __forceinline__ bool mbar_wait(unsigned int bar, unsigned int parity) {
+// true when the barrier's phase `parity` completed within limit_ns (about a second by default)
+__device__ __forceinline__ bool mbar_wait(unsigned int bar, unsigned int parity,
+                                          unsigned long long limit_ns = 1000000000ull) {
   const unsigned long long t0 = global_ns();
   while (true) {
     unsigned int done;
@@ -284,7 +285,7 @@ __device__ __forceinline__ bool mbar_wait(unsigned int bar, unsigned int parity)
         : "r"(bar), "r"(parity)
         : "memory");
     if (done) return true;
-    if (global_ns() - t0 > 1000000000ull) return false;
+    if (global_ns() - t0 > limit_ns) return false;
   }
 }
 __device__ __forceinline__ void tma_load5(unsigned int dst, const void* map, int c0, int c1, int c2, int c3, int c4,

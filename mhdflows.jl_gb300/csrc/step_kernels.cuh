@@ -300,6 +300,21 @@ __global__ void div_correct_kernel(float2* __restrict__ pool, Geom geo, long lon
   }
 }
 
+// Check of the bounded wait the TMA-fed passes use: one thread waits on an mbarrier that nothing
+// arrives on, with a limit of limit_ns, and records in out[0] whether the wait gave up (1) and in
+// out[1] the nanoseconds it waited.  The kernel then returns like a pass that timed out.
+__global__ void bounded_wait_check_kernel(unsigned long long limit_ns, unsigned long long* out) {
+  __shared__ __align__(8) unsigned long long bar;
+  if (threadIdx.x != 0) return;
+  const unsigned int b = smem_u32(&bar);
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(b) : "memory");
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  const unsigned long long t0 = global_ns();
+  const bool done = mbar_wait(b, 0u, limit_ns);
+  out[0] = done ? 0ull : 1ull;
+  out[1] = global_ns() - t0;
+}
+
 // max |x| over a float array via the ordered bit pattern of non-negative floats (NaN wins).
 __global__ void maxabs_kernel(const float* __restrict__ a, long long n, unsigned int* out) {
   unsigned int m = 0;

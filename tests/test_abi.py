@@ -58,6 +58,15 @@ def test_footprint(pkg, lib):
     assert pkg.footprint_bytes(512) > 7 * pkg.footprint_bytes(256)
 
 
+def test_bounded_wait_check_validates_arguments(pkg, lib):
+    import ctypes as C
+
+    t, ms = C.c_int(), C.c_double()
+    assert lib.mhd_check_bounded_wait(0, 0.0, C.byref(t), C.byref(ms)) == pkg._lib.MHD_ERR_INVALID
+    assert lib.mhd_check_bounded_wait(0, 2000.0, C.byref(t), C.byref(ms)) == pkg._lib.MHD_ERR_INVALID
+    assert lib.mhd_check_bounded_wait(0, 5.0, None, None) == pkg._lib.MHD_ERR_INVALID
+
+
 def test_null_handle_errors(pkg, lib):
     assert lib.mhd_step(None, 1) == pkg._lib.MHD_ERR_INVALID
     assert lib.mhd_destroy(None) == 0
