@@ -211,6 +211,18 @@ int mhd_get_forcing(mhd_handle h, int slot, double* A, double* kf_used);
  * TimeIntegrator! does with VP (src/integrator.jl:84-88,118-122); with the on-device CFL the next
  * dt then comes from the corrected fields, as getCFL! reads the corrected vars there.
  * VP needs precision MHD_PREC_FP32. */
+/* On-device diagnostics history: the getCFL! / increment!(diags) loop of TimeIntegrator!
+ * (src/integrator.jl:108-116, src/DiagnosticWrapper.jl:77-105) without host synchronisation.
+ * With freq > 0, every freq-th step of mhd_step (counted from this call) ends with the spectral
+ * diagnostics of every active slot, written on the device into the next of `capacity` samples
+ * (later samples are dropped); freq = 0 turns it off.  mhd_get_diag_history
+ * synchronises and copies up to max_samples samples of `slot`, 8 doubles each: handle step
+ * count, t, E_u, E_B, H_c, max|k.u|, max|k.B|, non-finite count (the quantities of
+ * mhd_diagnostics but max|div B|); *count is the number of samples stored so far (at most
+ * `capacity`). */
+int mhd_set_diag_history(mhd_handle h, int freq, int capacity);
+int mhd_get_diag_history(mhd_handle h, int slot, double* out, int max_samples, int* count);
+
 /* Failure detection: the device waits of the library (the TMA-fed passes' tile waits) are
  * bounded; a wait that runs out records an error word, the kernel drains its own copies and
  * returns, and mhd_synchronize reports MHD_ERR_CUDA.  mhd_check_bounded_wait exercises that path

@@ -32,7 +32,7 @@ __all__ = [
     "Diagnostics", "TimeIntegrator", "MHDError", "kept_modes", "supported_sizes", "footprint_bytes",
     "Batch", "Ensemble", "slot_bytes", "Diagnostic", "autotune", "variants", "select_variant",
     "TUNED_CLASSES", "PRECISIONS", "savefile", "Restart", "readMHDFlows", "checkpoint_path", "FIELDS",
-    "SetUpFk", "forcing_amplitude", "DivVCorrection", "DivBCorrection",
+    "SetUpFk", "forcing_amplitude", "DivVCorrection", "DivBCorrection", "HISTORY_COLUMNS",
 ]
 
 FIELDS = ("ux", "uy", "uz", "bx", "by", "bz")
@@ -105,6 +105,17 @@ def _vp_arrays(n, chi, U0, B0):
 
 def _ptr(a):
     return None if a is None else a.ctypes.data
+
+
+HISTORY_COLUMNS = ("step", "t", "E_u", "E_B", "H_c", "max_kdotu", "max_kdotb", "nonfinite")
+
+
+def _history(lib, h, slot):
+    n = C.c_int()
+    _lib.check(lib.mhd_get_diag_history(h, int(slot), None, 0, C.byref(n)))
+    out = np.zeros((max(n.value, 1), 8), dtype=np.float64)
+    _lib.check(lib.mhd_get_diag_history(h, int(slot), out.ctypes.data, n.value, C.byref(n)))
+    return out[: min(n.value, out.shape[0])] if n.value else out[:0]
 
 
 def footprint_bytes(n: int, L: float = 2 * math.pi, stepper: str = "RK4") -> int:
@@ -285,6 +296,15 @@ class Problem:
         a = np.ascontiguousarray(a, dtype=np.complex64)
         _lib.check(self._lib.mhd_set_state(self._h, a.ctypes.data))
 
+    def record_diagnostics(self, freq: int, capacity: int = 1024):
+        """Record the spectral diagnostics on the device every ``freq`` steps (0: off) into up to
+        ``capacity`` samples, without host synchronisation; read them with diagnostic_history."""
+        _lib.check(self._lib.mhd_set_diag_history(self._h, int(freq), int(capacity)))
+
+    def diagnostic_history(self):
+        """(samples, 8) float64: step, t, E_u, E_B, H_c, max|k.u|, max|k.B|, non-finite count."""
+        return _history(self._lib, self._h, 0)
+
     def set_vp(self, chi, U0=None, B0=None):
         """The volume-penalisation mask and walls, in place of writing params.χ, params.U₀x..U₀z and
         params.B₀x..B₀z (src/Structure/datastructure.jl:79-95): ``chi`` an (n, n, n) array indexed
@@ -428,13 +448,15 @@ class Diagnostic:
 
 
 def TimeIntegrator(prob: Problem, t0: float, N0: int, *, usr_dt: float = 0.0, CFL_Coef: float = 0.25,
-                   diags=()):
+                   diags=(), diag_freq: int = 0):
     """Stepping part of TimeIntegrator! (src/integrator.jl:31-156): runs while N0 >= step and
     t0 >= t, i.e. N0+1 steps from step 0 like the reference.  With usr_dt > 0 the step is fixed;
     with usr_dt = 0 getCFL! runs on the device before every step (dt = min(CFL_Coef dx / vmax,
     t_diff), src/integrator.jl:158-198) without host synchronisation.  Diagnostics are
-    incremented after every step (increment!(diags), src/integrator.jl:116).  Returns the zone
-    updates per second, the reference's own throughput figure (src/integrator.jl:150-153)."""
+    incremented after every step (increment!(diags), src/integrator.jl:116).  With diag_freq > 0
+    the spectral diagnostics are recorded on the device every diag_freq steps instead, with no host
+    round trip (prob.diagnostic_history() reads them).  Returns the zone updates per second, the
+    reference's own throughput figure (src/integrator.jl:150-153)."""
     import time
 
     vp = getattr(prob, "VP", False)
@@ -448,6 +470,8 @@ def TimeIntegrator(prob: Problem, t0: float, N0: int, *, usr_dt: float = 0.0, CF
     else:
         _lib.check(prob._lib.mhd_set_cfl(prob._h, 1, CFL_Coef))
     prob.clock.step = 0
+    if diag_freq > 0:
+        prob.record_diagnostics(diag_freq, (N0 + 1) // diag_freq + 1)
     if vp:  # src/integrator.jl:118-122: and after every step
         _lib.check(prob._lib.mhd_set_div_correction(prob._h, 1))
     start = time.perf_counter()
@@ -550,6 +574,14 @@ class Batch:
     def set_physical(self, slot: int, field: int, arr):
         a = np.ascontiguousarray(arr, dtype=np.float32)
         _lib.check(self._lib.mhd_slot_set_physical(self._h, int(slot), int(field), a.ctypes.data))
+
+    def record_diagnostics(self, freq: int, capacity: int = 1024):
+        """On-device diagnostics of every active slot every ``freq`` steps (Problem.record_diagnostics)."""
+        _lib.check(self._lib.mhd_set_diag_history(self._h, int(freq), int(capacity)))
+
+    def diagnostic_history(self, slot: int):
+        """(samples, 8) float64 of a slot, columns HISTORY_COLUMNS."""
+        return _history(self._lib, self._h, slot)
 
     def set_vp(self, slot: int, chi, U0=None, B0=None):
         """Volume-penalisation mask and walls of a slot (Problem.set_vp); needs VP_method=True."""

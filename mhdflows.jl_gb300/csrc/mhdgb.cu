@@ -322,6 +322,17 @@ struct mhd_problem {
   bool list_dirty = true;
   // step graph
   cudaGraphExec_t graph = nullptr;
+  // on-device diagnostics history: every diag_freq-th step of mhd_step ends with the batched
+  // diagnostics into sample *dhist_count (graph_diag is that step's graph); the host logs the
+  // step and clock of each sample as it launches them
+  int diag_freq = 0, diag_capacity = 0;
+  double* dhist = nullptr;
+  double* dhist_partial = nullptr;
+  int* dhist_count = nullptr;
+  long long hsteps = 0;
+  std::vector<long long> hist_step;
+  std::vector<std::vector<double>> hist_t;
+  cudaGraphExec_t graph_diag = nullptr;
   // profiling
   bool profiling = false;
   struct Rec { int cls; cudaEvent_t a, b; };
@@ -336,6 +347,9 @@ struct mhd_problem {
     cudaSetDevice(device);
     if (graph) cudaGraphExecDestroy(graph);
     graph = nullptr;
+    if (graph_diag) cudaGraphExecDestroy(graph_diag);
+    graph_diag = nullptr;
+    free_history();
     for (auto& r : recs) { cudaEventDestroy(r.a); cudaEventDestroy(r.b); }
     recs.clear();
     for (auto e : pool) cudaEventDestroy(e);
@@ -516,7 +530,7 @@ struct mhd_problem {
     return epilogue(X, op, hf, ca, cb, br, stage);
   }
   // One step of every active slot (launches only; see run_steps for graphs and clocks).
-  int issue_step() {
+  int issue_step(bool with_diag = false) {
     const BatchRef br = active_ref();
     int rc;
     if (p.scheme == MHD_RK4) {
@@ -538,8 +552,33 @@ struct mhd_problem {
       if ((rc = div_correct(br, cap, p.hydro_only ? 1 : 3))) return rc;
       if (cfl && (rc = cfl_prime())) return rc;
     }
-    if (cfl) return cfl_update(1);
+    if (cfl && (rc = cfl_update(1))) return rc;
+    if (with_diag) return record_diagnostics(br);
     return MHD_OK;
+  }
+  // the diagnostics of every active slot's state into the next history sample
+  int record_diagnostics(BatchRef br) {
+    int rc;
+    const int nb = sz.diag_blocks;
+    const double n3 = (double)g.n * g.n * g.n, dx = p.L / g.n;
+    const double scale = dx * dx * dx / n3;
+    if ((rc = launch(KC_OTHER, [&] {
+           diag_partial_batch_kernel<<<dim3(nb, cap), kDiagThreads, 0, stream>>>(sol, ST(), g, br, dhist_partial);
+         })))
+      return rc;
+    if ((rc = launch(KC_OTHER, [&] {
+           diag_record_kernel<<<cap, kDiagThreads, 0, stream>>>(dhist_partial, nb, br, cap, dhist, dhist_count,
+                                                                diag_capacity, cfl ? dtime : nullptr, scale);
+         })))
+      return rc;
+    return launch(KC_OTHER, [&] { hist_tick_kernel<<<1, 32, 0, stream>>>(dhist_count); });
+  }
+  void free_history() {
+    if (dhist) cudaFree(dhist);
+    if (dhist_partial) cudaFree(dhist_partial);
+    if (dhist_count) cudaFree(dhist_count);
+    dhist = dhist_partial = nullptr;
+    dhist_count = nullptr;
   }
   int cfl_update(int advance) {
     const float coef_dx = (float)(cfl_coef * p.L / g.n);
@@ -636,17 +675,18 @@ struct mhd_problem {
     invalidate_graph();
     return MHD_OK;
   }
-  int build_graph() {
-    if (graph) return MHD_OK;
+  int build_graph(bool with_diag = false) {
+    cudaGraphExec_t& out = with_diag ? graph_diag : graph;
+    if (out) return MHD_OK;
     cudaGraph_t gr = nullptr;
     MHD_CUDA(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
-    int rc = issue_step();
+    int rc = issue_step(with_diag);
     cudaError_t e = cudaStreamEndCapture(stream, &gr);
     if (rc) { if (gr) cudaGraphDestroy(gr); return rc; }
     if (e != cudaSuccess) return fail(MHD_ERR_CUDA, std::string("cudaStreamEndCapture: ") + cudaGetErrorString(e));
-    e = cudaGraphInstantiate(&graph, gr, 0);
+    e = cudaGraphInstantiate(&out, gr, 0);
     cudaGraphDestroy(gr);
-    if (e != cudaSuccess) { graph = nullptr; return fail(MHD_ERR_CUDA, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(e)); }
+    if (e != cudaSuccess) { out = nullptr; return fail(MHD_ERR_CUDA, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(e)); }
     return MHD_OK;
   }
   void advance_clocks() {
@@ -658,6 +698,8 @@ struct mhd_problem {
   void invalidate_graph() {
     if (graph) cudaGraphExecDestroy(graph);
     graph = nullptr;
+    if (graph_diag) cudaGraphExecDestroy(graph_diag);
+    graph_diag = nullptr;
     ++graph_version;
   }
   int run_steps(int nsteps) {
@@ -666,12 +708,21 @@ struct mhd_problem {
     if (active.empty()) return MHD_OK;
     if (!profiling && (rc = build_graph())) return rc;
     for (int i = 0; i < nsteps; ++i) {
+      const bool rec = diag_freq > 0 && (hsteps + 1) % diag_freq == 0;
       if (profiling) {
-        if ((rc = issue_step())) return rc;
+        if ((rc = issue_step(rec))) return rc;
       } else {
-        MHD_CUDA(cudaGraphLaunch(graph, stream));
+        if (rec && (rc = build_graph(true))) return rc;
+        MHD_CUDA(cudaGraphLaunch(rec ? graph_diag : graph, stream));
       }
       advance_clocks();
+      ++hsteps;
+      if (rec) {
+        hist_step.push_back(hsteps);
+        std::vector<double> tt(cap, 0.0);
+        for (int s2 : active) tt[s2] = t[s2];
+        hist_t.push_back(tt);
+      }
     }
     return MHD_OK;
   }
@@ -1234,6 +1285,57 @@ int mhd_set_div_correction(mhd_handle h, int on) {
     MHD_CUDA(cudaStreamSynchronize(h->stream));
     h->divcorr = on != 0;
     h->invalidate_graph();
+  }
+  return MHD_OK;
+}
+
+int mhd_set_diag_history(mhd_handle h, int freq, int capacity) {
+  int rc = check_handle(h);
+  if (rc) return rc;
+  if (freq < 0 || capacity < 0 || (freq > 0 && capacity < 1))
+    return fail(MHD_ERR_INVALID, "freq >= 0 and, with freq > 0, capacity >= 1 required");
+  MHD_CUDA(cudaStreamSynchronize(h->stream));
+  h->free_history();
+  h->hist_step.clear();
+  h->hist_t.clear();
+  h->hsteps = 0;
+  h->diag_freq = freq;
+  h->diag_capacity = freq > 0 ? capacity : 0;
+  if (freq > 0) {
+    const size_t c = (size_t)h->cap;
+    MHD_CUDA(cudaMalloc(&h->dhist, (size_t)capacity * c * kHistVals * sizeof(double)));
+    MHD_CUDA(cudaMalloc(&h->dhist_partial, c * h->sz.diag_blocks * kDiagSlots * sizeof(double)));
+    MHD_CUDA(cudaMalloc(&h->dhist_count, sizeof(int)));
+    MHD_CUDA(cudaMemsetAsync(h->dhist_count, 0, sizeof(int), h->stream));
+    MHD_CUDA(cudaStreamSynchronize(h->stream));
+  }
+  h->invalidate_graph();
+  return MHD_OK;
+}
+
+int mhd_get_diag_history(mhd_handle h, int slot, double* out, int max_samples, int* count) {
+  int rc = check_slot(h, slot);
+  if (rc) return rc;
+  if (!count || (max_samples > 0 && !out)) return fail(MHD_ERR_INVALID, "null output");
+  if (h->diag_freq <= 0) {
+    *count = 0;
+    return MHD_OK;
+  }
+  MHD_CUDA(cudaStreamSynchronize(h->stream));
+  int total = 0;
+  MHD_CUDA(cudaMemcpy(&total, h->dhist_count, sizeof(int), cudaMemcpyDeviceToHost));
+  const int stored = std::min(std::min(total, h->diag_capacity), (int)h->hist_step.size());
+  *count = stored;
+  const int n = std::min(stored, max_samples);
+  if (n <= 0) return MHD_OK;
+  std::vector<double> buf((size_t)n * h->cap * kHistVals);
+  MHD_CUDA(cudaMemcpy(buf.data(), h->dhist, buf.size() * sizeof(double), cudaMemcpyDeviceToHost));
+  for (int k = 0; k < n; ++k) {
+    const double* o = buf.data() + ((size_t)k * h->cap + slot) * kHistVals;
+    double* r = out + (size_t)k * 8;
+    r[0] = (double)h->hist_step[k];
+    r[1] = o[6] >= 0 ? o[6] : h->hist_t[k][slot];
+    for (int v = 0; v < 6; ++v) r[2 + v] = o[v];
   }
   return MHD_OK;
 }

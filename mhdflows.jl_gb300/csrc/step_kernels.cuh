@@ -255,6 +255,91 @@ __global__ void __launch_bounds__(kDiagThreads) diag_final_kernel(const double* 
   block_reduce_diag(acc, out);
 }
 
+// On-device diagnostics history (getCFL! / increment!(diags) without host synchronisation):
+// grid (blocks, cap), blockIdx.y = instance; the partial sums of slot s go to
+// partial[(s * gridDim.x + block) * kDiagSlots].
+__global__ void __launch_bounds__(kDiagThreads) diag_partial_batch_kernel(const float2* __restrict__ pool, long long stI,
+                                                                          Geom geo, BatchRef br, double* partial) {
+  const int inst = blockIdx.y;
+  if (inst >= *br.count) return;
+  const int slot = br.list[inst];
+  const float2* S = pool + slot * stI;
+  const long long plane = (long long)geo.k2 * geo.k2 * geo.kxp;
+  double acc[kDiagSlots] = {0, 0, 0, 0, 0, 0};
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < plane; i += (long long)gridDim.x * blockDim.x) {
+    const int x = (int)(i % geo.kxp);
+    if (x >= geo.kx) continue;
+    long long r = i / geo.kxp;
+    const int jy = (int)(r % geo.k2);
+    const int jz = (int)(r / geo.k2);
+    const double w = x == 0 ? 1.0 : 2.0;
+    const double kx = (double)geo.kscale * x;
+    const double ky = (double)geo.kscale * signed_of_kept(geo, jy);
+    const double kz = (double)geo.kscale * signed_of_kept(geo, jz);
+    double2 ku = make_double2(0, 0), kb = make_double2(0, 0);
+    double eu = 0, eb = 0, hc = 0;
+    bool bad = false;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      const float2 u = S[c * plane + i], b = S[(c + 3) * plane + i];
+      bad |= !isfinite(u.x) || !isfinite(u.y) || !isfinite(b.x) || !isfinite(b.y);
+      eu += (double)u.x * u.x + (double)u.y * u.y;
+      eb += (double)b.x * b.x + (double)b.y * b.y;
+      hc += (double)u.x * b.x + (double)u.y * b.y;
+      const double kc = c == 0 ? kx : (c == 1 ? ky : kz);
+      ku.x += kc * u.x; ku.y += kc * u.y;
+      kb.x += kc * b.x; kb.y += kc * b.y;
+    }
+    acc[0] += w * eu;
+    acc[1] += w * eb;
+    acc[2] += w * hc;
+    acc[3] = fmax(acc[3], sqrt(ku.x * ku.x + ku.y * ku.y));
+    acc[4] = fmax(acc[4], sqrt(kb.x * kb.x + kb.y * kb.y));
+    acc[5] += bad ? 1.0 : 0.0;
+  }
+  block_reduce_diag(acc, partial + ((long long)slot * gridDim.x + blockIdx.x) * kDiagSlots);
+}
+
+// grid (cap): one block per instance reduces its slot's partials (block order, deterministic)
+// into sample *count of the history: hist[(sample * cap + slot) * kHistVals + v] with v =
+// E_u, E_B, H_c (times scale = dV / n^3), max|k.u|, max|k.B|, non-finite count, device time
+// (dtime[slot], or -1 without the on-device clock).  Samples past `capacity` are counted, not
+// stored.  hist_tick_kernel advances the count after every slot has read it.
+constexpr int kHistVals = 7;
+__global__ void __launch_bounds__(kDiagThreads) diag_record_kernel(const double* __restrict__ partial, int nblocks, BatchRef br,
+                                                                   int cap, double* hist, const int* count, int capacity,
+                                                                   const double* dtime, double scale) {
+  const int inst = blockIdx.x;
+  if (inst >= *br.count) return;
+  const int slot = br.list[inst];
+  double acc[kDiagSlots] = {0, 0, 0, 0, 0, 0};
+  const double* p = partial + (long long)slot * nblocks * kDiagSlots;
+  for (int b = threadIdx.x; b < nblocks; b += blockDim.x) {
+#pragma unroll
+    for (int s = 0; s < kDiagSlots; ++s) {
+      const double x = p[b * kDiagSlots + s];
+      acc[s] = (s == 3 || s == 4) ? fmax(acc[s], x) : acc[s] + x;
+    }
+  }
+  __shared__ double red[kDiagSlots];
+  block_reduce_diag(acc, red);
+  __syncthreads();
+  const int sample = *count;
+  if (threadIdx.x == 0 && sample < capacity) {
+    double* o = hist + ((long long)sample * cap + slot) * kHistVals;
+    o[0] = red[0] * scale;
+    o[1] = red[1] * scale;
+    o[2] = red[2] * scale;
+    o[3] = red[3];
+    o[4] = red[4];
+    o[5] = red[5];
+    o[6] = dtime ? dtime[slot] : -1.0;
+  }
+}
+__global__ void hist_tick_kernel(int* count) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) *count += 1;
+}
+
 // i k.B into a one-field compact buffer (input of the div B inverse transform).
 __global__ void divb_spectrum_kernel(const float2* __restrict__ S, float2* __restrict__ out, Geom geo) {
   const long long plane = (long long)geo.k2 * geo.k2 * geo.kxp;

@@ -14,7 +14,8 @@ using FourierFlows
 import FourierFlows: stepforward!
 
 export GB300TimeStepper, gb300_updatevars!, sync_sol!, push_sol!, gb300_diagnostics, gb300_autotune!,
-       gb300_SetUpFk!, gb300_set_vp!, gb300_DivVCorrection!, gb300_DivBCorrection!, gb300_div_correction!
+       gb300_SetUpFk!, gb300_set_vp!, gb300_DivVCorrection!, gb300_DivBCorrection!, gb300_div_correction!,
+       gb300_record_diagnostics!, gb300_diagnostic_history
 
 const libmhdgb = get(ENV, "MHDGB_LIB", joinpath(@__DIR__, "..", "lib", "libmhdgb.so"))
 
@@ -136,5 +137,21 @@ gb300_DivBCorrection!(ts::GB300TimeStepper) =
 # DivVCorrection! / DivBCorrection! itself leaves this off.
 gb300_div_correction!(ts::GB300TimeStepper, on::Bool) =
   check(ccall((:mhd_set_div_correction, libmhdgb), Cint, (Ptr{Cvoid}, Cint), ts.handle, on ? 1 : 0))
+
+# increment!(diags) on the device: every `freq` steps the spectral diagnostics are written to a
+# device history of `capacity` samples, with no host synchronisation in the stepping loop.
+gb300_record_diagnostics!(ts::GB300TimeStepper, freq::Integer; capacity::Integer = 1024) =
+  check(ccall((:mhd_set_diag_history, libmhdgb), Cint, (Ptr{Cvoid}, Cint, Cint), ts.handle, freq, capacity))
+
+# (samples × 8) Float64: step, t, E_u, E_B, H_c, max|k·u|, max|k·B|, non-finite count
+function gb300_diagnostic_history(ts::GB300TimeStepper)
+  n = Ref{Cint}(0)
+  check(ccall((:mhd_get_diag_history, libmhdgb), Cint, (Ptr{Cvoid}, Cint, Ptr{Cdouble}, Cint, Ref{Cint}),
+              ts.handle, 0, C_NULL, 0, n))
+  out = zeros(Float64, 8, max(n[], 1))
+  check(ccall((:mhd_get_diag_history, libmhdgb), Cint, (Ptr{Cvoid}, Cint, Ptr{Cdouble}, Cint, Ref{Cint}),
+              ts.handle, 0, out, n[], n))
+  return permutedims(out[:, 1:n[]])
+end
 
 end # module
