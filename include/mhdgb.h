@@ -230,6 +230,11 @@ int mhd_get_diag_history(mhd_handle h, int slot, double* out, int max_samples, i
  * nothing arrives on; *timed_out = 1 and *waited_ms the time it waited.  The context stays usable. */
 int mhd_check_bounded_wait(int device, double limit_ms, int* timed_out, double* waited_ms);
 
+/* Memory-safety check: the large device buffers of a handle (states, pass buffers, staging, VP
+ * mask and walls) end in 4 KB guard bands filled with a fixed byte; *bad_bytes is the number of
+ * guard bytes some kernel overwrote (0 when every write stayed in bounds). */
+int mhd_check_guards(mhd_handle h, long long* bad_bytes);
+
 #define MHD_DIV_U 1
 #define MHD_DIV_B 2
 int mhd_set_vp(mhd_handle h, const float* chi, const float* U0, const float* B0);

@@ -111,6 +111,7 @@ _SIGS = {
     "mhd_set_div_correction": (C.c_int, [C.c_void_p, C.c_int]),
     "mhd_set_diag_history": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),
     "mhd_get_diag_history": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.POINTER(C.c_int)]),
+    "mhd_check_guards": (C.c_int, [C.c_void_p, C.POINTER(C.c_longlong)]),
     "mhd_check_bounded_wait": (C.c_int, [C.c_int, C.c_double, C.POINTER(C.c_int), C.POINTER(C.c_double)]),
     "mhd_autotune": (C.c_int, [C.c_void_p, C.c_int]),
     "mhd_variant_count": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_int)]),

@@ -322,6 +322,22 @@ struct mhd_problem {
   bool list_dirty = true;
   // step graph
   cudaGraphExec_t graph = nullptr;
+  // guard bands: every large buffer is allocated kGuardBytes longer and the tail filled with
+  // kGuardByte, so that a kernel writing past a buffer's end shows up in mhd_check_guards
+  static constexpr size_t kGuardBytes = 4096;
+  static constexpr unsigned char kGuardByte = 0xA5;
+  std::vector<std::pair<unsigned char*, size_t>> guards;
+  template <typename T>
+  cudaError_t alloc_guarded(T** p, size_t bytes) {
+    void* q = nullptr;
+    cudaError_t e = cudaMalloc(&q, bytes + kGuardBytes);
+    if (e != cudaSuccess) return e;
+    e = cudaMemset(static_cast<unsigned char*>(q) + bytes, kGuardByte, kGuardBytes);
+    if (e != cudaSuccess) { cudaFree(q); return e; }
+    *p = static_cast<T*>(q);
+    guards.emplace_back(static_cast<unsigned char*>(q) + bytes, kGuardBytes);
+    return cudaSuccess;
+  }
   // on-device diagnostics history: every diag_freq-th step of mhd_step ends with the batched
   // diagnostics into sample *dhist_count (graph_diag is that step's graph); the host logs the
   // step and clock of each sample as it launches them
@@ -359,6 +375,7 @@ struct mhd_problem {
     for (void* q : ptrs) if (q) cudaFree(q);
     vchi = vwall = nullptr;
     sol = xs = acc = aux = colbuf = rowbuf = ref = nullptr;
+    guards.clear();
     phys = nullptr; diag_partial = nullptr; diag_out = nullptr; maxabs = nullptr; dparams = nullptr; dlist = nullptr;
     dvmax = nullptr; dtime = nullptr; dstep = nullptr; derr = nullptr;
     if (own_stream) cudaStreamDestroy(own_stream);
@@ -870,14 +887,14 @@ int create_class(const mhd_params* params, int cap, mhd_handle* out) {
   h->stream = h->own_stream;
   const Sizes& s = h->sz;
   const size_t c = (size_t)cap;
-  MHD_CUDA(cudaMalloc(&h->sol, c * s.state * sizeof(float2)));
-  MHD_CUDA(cudaMalloc(&h->xs, c * s.state * sizeof(float2)));
-  MHD_CUDA(cudaMalloc(&h->acc, c * s.state * sizeof(float2)));
-  MHD_CUDA(cudaMalloc(&h->aux, c * s.fs * sizeof(float2)));
-  MHD_CUDA(cudaMalloc(&h->colbuf, c * s.colbuf * sizeof(float2)));
-  MHD_CUDA(cudaMalloc(&h->rowbuf, c * s.rowbuf * sizeof(float2)));
-  MHD_CUDA(cudaMalloc(&h->ref, s.ref * sizeof(float2)));
-  MHD_CUDA(cudaMalloc(&h->phys, s.phys * sizeof(float)));
+  MHD_CUDA(h->alloc_guarded(&h->sol, c * s.state * sizeof(float2)));
+  MHD_CUDA(h->alloc_guarded(&h->xs, c * s.state * sizeof(float2)));
+  MHD_CUDA(h->alloc_guarded(&h->acc, c * s.state * sizeof(float2)));
+  MHD_CUDA(h->alloc_guarded(&h->aux, c * s.fs * sizeof(float2)));
+  MHD_CUDA(h->alloc_guarded(&h->colbuf, c * s.colbuf * sizeof(float2)));
+  MHD_CUDA(h->alloc_guarded(&h->rowbuf, c * s.rowbuf * sizeof(float2)));
+  MHD_CUDA(h->alloc_guarded(&h->ref, s.ref * sizeof(float2)));
+  MHD_CUDA(h->alloc_guarded(&h->phys, s.phys * sizeof(float)));
   MHD_CUDA(cudaMalloc(&h->diag_partial, (size_t)s.diag_blocks * kDiagSlots * sizeof(double)));
   MHD_CUDA(cudaMalloc(&h->diag_out, 16 * sizeof(double)));
   MHD_CUDA(cudaMalloc(&h->maxabs, 16 * sizeof(unsigned int)));
@@ -895,8 +912,8 @@ int create_class(const mhd_params* params, int cap, mhd_handle* out) {
   MHD_CUDA(cudaMemsetAsync(h->xs, 0, c * s.state * sizeof(float2), h->stream));
   MHD_CUDA(cudaMemsetAsync(h->acc, 0, c * s.state * sizeof(float2), h->stream));
   if (params->vp) {
-    MHD_CUDA(cudaMalloc(&h->vchi, c * s.phys * sizeof(float)));
-    MHD_CUDA(cudaMalloc(&h->vwall, 6 * c * s.phys * sizeof(float)));
+    MHD_CUDA(h->alloc_guarded(&h->vchi, c * s.phys * sizeof(float)));
+    MHD_CUDA(h->alloc_guarded(&h->vwall, 6 * c * s.phys * sizeof(float)));
     MHD_CUDA(cudaMemsetAsync(h->vchi, 0, c * s.phys * sizeof(float), h->stream));
     MHD_CUDA(cudaMemsetAsync(h->vwall, 0, 6 * c * s.phys * sizeof(float), h->stream));
   }
@@ -1337,6 +1354,25 @@ int mhd_get_diag_history(mhd_handle h, int slot, double* out, int max_samples, i
     r[1] = o[6] >= 0 ? o[6] : h->hist_t[k][slot];
     for (int v = 0; v < 6; ++v) r[2 + v] = o[v];
   }
+  return MHD_OK;
+}
+
+int mhd_check_guards(mhd_handle h, long long* bad_bytes) {
+  int rc = check_handle(h);
+  if (rc) return rc;
+  if (!bad_bytes) return fail(MHD_ERR_INVALID, "null output");
+  MHD_CUDA(cudaStreamSynchronize(h->stream));
+  unsigned long long* d = nullptr;
+  MHD_CUDA(cudaMalloc(&d, sizeof(unsigned long long)));
+  MHD_CUDA(cudaMemset(d, 0, sizeof(unsigned long long)));
+  for (auto& gd : h->guards)
+    guard_check_kernel<<<(unsigned)((gd.second + 255) / 256), 256>>>(gd.first, (long long)gd.second, mhd_problem::kGuardByte, d);
+  unsigned long long bad = 0;
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaMemcpy(&bad, d, sizeof(bad), cudaMemcpyDeviceToHost);
+  cudaFree(d);
+  if (e != cudaSuccess) return fail(MHD_ERR_CUDA, std::string("guard check: ") + cudaGetErrorString(e));
+  *bad_bytes = (long long)bad;
   return MHD_OK;
 }
 

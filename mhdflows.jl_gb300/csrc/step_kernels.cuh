@@ -400,6 +400,15 @@ __global__ void bounded_wait_check_kernel(unsigned long long limit_ns, unsigned 
   out[1] = global_ns() - t0;
 }
 
+// Bytes of a guard band that differ from its fill value, added to *bad.
+__global__ void guard_check_kernel(const unsigned char* __restrict__ g, long long n, unsigned char fill,
+                                   unsigned long long* bad) {
+  const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  const unsigned int b = (i < n && g[i] != fill) ? 1u : 0u;
+  const unsigned int cnt = __popc(__ballot_sync(0xffffffffu, b));
+  if ((threadIdx.x & 31) == 0 && cnt) atomicAdd(bad, (unsigned long long)cnt);
+}
+
 // max |x| over a float array via the ordered bit pattern of non-negative floats (NaN wins).
 __global__ void maxabs_kernel(const float* __restrict__ a, long long n, unsigned int* out) {
   unsigned int m = 0;
