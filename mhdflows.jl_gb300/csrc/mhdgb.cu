@@ -129,15 +129,17 @@ Sizes sizes_of(const Geom& g, int ns) {
 
 // Device bytes of one slot (state, stage arrays, pass buffers; with VP the mask and the six wall
 // fields) and of the per-class staging.
-long long slot_bytes(const Geom& g, bool vp = false) {
-  Sizes s = sizes_of(g, slots_of(vp));
+long long slot_bytes(const Geom& g, bool vp = false, bool hydro = false) {
+  Sizes s = sizes_of(g, slots_of(vp && !hydro));
   return (3 * s.state + s.fs + s.colbuf + s.rowbuf) * 8 + 16 * 4 + (vp ? 7 * s.phys * 4 : 0);
 }
 long long class_bytes(const Geom& g) {
   Sizes s = sizes_of(g, 8);
   return s.ref * 8 + s.phys * 4 + 6LL * g.n * 8 + (long long)s.diag_blocks * kDiagSlots * 8 + 256;
 }
-long long footprint(const Geom& g, int cap, bool vp = false) { return class_bytes(g) + (long long)cap * slot_bytes(g, vp); }
+long long footprint(const Geom& g, int cap, bool vp = false, bool hydro = false) {
+  return class_bytes(g) + (long long)cap * slot_bytes(g, vp, hydro);
+}
 
 }  // namespace
 
@@ -510,7 +512,8 @@ struct mhd_problem {
     const dim3 grid((g.kx + bx - 1) / bx, g.k2, g.k2 * cap);
     const bool f = forced(), v = p.vp != 0;
     return launch(KC_RKEPI, [&] {
-      if (hd_form()) launch_epilogue<false, false, true>(op, grid, bx, a, br);
+      if (hd_form() && v) launch_epilogue<false, true, true>(op, grid, bx, a, br);
+      else if (hd_form()) launch_epilogue<false, false, true>(op, grid, bx, a, br);
       else if (f && v) launch_epilogue<true, true>(op, grid, bx, a, br);
       else if (f) launch_epilogue<true, false>(op, grid, bx, a, br);
       else if (v) launch_epilogue<false, true>(op, grid, bx, a, br);
@@ -538,7 +541,7 @@ struct mhd_problem {
   // stage: right-hand-side evaluation within the step (7 outside a step)
   int rhs(const float2* X, int op, float hf, float ca, float cb, BatchRef br, int stage, bool record = false) {
     int rc;
-    const int nin = hd_form() ? 3 : 6, nout = hd_form() ? 5 : ns;
+    const int nin = hd_form() ? 3 : 6, nout = hd_form() ? (p.vp ? 8 : 5) : ns;
     if ((rc = z_inverse(X, ST(), nin, br))) return rc;
     if ((rc = y_inverse(nin, br))) return rc;
     if ((rc = x_fused(br, (record && cfl) ? dvmax : nullptr))) return rc;
@@ -808,9 +811,9 @@ struct mhd_problem {
   // products enter the momentum at ~1e-14 relative).  Only the three velocity fields cross the
   // boundary.
   int nfields() const { return p.hydro_only ? 3 : 6; }
-  // the dedicated hydrodynamic passes (three fields in, five products out); hydrodynamics with
-  // volume penalisation runs the MHD passes with B = 0
-  bool hd_form() const { return p.hydro_only && !p.vp; }
+  // the dedicated hydrodynamic passes (three fields in, five products out; with volume
+  // penalisation also the three velocity penalty fields, in the spare slots 5..7)
+  bool hd_form() const { return p.hydro_only != 0; }
   long long ref_elems() const { return sz.ref / 6 * nfields(); }
 };
 
@@ -867,7 +870,7 @@ int create_class(const mhd_params* params, int cap, mhd_handle* out) {
   h->device = params->device;
   MHD_CUDA(cudaSetDevice(h->device));
   h->g = make_geom(params->n, params->L);
-  h->ns = slots_of(params->vp != 0);
+  h->ns = slots_of(params->vp != 0 && !params->hydro_only);
   h->sz = sizes_of(h->g, h->ns);
   h->ops.reset(make_ops(params->n));
   if (!h->ops) return fail(MHD_ERR_INVALID, "no plan for n");
@@ -967,7 +970,7 @@ int mhd_footprint_bytes(const mhd_params* params, long long* bytes) {
   int rc = validate(params);
   if (rc) return rc;
   if (!bytes) return fail(MHD_ERR_INVALID, "null output");
-  *bytes = footprint(make_geom(params->n, params->L), 1, params->vp != 0);
+  *bytes = footprint(make_geom(params->n, params->L), 1, params->vp != 0, params->hydro_only != 0);
   return MHD_OK;
 }
 
@@ -975,7 +978,7 @@ int mhd_slot_bytes(const mhd_params* params, long long* per_slot, long long* per
   int rc = validate(params);
   if (rc) return rc;
   const Geom g = make_geom(params->n, params->L);
-  if (per_slot) *per_slot = slot_bytes(g, params->vp != 0);
+  if (per_slot) *per_slot = slot_bytes(g, params->vp != 0, params->hydro_only != 0);
   if (per_class) *per_class = class_bytes(g);
   return MHD_OK;
 }
@@ -1515,7 +1518,7 @@ void* mhd_get_stream(mhd_handle h) { return h ? (void*)h->stream : nullptr; }
 
 int mhd_memory_bytes(mhd_handle h, long long* bytes) {
   if (!h || !bytes) return fail(MHD_ERR_INVALID, "null argument");
-  *bytes = footprint(h->g, h->cap, h->p.vp != 0);
+  *bytes = footprint(h->g, h->cap, h->p.vp != 0, h->p.hydro_only != 0);
   return MHD_OK;
 }
 
@@ -1567,10 +1570,12 @@ int mhd_kernel_class_bytes(mhd_handle h, int cls, double* bytes) {
   // state arrays (6 fields each) one epilogue launch touches, averaged over the scheme's stages
   const double arrays = h->p.scheme == MHD_RK4 ? (3 + 5 + 5 + 4) / 4.0 : (3 + 4 * 4) / 5.0;
   // out-going planes (8 products, 14 with the VP penalty fields) and the VP mask / wall reads
-  // the hydrodynamic form moves 3 fields in and 5 products out (6 product slots leave x_fused)
+  // the hydrodynamic form moves 3 fields in and 5 products out (6 product slots leave x_fused;
+  // with VP 8 slots, the penalty fields in 5..7)
   const bool hd = h->hd_form();
-  const double ns = hd ? 5 : h->ns, nin = hd ? 3 : 6, xout = hd ? 6 : ns;
-  const double vpin = h->p.vp ? (h->ops->vp == 2 ? 7.0 : 1.0) * n * n * n * 4.0 : 0.0;
+  const bool vp = h->p.vp != 0;
+  const double ns = hd ? (vp ? 8 : 5) : h->ns, nin = hd ? 3 : 6, xout = hd ? (vp ? 8 : 6) : ns;
+  const double vpin = vp ? (h->ops->vp == 2 ? (hd ? 4.0 : 7.0) : 1.0) * n * n * n * 4.0 : 0.0;
   switch (cls) {
     case KC_ZINV: b = nin * (state_field + n * k2 * kx * c); break;
     case KC_YINV: b = nin * (n * k2 * kx * c + n * n * kx * c); break;

@@ -200,13 +200,15 @@ class Ops : public OpsBase {
     xv.push_back(v);
   }
 
-  // x rows of the hydrodynamic form (one transform per exchange round)
-  template <class R, int GROUPS, int MINB>
+  // x rows of the hydrodynamic form (one transform per exchange round); VPM > 0 adds the
+  // velocity penalty fields (VP on hydrodynamics)
+  template <class R, int GROUPS, int MINB, int VPM = 0>
   void add_x_hd() {
     using XC = XCfg<R, 1>;
     XVariant v;
-    v.name = "xhd:" + plan_name<R>() + "/nt11/c" + std::to_string(GROUPS) + "/b" + std::to_string(MINB);
-    v.fn = x_fused_kernel<R, GROUPS, 1, 1, MINB, 0, true>;
+    v.name = std::string(VPM ? "xhdvp" + std::to_string(VPM) : "xhd") + ":" + plan_name<R>() + "/nt11/c" +
+             std::to_string(GROUPS) + "/b" + std::to_string(MINB);
+    v.fn = x_fused_kernel<R, GROUPS, 1, 1, MINB, VPM, true>;
     v.threads = GROUPS * XC::TPG;
     v.rpg = XC::RPG;
     v.groups = GROUPS;
@@ -214,7 +216,14 @@ class Ops : public OpsBase {
     v.tw = twiddles<R>();
     v.twr = twiddles<typename Reverse<R>::type>();
     v.hd = 1;
+    v.vp = VPM;
     xv.push_back(v);
+  }
+  // both penalisation forms (mask only, mask and walls) of the hydrodynamic x rows
+  template <class R, int GROUPS, int MINB>
+  void add_x_hdvp() {
+    add_x_hd<R, GROUPS, MINB, 1>();
+    add_x_hd<R, GROUPS, MINB, 2>();
   }
 
   // x rows on the tensor cores (split FP16 or BF16 operands), GROUPS warps (rows) per CTA

@@ -25,6 +25,7 @@ OpsBase* make_ops_256() {
   o->add_x_vp<Plan<256, 32, 8, 8, 4>, 4, 1, 3>();
   o->add_x_hd<Plan<256, 32, 8, 8, 4>, 8, 2>();
   o->add_x_hd<Plan<256, 32, 8, 8, 4>, 4, 4>();
+  o->add_x_hdvp<Plan<256, 32, 8, 8, 4>, 4, 3>();
   o->add_x_tc<SPLIT_F16, 4, 2>();
   o->add_x_tc<SPLIT_BF16, 4, 2>();
   o->set_rows<Plan<256, 32, 8, 8, 4>, 4>();

@@ -16,6 +16,7 @@ OpsBase* make_ops_512() {
   o->add_x<Plan<512, 32, 8, 8, 8>, 4, 1, 1, 2>();
   o->add_x_vp<Plan<512, 64, 8, 8, 8>, 2, 1, 4>();
   o->add_x_hd<Plan<512, 64, 8, 8, 8>, 2, 4>();
+  o->add_x_hdvp<Plan<512, 64, 8, 8, 8>, 2, 4>();
   o->add_x_tc<SPLIT_F16, 4, 2>();
   o->add_x_tc<SPLIT_BF16, 4, 2>();
   o->set_rows<Plan<512, 64, 8, 8, 8>, 2>();

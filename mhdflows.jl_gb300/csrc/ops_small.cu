@@ -9,6 +9,7 @@ OpsBase* make_ops_16() {
   o->add_x<Plan<16, 4, 4, 4>, 4, 1, 1, 4>();
   o->add_x_vp<Plan<16, 4, 4, 4>, 4, 1, 4>();
   o->add_x_hd<Plan<16, 4, 4, 4>, 4, 4>();
+  o->add_x_hdvp<Plan<16, 4, 4, 4>, 4, 4>();
   o->set_rows<Plan<16, 4, 4, 4>, 32>();
   return o;
 }
@@ -20,6 +21,7 @@ OpsBase* make_ops_32() {
   o->add_x<Plan<32, 4, 8, 4>, 4, 1, 1, 4>();
   o->add_x_vp<Plan<32, 4, 8, 4>, 4, 1, 4>();
   o->add_x_hd<Plan<32, 4, 8, 4>, 4, 4>();
+  o->add_x_hdvp<Plan<32, 4, 8, 4>, 4, 4>();
   o->set_rows<Plan<32, 4, 8, 4>, 32>();
   return o;
 }
@@ -31,6 +33,7 @@ OpsBase* make_ops_48() {
   o->add_x<Plan<48, 4, 12, 4>, 4, 1, 1, 2>();
   o->add_x_vp<Plan<48, 4, 12, 4>, 4, 1, 2>();
   o->add_x_hd<Plan<48, 4, 12, 4>, 4, 2>();
+  o->add_x_hdvp<Plan<48, 4, 12, 4>, 4, 2>();
   o->set_rows<Plan<48, 4, 12, 4>, 32>();
   return o;
 }
@@ -42,6 +45,7 @@ OpsBase* make_ops_64() {
   o->add_x<Plan<64, 8, 8, 8>, 4, 1, 1, 4>();
   o->add_x_vp<Plan<64, 8, 8, 8>, 4, 1, 3>();
   o->add_x_hd<Plan<64, 8, 8, 8>, 4, 4>();
+  o->add_x_hdvp<Plan<64, 8, 8, 8>, 4, 3>();
   o->set_rows<Plan<64, 8, 8, 8>, 16>();
   return o;
 }
@@ -53,6 +57,7 @@ OpsBase* make_ops_96() {
   o->add_x<Plan<96, 8, 12, 4, 2>, 4, 1, 1, 2>();
   o->add_x_vp<Plan<96, 8, 12, 4, 2>, 4, 1, 2>();
   o->add_x_hd<Plan<96, 8, 12, 4, 2>, 4, 2>();
+  o->add_x_hdvp<Plan<96, 8, 12, 4, 2>, 4, 2>();
   o->set_rows<Plan<96, 8, 12, 4, 2>, 16>();
   return o;
 }

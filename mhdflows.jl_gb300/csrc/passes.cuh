@@ -574,8 +574,11 @@ __global__ void __launch_bounds__(GROUPS * XCfg<P>::TPG, MINB)
   static_assert(NTF == 1 || NTF == 2 || NTF == 4, "forward transforms go one, two or four at a time");
   static_assert(NTF == 1 || P::G <= 32, "batched forward transforms need the row inside one warp");
   static_assert(VPM == 0 || NTF == 1, "the penalty pairs go one at a time");
-  static_assert(!HDX || (VPM == 0 && NTI == 1 && NTF == 1), "the hydrodynamic form is plain and one at a time");
-  constexpr int NPAIR = HDX ? 3 : VPM ? 7 : 4;  // forward transform pairs per row
+  static_assert(!HDX || (NTI == 1 && NTF == 1), "the hydrodynamic form goes one transform at a time");
+  // forward transform pairs per row; the hydrodynamic form with penalisation fills the three
+  // spare product slots: pair 2 = (-uy uz, n^3 chi (uz - U0z)), pair 3 = n^3 (chi (ux - U0x),
+  // chi (uy - U0y))
+  constexpr int NPAIR = HDX ? (VPM ? 4 : 3) : VPM ? 7 : 4;
   constexpr int NINV = HDX ? 2 : 3;             // inverse transforms (field pairs) per row
   constexpr int G = P::G, V = P::V, N = P::N, RPG = XC::RPG, TPG = XC::TPG, TS = XC::TS;
   constexpr int KX = kept_kx_of(N);  // the host checks geo.kx == KX
@@ -694,7 +697,18 @@ __global__ void __launch_bounds__(GROUPS * XCfg<P>::TPG, MINB)
         for (int i = 0; i < V; ++i) {
           const float ux = v[0][i].x, uy = v[0][i].y, uz = v[1][i].x;
           const float bx = v[1][i].y, by = v[2][i].x, bz = v[2][i].y;
-          if (t >= 4) {  // penalty pair t - 4: (u x, u y), (u z, B x), (B y, B z) of the field pairs
+          if (HDX && VPM > 0 && t >= 2) {
+            if constexpr (HDX && VPM > 0) {
+              constexpr float n3 = (float)N * (float)N * (float)N;
+              const int x = g + G * (i / P::RF) + P::LF * (i % P::RF);
+              auto wall = [&](int c) { return VPM == 2 ? n3 * __ldg(wrow + c * vp.cs + x) : 0.f; };
+              // scaled by n^3 to the products' magnitude (n^6 times physical): a pair whose halves
+              // differ by n^3 would lose the small half to the large one's rounding in the split
+              const float c3 = n3 * chi[i];
+              if (t == 2) w[j][i] = make_float2(-uy * uz, c3 * (uz - wall(2)));
+              else w[j][i] = make_float2(c3 * (ux - wall(0)), c3 * (uy - wall(1)));
+            }
+          } else if (t >= 4) {  // penalty pair t - 4: (u x, u y), (u z, B x), (B y, B z) of the field pairs
             if constexpr (VPM > 0) {
               float2 f = v[t - 4][i];
               if constexpr (VPM == 2) {  // the fields are n^3 times physical: so are the walls

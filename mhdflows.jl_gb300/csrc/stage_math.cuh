@@ -170,12 +170,18 @@ __device__ __forceinline__ void finish_mode(const RkArgs& a, const Geom& geo, in
   if constexpr (VPEN) {
     // VP_UᵢUpdate! / VP_BᵢUpdate! (src/Solver/VPSolver.jl:20-58): N_a += -(δ_aj - k_a k_j / k^2) F_j
     // with F = rfft(chi / eta (u - U0)) (and chi / eta (B - B0)), eta = 13 dt / 7, 1/k^2 = 0 at k = 0
-    const float sc = -a.vscale * 7.f / (13.f * sp.dt);
+    // MHD: the six penalty planes are 8..13 (u x, u y, u z, B x, B y, B z), n^3 times the
+    // reference's rfft; the hydrodynamic form keeps u in the spare product slots 6, 7, 5 (x, y, z)
+    // at the products' scale, n^6
+    const float sc = -(HD ? a.pscale : a.vscale) * 7.f / (13.f * sp.dt);
     float2 F[6];
 #pragma unroll
-    for (int q = 0; q < 6; ++q) F[q] = cscale(__ldcs(prod + (8 + q) * fs + i), sc);
+    for (int q = 0; q < 6; ++q) {
+      const int plane = HD ? (q == 0 ? 6 : q == 1 ? 7 : 5) : 8 + q;
+      F[q] = (HD && q >= 3) ? make_float2(0.f, 0.f) : cscale(__ldcs(prod + plane * fs + i), sc);
+    }
 #pragma unroll
-    for (int h = 0; h < 2; ++h) {
+    for (int h = 0; h < (HD ? 1 : 2); ++h) {
       const float2 f0 = F[3 * h], f1 = F[3 * h + 1], f2 = F[3 * h + 2];
       const float px = (kxv * f0.x + kyv * f1.x + kzv * f2.x) * ik2;
       const float py = (kxv * f0.y + kyv * f1.y + kzv * f2.y) * ik2;

@@ -32,6 +32,7 @@ def _exercise(pkg, prob, s, nf):
     (48, dict(stepper="LSRK4")),
     (96, dict(B_field=False)),
     (64, dict(VP_method=True)),
+    (48, dict(VP_method=True, B_field=False)),
     (128, dict(precision="split_fp16")),
     (256, {}),
 ])

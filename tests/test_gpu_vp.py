@@ -85,34 +85,36 @@ def test_vp_steps_match_oracle(pkg, mo, scheme, steps):
     assert err < 1e-5, err
 
 
-def test_vp_hydrodynamic(pkg, mo):
-    n, dt = 32, 1e-3
+@pytest.mark.parametrize("n,walls,scheme", [(32, True, "RK4"), (48, False, "LSRK4"), (128, True, "RK4")])
+def test_vp_hydrodynamic(pkg, mo, n, walls, scheme):
+    """VP on the hydrodynamic passes: the velocity penalty fields ride in the spare product slots."""
+    dt = 1e-3
     g = mo.Grid(n)
     s = _state(mo, g, 63, hydro=True)
     chi = _mask(g)
-    U0 = _walls(g, 4)
-    with pkg.Problem(pkg.GPU(0), nx=n, nu=2e-3, dt=dt, B_field=False, VP_method=True) as prob:
+    U0 = _walls(g, 4) if walls else None
+    with pkg.Problem(pkg.GPU(0), nx=n, nu=2e-3, dt=dt, B_field=False, VP_method=True, stepper=scheme) as prob:
         prob.set_sol(s[:3].T)
         prob.set_vp(chi.T, U0=_T(U0))
         got_rhs = prob.rhs_c()
         pkg.stepforward(prob, 2)
         got = prob.sol_c()
         d = prob.diagnostics()
-    vp = dict(chi=chi.astype(np.float64), U0=tuple(a.astype(np.float64) for a in U0))
+    vp = dict(chi=chi.astype(np.float64), U0=None if U0 is None else tuple(a.astype(np.float64) for a in U0))
     N = np.zeros(s.shape, dtype=np.complex128)
-    mo.calcN_literal(N, s.astype(np.complex128), g, 2e-3, 0.0, vp=dict(vp, dt=dt))
+    mo.calcN_fast(N, s.astype(np.complex128), g, 2e-3, 0.0, vp=dict(vp, dt=dt))
     m = g.retained_mask()
     e_rhs = mo.rel_l2(got_rhs, N[:3], m)
-    print(f"VP HD RHS rel L2 vs FP64 oracle: {e_rhs:.3e}")
+    print(f"VP HD n={n} walls={walls} RHS rel L2 vs FP64 oracle: {e_rhs:.3e}")
     assert e_rhs < 1e-5, e_rhs
-    st = mo.Stepper(g, 2e-3, 0.0, dt, "RK4", literal=False)
+    st = mo.Stepper(g, 2e-3, 0.0, dt, scheme, literal=False)
     st.vp = vp
     ref = s.astype(np.complex128)
     for _ in range(2):
         st.stepforward(ref)
     g.dealias(ref)
     err = mo.rel_l2(got, ref[:3], m)
-    print(f"VP HD two RK4 steps rel L2 vs FP64 oracle: {err:.3e}")
+    print(f"VP HD n={n} two {scheme} steps rel L2 vs FP64 oracle: {err:.3e}")
     assert err < 1e-5, err
     assert d.E_B == 0.0
 
