@@ -245,6 +245,14 @@ def run_serve(args):
         r.init_state = initial_state(r.n, r.seed)
     srv = serving.Server(serving.GpuBackend(pkg, "RK4"), budget_bytes=150e9, steps_per_tick=8)
     rep = srv.run(reqs, realtime=True)
+    nat_reqs = mk()  # the same stream through the C++ scheduler (mhd_server_*)
+    for r, q in zip(nat_reqs, reqs):
+        r.init_state = q.init_state
+    nat = serving.NativeServer(pkg, budget_bytes=150e9, steps_per_tick=8)
+    try:
+        nrep = nat.run(nat_reqs, realtime=True)
+    finally:
+        nat.close()
     seq_reqs = mk()
     for r, q in zip(seq_reqs, reqs):
         r.init_state = q.init_state
@@ -258,6 +266,11 @@ def run_serve(args):
                                     "p50_latency_s": seq["p50_latency_s"], "p99_latency_s": seq["p99_latency_s"],
                                     "makespan_s": seq["makespan_s"]},
             "speedup_vs_plain": rep["grid_pt_steps_per_s"] / seq["grid_pt_steps_per_s"],
+            "native_scheduler": {"grid_pt_steps_per_s": nrep["grid_pt_steps_per_s"],
+                                 "p50_latency_s": nrep["p50_latency_s"], "p99_latency_s": nrep["p99_latency_s"],
+                                 "makespan_s": nrep["makespan_s"], "done": nrep["done"],
+                                 "peak_active": nrep.get("peak_active"),
+                                 "peak_reserved_gb": nrep.get("peak_reserved_bytes", 0) / 1e9},
             "dtype": "f32", "data": "synthetic",
             "config": {"workload": "serving loop: Poisson requests for N in {32,48,64,128,256}, continuous batching",
                        "requests": args.serve_count,

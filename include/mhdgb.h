@@ -168,6 +168,51 @@ int mhd_slot_diagnostics(mhd_handle h, int slot, double* out, int nout);
 int mhd_slot_get_clock(mhd_handle h, int slot, double* t, long long* step, double* dt);
 int mhd_slot_set_clock(mhd_handle h, int slot, double t, long long step, double dt);
 
+/* Serving: a continuous-batching scheduler over size classes (no counterpart in the reference,
+ * which runs one problem per process).  Requests of any supported n queue in arrival order; a
+ * request is admitted when its size class has a free slot or a new class fits the device-memory
+ * budget (first fit), runs in the same launches as every other active solve of its class, and
+ * retires with its diagnostics (and its final state when keep_states) when its steps are done.
+ * The caller drives it: mhd_server_tick admits what fits, advances every active solve by
+ * min(steps_per_tick, the smallest remaining step count) and retires the finished ones.
+ * A request whose class can never fit the budget, whose class allocation fails, or whose initial
+ * state is not finite is rejected / failed alone; mhd_server_cancel frees a slot at once. */
+typedef struct mhd_server_s* mhd_server;
+typedef struct mhd_server_params {
+  double budget_bytes;   /* device memory the size classes may reserve */
+  int steps_per_tick;    /* upper bound of the steps one tick advances */
+  int scheme;            /* MHD_RK4 or MHD_LSRK4, for every request */
+  int device;
+  int keep_states;       /* 1: keep each finished request's final state for mhd_server_result */
+  int capacity[8];       /* slots per class for n = 16, 32, 48, 64, 96, 128, 256, 512 (0: default) */
+} mhd_server_params;
+typedef struct mhd_request {
+  int n;                 /* grid size (cubic box of side L) */
+  double L, nu, eta;
+  double dt;             /* <= 0: 0.2 * L / n */
+  long long steps;
+  const float* sol;      /* initial state, mhd_set_state layout (nkr, n, n, 6); copied at submit */
+} mhd_request;
+#define MHD_REQ_QUEUED 0
+#define MHD_REQ_ACTIVE 1
+#define MHD_REQ_DONE 2
+#define MHD_REQ_FAILED 3
+#define MHD_REQ_REJECTED 4
+#define MHD_REQ_CANCELLED 5
+int mhd_server_create(const mhd_server_params* params, mhd_server* out);
+int mhd_server_destroy(mhd_server s);
+int mhd_server_submit(mhd_server s, const mhd_request* req, long long* rid);
+/* one scheduling round; *active and *queued count the requests in those states afterwards */
+int mhd_server_tick(mhd_server s, int* active, int* queued);
+int mhd_server_poll(mhd_server s, long long rid, int* status, long long* steps_done);
+/* diag: 8 doubles as mhd_diagnostics (done or failed requests); sol: the final state (done
+ * requests with keep_states; may be NULL); the message of a failed / rejected request goes to
+ * mhd_last_error */
+int mhd_server_result(mhd_server s, long long rid, double* diag, float* sol);
+int mhd_server_cancel(mhd_server s, long long rid);
+/* device bytes reserved by the server's size classes now, and the peak so far */
+int mhd_server_memory(mhd_server s, double* reserved, double* peak);
+
 /* Ensembles of size classes stepped together: one CUDA graph holds one step of every member,
  * each member on its own stream, so boxes of different sizes run concurrently. */
 int mhd_ensemble_create(mhd_handle* handles, int count, mhd_ensemble* out);

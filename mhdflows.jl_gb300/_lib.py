@@ -55,6 +55,29 @@ class MhdParams(C.Structure):
     ]
 
 
+class MhdServerParams(C.Structure):
+    _fields_ = [
+        ("budget_bytes", C.c_double),
+        ("steps_per_tick", C.c_int),
+        ("scheme", C.c_int),
+        ("device", C.c_int),
+        ("keep_states", C.c_int),
+        ("capacity", C.c_int * 8),
+    ]
+
+
+class MhdRequest(C.Structure):
+    _fields_ = [
+        ("n", C.c_int),
+        ("L", C.c_double),
+        ("nu", C.c_double),
+        ("eta", C.c_double),
+        ("dt", C.c_double),
+        ("steps", C.c_longlong),
+        ("sol", C.c_void_p),
+    ]
+
+
 _SIGS = {
     "mhd_create": (C.c_int, [C.POINTER(MhdParams), C.POINTER(C.c_void_p)]),
     "mhd_destroy": (C.c_int, [C.c_void_p]),
@@ -112,6 +135,14 @@ _SIGS = {
     "mhd_set_diag_history": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),
     "mhd_get_diag_history": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.POINTER(C.c_int)]),
     "mhd_check_guards": (C.c_int, [C.c_void_p, C.POINTER(C.c_longlong)]),
+    "mhd_server_create": (C.c_int, [C.POINTER(MhdServerParams), C.POINTER(C.c_void_p)]),
+    "mhd_server_destroy": (C.c_int, [C.c_void_p]),
+    "mhd_server_submit": (C.c_int, [C.c_void_p, C.POINTER(MhdRequest), C.POINTER(C.c_longlong)]),
+    "mhd_server_tick": (C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
+    "mhd_server_poll": (C.c_int, [C.c_void_p, C.c_longlong, C.POINTER(C.c_int), C.POINTER(C.c_longlong)]),
+    "mhd_server_result": (C.c_int, [C.c_void_p, C.c_longlong, C.c_void_p, C.c_void_p]),
+    "mhd_server_cancel": (C.c_int, [C.c_void_p, C.c_longlong]),
+    "mhd_server_memory": (C.c_int, [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     "mhd_check_bounded_wait": (C.c_int, [C.c_int, C.c_double, C.POINTER(C.c_int), C.POINTER(C.c_double)]),
     "mhd_autotune": (C.c_int, [C.c_void_p, C.c_int]),
     "mhd_variant_count": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_int)]),

@@ -15,6 +15,7 @@ fails (device allocation) rejects the requests that needed it; cancel() removes 
 """
 from __future__ import annotations
 
+import ctypes as C
 import math
 import time
 from dataclasses import dataclass, field
@@ -307,3 +308,160 @@ def run_sequential(pkg, requests, stepper="RK4", device=0, realtime=True, clock=
     for p in probs.values():
         p.close()
     return report(requests)
+
+
+_NATIVE_STATUS = ("queued", "active", "done", "failed", "rejected", "cancelled")
+_SIZES = (16, 32, 48, 64, 96, 128, 256, 512)
+
+
+class NativeServer:
+    """The library's own continuous-batching scheduler (mhd_server_* of the C ABI): the same
+    policy as Server (first-fit admission in arrival order under a device-memory budget, size
+    classes stepped together, min(steps_per_tick, smallest remaining) steps per tick), with the
+    scheduling loop in C++.  ``submit`` copies the request; ``tick`` runs one round."""
+
+    def __init__(self, pkg, budget_bytes=150e9, steps_per_tick=8, stepper="RK4", device=0, keep_states=False,
+                 capacity=None):
+        from . import _lib
+
+        self._L = _lib
+        self.lib = _lib.load()
+        p = _lib.MhdServerParams()
+        p.budget_bytes = float(budget_bytes)
+        p.steps_per_tick = int(steps_per_tick)
+        p.scheme = _lib.MHD_RK4 if str(stepper).upper() == "RK4" else _lib.MHD_LSRK4
+        p.device = int(device)
+        p.keep_states = int(bool(keep_states))
+        for i, n in enumerate(_SIZES):
+            p.capacity[i] = int((capacity or {}).get(n, 0))
+        h = C.c_void_p()
+        _lib.check(self.lib.mhd_server_create(C.byref(p), C.byref(h)))
+        self._h = h
+        self.keep_states = bool(keep_states)
+        self.ticks = 0
+        self.peak_active = 0
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self.lib.mhd_server_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def submit(self, n, nu, eta, steps, sol=None, dt=None, L=2 * math.pi):
+        """Queue a solve; sol is the (6, n, n, n/2+1) complex64 initial state (None: zero)."""
+        r = self._L.MhdRequest()
+        r.n, r.L, r.nu, r.eta = int(n), float(L), float(nu), float(eta)
+        r.dt = 0.0 if dt is None else float(dt)
+        r.steps = int(steps)
+        buf = None
+        if sol is not None:
+            buf = np.ascontiguousarray(sol, dtype=np.complex64)
+            if buf.shape != (6, n, n, n // 2 + 1):
+                raise ValueError("sol must be (6, n, n, n/2+1)")
+            r.sol = buf.ctypes.data
+        rid = C.c_longlong()
+        self._L.check(self.lib.mhd_server_submit(self._h, C.byref(r), C.byref(rid)))
+        return rid.value
+
+    def tick(self):
+        a, q = C.c_int(), C.c_int()
+        self._L.check(self.lib.mhd_server_tick(self._h, C.byref(a), C.byref(q)))
+        self.ticks += 1
+        self.peak_active = max(self.peak_active, a.value)
+        return a.value, q.value
+
+    def poll(self, rid):
+        st, done = C.c_int(), C.c_longlong()
+        self._L.check(self.lib.mhd_server_poll(self._h, int(rid), C.byref(st), C.byref(done)))
+        return _NATIVE_STATUS[st.value], done.value
+
+    def result(self, rid, n=None):
+        """(diagnostics dict, final state or None) of a done request; raises MHDError otherwise."""
+        d = (C.c_double * 8)()
+        out = None
+        if self.keep_states and n is not None:
+            out = np.empty((6, n, n, n // 2 + 1), dtype=np.complex64)
+        self._L.check(self.lib.mhd_server_result(self._h, int(rid), d, None if out is None else out.ctypes.data))
+        keys = ("E_u", "E_B", "H_c", "max_kdotu", "max_kdotb", "max_divb", "nonfinite", "t")
+        return dict(zip(keys, list(d))), out
+
+    def cancel(self, rid):
+        self._L.check(self.lib.mhd_server_cancel(self._h, int(rid)))
+
+    def memory(self):
+        r, p = C.c_double(), C.c_double()
+        self._L.check(self.lib.mhd_server_memory(self._h, C.byref(r), C.byref(p)))
+        return r.value, p.value
+
+    def run(self, requests, realtime=True, clock=None, sleep=None):
+        """Serve SolveRequest objects arriving at their `arrival` times (seconds from the start);
+        fills each request's status, latency, diagnostics (and final state with keep_states).
+        realtime=False jumps a virtual clock to the next arrival when nothing runs."""
+        from . import ic
+
+        clock = clock or time.perf_counter
+        sleep = sleep or time.sleep
+        reqs = sorted(requests, key=lambda r: r.arrival)
+        ids = {}
+        i = 0
+        t0 = clock()
+        now = lambda: clock() - t0  # noqa: E731
+        live = []
+        while i < len(reqs) or live:
+            t = now()
+            while i < len(reqs) and reqs[i].arrival <= t:
+                r = reqs[i]
+                st = r.init_state if r.init_state is not None else ic.random_spectrum_state(r.n, r.seed)
+                ids[r.rid] = self.submit(r.n, r.nu, r.eta, r.steps, st, r.dt)
+                live.append(r)
+                i += 1
+            if not live:
+                wait = reqs[i].arrival - now()
+                if wait > 0:
+                    if realtime:
+                        sleep(wait)
+                    else:
+                        t0 -= wait
+                continue
+            active, queued = self.tick()
+            t = now()
+            keep = []
+            for r in live:
+                status, done = self.poll(ids[r.rid])
+                r.steps_done = done
+                if status == "active" and math.isnan(r.admitted_at):
+                    r.admitted_at = t
+                if status in ("queued", "active"):
+                    keep.append(r)
+                    continue
+                r.status = status
+                r.completed_at = t
+                if status == "done":
+                    r.diagnostics, r.final_state = self.result(ids[r.rid], r.n)
+                else:
+                    try:
+                        self.result(ids[r.rid])
+                    except Exception as e:  # the request's failure message
+                        r.error = str(e)
+            live = keep
+            if active == 0 and queued:
+                if i >= len(reqs):
+                    for r in live:  # nothing runs and nothing fits: cannot ever run
+                        self.cancel(ids[r.rid])
+                        r.status, r.error = "rejected", "request does not fit the memory budget"
+                    live = []
+                else:  # nothing fits until later arrivals change the mix: wait for the next one
+                    wait = reqs[i].arrival - now()
+                    if wait > 0:
+                        if realtime:
+                            sleep(wait)
+                        else:
+                            t0 -= wait
+        out = report(requests)
+        out.update({"peak_reserved_bytes": self.memory()[1], "peak_active": self.peak_active, "ticks": self.ticks})
+        return out

@@ -67,6 +67,40 @@ def test_bounded_wait_check_validates_arguments(pkg, lib):
     assert lib.mhd_check_bounded_wait(0, 5.0, None, None) == pkg._lib.MHD_ERR_INVALID
 
 
+def test_native_server_host_logic(pkg, lib):
+    """The C++ scheduler's validation and, with no GPU here, its rejection path: the size class of
+    an admitted request cannot be allocated, so that request alone is rejected."""
+    import ctypes as C
+
+    L = pkg._lib
+    p = L.MhdServerParams()
+    p.budget_bytes, p.steps_per_tick, p.scheme = 0.0, 4, L.MHD_RK4
+    h = C.c_void_p()
+    assert lib.mhd_server_create(C.byref(p), C.byref(h)) == L.MHD_ERR_INVALID
+    p.budget_bytes = 1e9
+    assert lib.mhd_server_create(C.byref(p), C.byref(h)) == L.MHD_OK
+    try:
+        r = L.MhdRequest()
+        r.n, r.L, r.nu, r.eta, r.steps = 17, 6.283, 1e-3, 1e-3, 5
+        rid = C.c_longlong()
+        assert lib.mhd_server_submit(h, C.byref(r), C.byref(rid)) == L.MHD_ERR_INVALID
+        a, q = C.c_int(), C.c_int()
+        assert lib.mhd_server_tick(h, C.byref(a), C.byref(q)) == L.MHD_OK and (a.value, q.value) == (0, 0)
+        r.n = 32
+        assert lib.mhd_server_submit(h, C.byref(r), C.byref(rid)) == L.MHD_OK
+        st, done = C.c_int(), C.c_longlong()
+        assert lib.mhd_server_poll(h, rid, C.byref(st), C.byref(done)) == L.MHD_OK and st.value == 0  # queued
+        if not __import__("torch").cuda.is_available():
+            assert lib.mhd_server_tick(h, C.byref(a), C.byref(q)) == L.MHD_OK
+            assert lib.mhd_server_poll(h, rid, C.byref(st), C.byref(done)) == L.MHD_OK
+            assert st.value == 4  # rejected: the size class could not be allocated
+            assert lib.mhd_server_result(h, rid, None, None) == L.MHD_ERR_OOM
+            assert b"allocation failed" in lib.mhd_last_error()
+        assert lib.mhd_server_poll(h, 999, C.byref(st), C.byref(done)) == L.MHD_ERR_INVALID
+    finally:
+        lib.mhd_server_destroy(h)
+
+
 def test_null_handle_errors(pkg, lib):
     assert lib.mhd_step(None, 1) == pkg._lib.MHD_ERR_INVALID
     assert lib.mhd_destroy(None) == 0
