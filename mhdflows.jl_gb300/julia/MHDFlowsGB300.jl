@@ -15,7 +15,8 @@ import FourierFlows: stepforward!
 
 export GB300TimeStepper, gb300_updatevars!, sync_sol!, push_sol!, gb300_diagnostics, gb300_autotune!,
        gb300_SetUpFk!, gb300_set_vp!, gb300_DivVCorrection!, gb300_DivBCorrection!, gb300_div_correction!,
-       gb300_record_diagnostics!, gb300_diagnostic_history
+       gb300_record_diagnostics!, gb300_diagnostic_history, MhdServerParams, MhdRequest, GB300Server,
+       gb300_submit!, gb300_tick!, gb300_poll, gb300_result
 
 const libmhdgb = get(ENV, "MHDGB_LIB", joinpath(@__DIR__, "..", "lib", "libmhdgb.so"))
 
@@ -152,6 +153,72 @@ function gb300_diagnostic_history(ts::GB300TimeStepper)
   check(ccall((:mhd_get_diag_history, libmhdgb), Cint, (Ptr{Cvoid}, Cint, Ptr{Cdouble}, Cint, Ref{Cint}),
               ts.handle, 0, out, n[], n))
   return permutedims(out[:, 1:n[]])
+end
+
+# Serving scheduler (mhd_server_*): continuous batching of independent solves on one GPU.
+struct MhdServerParams
+  budget_bytes::Cdouble
+  steps_per_tick::Cint
+  scheme::Cint
+  device::Cint
+  keep_states::Cint
+  capacity::NTuple{8,Cint}
+end
+
+struct MhdRequest
+  n::Cint
+  L::Cdouble
+  nu::Cdouble
+  eta::Cdouble
+  dt::Cdouble
+  steps::Clonglong
+  sol::Ptr{ComplexF32}
+end
+
+mutable struct GB300Server
+  handle::Ptr{Cvoid}
+end
+
+function GB300Server(; budget_bytes = 150e9, steps_per_tick = 8, scheme::Symbol = :RK4, device = 0,
+                     keep_states::Bool = false)
+  p = MhdServerParams(budget_bytes, steps_per_tick, scheme == :RK4 ? 0 : 1, device, keep_states ? 1 : 0,
+                      ntuple(_ -> Cint(0), 8))
+  h = Ref{Ptr{Cvoid}}(C_NULL)
+  check(ccall((:mhd_server_create, libmhdgb), Cint, (Ref{MhdServerParams}, Ref{Ptr{Cvoid}}), p, h))
+  s = GB300Server(h[])
+  finalizer(x -> ccall((:mhd_server_destroy, libmhdgb), Cint, (Ptr{Cvoid},), x.handle), s)
+  return s
+end
+
+# sol: (nkr, n, n, 6) ComplexF32 initial state (copied at submit); returns the request id
+function gb300_submit!(s::GB300Server, n, L, ν, η, steps, sol; dt = 0.0)
+  rid = Ref{Clonglong}(0)
+  GC.@preserve sol begin
+    r = MhdRequest(n, L, ν, η, dt, steps, pointer(sol))
+    check(ccall((:mhd_server_submit, libmhdgb), Cint, (Ptr{Cvoid}, Ref{MhdRequest}, Ref{Clonglong}), s.handle, r, rid))
+  end
+  return rid[]
+end
+
+function gb300_tick!(s::GB300Server)
+  a, q = Ref{Cint}(0), Ref{Cint}(0)
+  check(ccall((:mhd_server_tick, libmhdgb), Cint, (Ptr{Cvoid}, Ref{Cint}, Ref{Cint}), s.handle, a, q))
+  return a[], q[]
+end
+
+const REQ_STATUS = (:queued, :active, :done, :failed, :rejected, :cancelled)
+function gb300_poll(s::GB300Server, rid)
+  st, done = Ref{Cint}(0), Ref{Clonglong}(0)
+  check(ccall((:mhd_server_poll, libmhdgb), Cint, (Ptr{Cvoid}, Clonglong, Ref{Cint}, Ref{Clonglong}), s.handle, rid, st, done))
+  return REQ_STATUS[st[] + 1], done[]
+end
+
+# diagnostics (8 values as gb300_diagnostics) of a finished request
+function gb300_result(s::GB300Server, rid)
+  d = zeros(Float64, 8)
+  check(ccall((:mhd_server_result, libmhdgb), Cint, (Ptr{Cvoid}, Clonglong, Ptr{Cdouble}, Ptr{Cvoid}),
+              s.handle, rid, d, C_NULL))
+  return d
 end
 
 end # module
