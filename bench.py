@@ -284,7 +284,7 @@ def run_gpu(args, rank, world, local, dist: Dist):
     lib = pkg._lib.load()
     n = args.n
     s0 = initial_state(n)
-    prob = pkg.Problem(pkg.GPU(local), nx=n, Lx=2 * math.pi, nu=NU, eta=ETA, dt=DT, stepper="RK4",
+    prob = pkg.Problem(pkg.GPU(local), nx=n, Lx=2 * math.pi, nu=NU, eta=ETA, dt=DT, stepper=args.scheme,
                        precision=args.precision, B_field=not args.hydro, VP_method=args.vp)
     if args.hydro:
         s0 = s0[:3]
@@ -452,6 +452,7 @@ def main():
     ap.add_argument("--grid", dest="n", type=int, default=256, help="grid points per axis of the step workload")
     ap.add_argument("--precision", default="fp32", choices=["fp32", "split_fp16", "split_bf16"],
                     help="x-row transforms in FP32 (plain form) or as split 16-bit tensor-core DFTs")
+    ap.add_argument("--scheme", default="RK4", choices=["RK4", "LSRK4"], help="time stepper of the step workload")
     ap.add_argument("--hydro", action="store_true", help="hydrodynamic problem (B_field = false)")
     ap.add_argument("--forcing", action="store_true", help="A99 random forcing on (SetUpFk!)")
     ap.add_argument("--vp", action="store_true", help="volume penalisation on (VP_method, a ball obstacle)")
@@ -463,8 +464,8 @@ def main():
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     rank, world, local = dist_env()
-    config = {"workload": f"MHD RK4 step, {args.n}^3 FP32, nu=eta=1e-3, dt=5e-4, seeded k^4 exp(-2(k/4)^2) u and B",
-              "n": args.n, "scheme": "RK4", "precision": args.precision, "hydro": args.hydro, "forcing": args.forcing, "vp": args.vp,
+    config = {"workload": f"MHD {args.scheme} step, {args.n}^3 FP32, nu=eta=1e-3, dt=5e-4, seeded k^4 exp(-2(k/4)^2) u and B",
+              "n": args.n, "scheme": args.scheme, "precision": args.precision, "hydro": args.hydro, "forcing": args.forcing, "vp": args.vp,
               "l2": "inputs larger than L2 (step working set > 1 GB)",
               "parallelism": "replicas" if args.gpus > 1 else "single"}
 
