@@ -47,3 +47,22 @@ def test_long_decaying_run(pkg, mo):
     amp_u = math.sqrt(e[-1] / scale)
     assert np.all(h[:, 5] < 1e-5 * kmax * amp_u) and np.all(h[:, 6] < 1e-5 * kmax * amp_u)
     print(f"E(0) {e0:.6f} -> E(2001 steps) {e[-1]:.6f}")
+
+
+def test_ideal_invariants(pkg):
+    """nu = eta = 0: the nonlinear terms conserve the total energy and the cross-helicity
+    (ideal MHD invariants; dealiased Galerkin truncation keeps both).  200 RK4 steps at 128^3
+    change them only by the scheme's O(dt^5) error and FP32 roundoff."""
+    from importlib import import_module
+
+    s0 = import_module(pkg.__name__ + ".ic").random_spectrum_state(128, 122)
+    with pkg.Problem(pkg.GPU(0), nx=128, Lx=2 * math.pi, nu=0.0, eta=0.0, dt=2e-4) as p:
+        p.set_sol(s0.T)
+        d0 = p.diagnostics()
+        pkg.stepforward(p, 200)
+        d1 = p.diagnostics()
+    e0, e1 = d0.E_u + d0.E_B, d1.E_u + d1.E_B
+    print(f"ideal: dE/E {(e1 - e0) / e0:.3e}, dHc {d1.H_c - d0.H_c:.3e} (E {e0:.4f}, Hc {d0.H_c:.4f})")
+    assert abs(e1 - e0) < 2e-5 * e0
+    assert abs(d1.H_c - d0.H_c) < 2e-5 * e0
+    assert abs(d1.E_u - d0.E_u) > 1e-4 * e0  # energy does move between u and B
