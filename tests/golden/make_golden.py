@@ -6,6 +6,12 @@ Fixtures (retained band only, complex128, compressed npz):
   rand48_lsrk4.npz   seeded k^4 exp(-2(k/4)^2) spectrum at 48^3 (seed 7), nu = 1e-3, eta = 2e-3,
                      dt = 0.2*dx: state after 0 and 10 LSRK4 steps
   rhs32.npz          one calcN! evaluation of the 32^3 random state (seed 11), nu = 2e-3, eta = 3e-3
+  vp32_rhs.npz       one calcN! evaluation with volume penalisation (VP_UᵢUpdate! / VP_BᵢUpdate!) of
+                     the 32^3 random state (seed 13), nu = 2e-3, eta = 3e-3, dt = 1e-3, mask and
+                     walls from vp_inputs()
+  hd48_rk4.npz       hydrodynamics (B = 0) at 48^3 (seed 17), nu = 1e-3, dt = 1e-3: 0 and 3 RK4 steps
+  hdvp32_rk4.npz     hydrodynamics with volume penalisation at 32^3 (seed 19), nu = 2e-3, dt = 1e-3,
+                     mask and velocity walls from vp_inputs(): 0 and 2 RK4 steps
 
 Run from the repository root:  python tests/golden/make_golden.py
 """
@@ -63,10 +69,61 @@ def rhs32():
     np.savez_compressed(os.path.join(HERE, "rhs32.npz"), s=compact(g, s), rhs=compact(g, N))
 
 
+def vp_inputs(g):
+    """Mask chi (a smoothed ball of radius 1.2 off the box centre) and wall fields U0, B0 as FP32
+    physical arrays (nz, ny, nx), analytic in the grid coordinates."""
+    x, y, z = g.mesh()
+    chi = (0.5 * (1 - np.tanh((np.sqrt(x ** 2 + (y - 0.3) ** 2 + z ** 2) - 1.2) / 0.25))).astype(np.float32)
+    U0 = tuple((a * np.sin(x + p) * np.cos(y - z)).astype(np.float32) for a, p in ((0.6, 0.3), (0.4, 1.1), (0.8, 2.0)))
+    B0 = tuple((a * np.cos(x - p) * np.sin(y + z)).astype(np.float32) for a, p in ((0.2, 0.5), (0.3, 1.7), (0.1, 2.9)))
+    return chi, U0, B0
+
+
+def _vp(g, dt, walls_b=True):
+    chi, U0, B0 = vp_inputs(g)
+    return dict(chi=chi.astype(np.float64), dt=dt, U0=tuple(a.astype(np.float64) for a in U0),
+                B0=tuple(a.astype(np.float64) for a in B0) if walls_b else None)
+
+
+def vp32():
+    g = mo.Grid(32)
+    s = mo.random_spectrum_state(g, 13)
+    N = np.zeros_like(s)
+    mo.calcN_literal(N, s.copy(), g, 2e-3, 3e-3, vp=_vp(g, 1e-3))
+    np.savez_compressed(os.path.join(HERE, "vp32_rhs.npz"), s=compact(g, s), rhs=compact(g, N))
+
+
+def hd48():
+    g = mo.Grid(48)
+    s = mo.random_spectrum_state(g, 17)
+    s[3:] = 0
+    st = mo.Stepper(g, 1e-3, 0.0, 1e-3, "RK4", literal=True)
+    s0 = compact(g, s)
+    for _ in range(3):
+        st.stepforward(s)
+    np.savez_compressed(os.path.join(HERE, "hd48_rk4.npz"), s0=s0[:3], s3=compact(g, g.dealias(s.copy()))[:3])
+
+
+def hdvp32():
+    g = mo.Grid(32)
+    s = mo.random_spectrum_state(g, 19)
+    s[3:] = 0
+    st = mo.Stepper(g, 2e-3, 0.0, 1e-3, "RK4", literal=True)
+    v = _vp(g, 1e-3, walls_b=False)
+    st.vp = dict(chi=v["chi"], U0=v["U0"])
+    s0 = compact(g, s)
+    for _ in range(2):
+        st.stepforward(s)
+    np.savez_compressed(os.path.join(HERE, "hdvp32_rk4.npz"), s0=s0[:3], s2=compact(g, g.dealias(s.copy()))[:3])
+
+
 if __name__ == "__main__":
     tg32()
     rand48()
     rhs32()
+    vp32()
+    hd48()
+    hdvp32()
     for f in sorted(os.listdir(HERE)):
         if f.endswith(".npz"):
             print(f, os.path.getsize(os.path.join(HERE, f)))

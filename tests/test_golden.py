@@ -96,3 +96,72 @@ def test_gpu_rhs32_against_golden(pkg, mo):
         prob.set_sol(mo.expand_compact(32, d["s"], np.complex64).T)
         got = prob.rhs_c()
     assert rel(compact(mo, g, got), d["rhs"]) < 1e-5
+
+
+def _make_golden():
+    import importlib.util
+
+    spec = importlib.util.spec_from_file_location("make_golden", os.path.join(HERE, "make_golden.py"))
+    mg = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mg)
+    return mg
+
+
+def test_oracle_reproduces_vp_and_hd_fixtures(mo):
+    mg = _make_golden()
+    g32, g48 = mo.Grid(32), mo.Grid(48)
+    d = load("vp32_rhs.npz")
+    s = mo.random_spectrum_state(g32, 13)
+    N = np.zeros_like(s)
+    mo.calcN_literal(N, s.copy(), g32, 2e-3, 3e-3, vp=mg._vp(g32, 1e-3))
+    assert rel(compact(mo, g32, N), d["rhs"]) < 1e-12
+    d = load("hd48_rk4.npz")
+    s = mo.random_spectrum_state(g48, 17)
+    s[3:] = 0
+    st = mo.Stepper(g48, 1e-3, 0.0, 1e-3, "RK4", literal=False)
+    for _ in range(3):
+        st.stepforward(s)
+    assert rel(compact(mo, g48, g48.dealias(s))[:3], d["s3"]) < 1e-12
+
+
+def _vp_arrays(mg, g, walls_b=True):
+    chi, U0, B0 = mg.vp_inputs(g)
+    return chi.T, tuple(a.T for a in U0), (tuple(a.T for a in B0) if walls_b else None)
+
+
+@pytest.mark.gpu
+def test_gpu_vp32_rhs_against_golden(pkg, mo):
+    mg = _make_golden()
+    d = load("vp32_rhs.npz")
+    g = mo.Grid(32)
+    chi, U0, B0 = _vp_arrays(mg, g)
+    with pkg.Problem(pkg.GPU(0), nx=32, Lx=2 * math.pi, nu=2e-3, eta=3e-3, dt=1e-3, VP_method=True) as prob:
+        prob.set_sol(mo.expand_compact(32, d["s"], np.complex64).T)
+        prob.set_vp(chi, U0=U0, B0=B0)
+        got = prob.rhs_c()
+    assert rel(compact(mo, g, got), d["rhs"]) < 1e-5
+
+
+@pytest.mark.gpu
+def test_gpu_hd_fixtures(pkg, mo):
+    mg = _make_golden()
+    d = load("hd48_rk4.npz")
+    g = mo.Grid(48)
+    full = np.zeros((6,) + d["s0"].shape[1:], np.complex128)
+    full[:3] = d["s0"]
+    with pkg.Problem(pkg.GPU(0), nx=48, Lx=2 * math.pi, nu=1e-3, dt=1e-3, B_field=False) as prob:
+        prob.set_sol(mo.expand_compact(48, full, np.complex64)[:3].T)
+        pkg.stepforward(prob, 3)
+        err = rel(compact(mo, g, prob.sol_c()), d["s3"])
+    assert err < 1e-5, err
+    d = load("hdvp32_rk4.npz")
+    g = mo.Grid(32)
+    full = np.zeros((6,) + d["s0"].shape[1:], np.complex128)
+    full[:3] = d["s0"]
+    chi, U0, _ = _vp_arrays(mg, g, walls_b=False)
+    with pkg.Problem(pkg.GPU(0), nx=32, Lx=2 * math.pi, nu=2e-3, dt=1e-3, B_field=False, VP_method=True) as prob:
+        prob.set_sol(mo.expand_compact(32, full, np.complex64)[:3].T)
+        prob.set_vp(chi, U0=U0)
+        pkg.stepforward(prob, 2)
+        err = rel(compact(mo, g, prob.sol_c()), d["s2"])
+    assert err < 1e-5, err
