@@ -34,6 +34,16 @@ What it restates (file:line into MHDFlows.jl):
   FourierFlows 0.10.1, unverified, same double arithmetic as Julia).
 * ``prob_diagnostic``: ``ProbDiagnostic`` (src/utils/UserInterface.jl:29,65-86),
   KE = ME = sum(|.|^2)*dV with no 1/2, and ``Div`` (src/utils/VectorCalculus.jl:72-94).
+* ``vp_update`` / ``add_vp``: ``VP_UᵢUpdate!`` / ``VP_BᵢUpdate!`` (src/Solver/VPSolver.jl:20-58),
+  called from src/Solver/MHDSolver.jl:85-88,160-163 (and HDSolver.jl:76-79): eta = dt*13/7,
+  out += -(delta_aj - k_j k_a / k^2) rfft(chi/eta (f_j - W_j)).  ``div_correct``:
+  ``DivVCorrection!`` / ``DivBCorrection!`` (src/Solver/VPSolver.jl:60-138).
+* Hydrodynamics (``HDcalcN!``, src/pgen.jl:176-182): the MHD right-hand side with B = 0 and
+  eta = 0 (the induction terms vanish identically); HDcalcN! applies addforcing! before the
+  advection step zeroes the velocity right-hand side, so a forced HD run is unforced.
+* ``add_a99_forcing`` / ``a99_force``: SetUpFk! and A99ForceDriving!
+  (src/pgen/A99ForceDriving_GPU.jl:18-130) with a counter-based generator in place of the
+  device rand().
 
 Array layout: numpy C order ``(nz, ny, nx)`` for physical fields and
 ``(nz, ny, nkr)`` for half spectra, which is the same memory as Julia's
