@@ -132,6 +132,17 @@ def test_build_is_in_tree(pkg):
     assert "arch=compute_103a,code=sm_103a" in b.ARCH_FLAGS
 
 
+def test_missing_library_fails_loudly(pkg, tmp_path):
+    """No CPU fallback: pointing the loader at a library that does not exist raises."""
+    saved = pkg._lib._lib
+    pkg._lib._lib = None
+    try:
+        with pytest.raises(pkg.MHDError):
+            pkg._lib.load(str(tmp_path / "libmhdgb_missing.so"))
+    finally:
+        pkg._lib._lib = saved
+
+
 def test_product_does_not_import_oracle():
     root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
     pkgdir = os.path.join(root, "mhdflows.jl_gb300")
