@@ -12,6 +12,8 @@ Fixtures (retained band only, complex128, compressed npz):
   hd48_rk4.npz       hydrodynamics (B = 0) at 48^3 (seed 17), nu = 1e-3, dt = 1e-3: 0 and 3 RK4 steps
   hdvp32_rk4.npz     hydrodynamics with volume penalisation at 32^3 (seed 19), nu = 2e-3, dt = 1e-3,
                      mask and velocity walls from vp_inputs(): 0 and 2 RK4 steps
+  forced32_rk4.npz   A99 forcing (SetUpFk! kf = 2, P = 1e-5, sigma = 1, b = 1, seed 1234) on the 32^3
+                     random state (seed 23), nu = eta = 1e-3, dt = 1e-3: 0 and 2 RK4 steps
 
 Run from the repository root:  python tests/golden/make_golden.py
 """
@@ -117,6 +119,17 @@ def hdvp32():
     np.savez_compressed(os.path.join(HERE, "hdvp32_rk4.npz"), s0=s0[:3], s2=compact(g, g.dealias(s.copy()))[:3])
 
 
+def forced32():
+    g = mo.Grid(32)
+    s = mo.random_spectrum_state(g, 23)
+    st = mo.Stepper(g, 1e-3, 1e-3, 1e-3, "RK4", literal=True)
+    st.forcing = dict(A=mo.a99_amplitude(g, 2.0, 1e-5, 1.0), kf_used=1.0, sigma2=1.0, b=1.0, seed=1234)
+    s0 = compact(g, s)
+    for _ in range(2):
+        st.stepforward(s)
+    np.savez_compressed(os.path.join(HERE, "forced32_rk4.npz"), s0=s0, s2=compact(g, g.dealias(s.copy())))
+
+
 if __name__ == "__main__":
     tg32()
     rand48()
@@ -124,6 +137,7 @@ if __name__ == "__main__":
     vp32()
     hd48()
     hdvp32()
+    forced32()
     for f in sorted(os.listdir(HERE)):
         if f.endswith(".npz"):
             print(f, os.path.getsize(os.path.join(HERE, f)))

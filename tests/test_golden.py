@@ -165,3 +165,27 @@ def test_gpu_hd_fixtures(pkg, mo):
         pkg.stepforward(prob, 2)
         err = rel(compact(mo, g, prob.sol_c()), d["s2"])
     assert err < 1e-5, err
+
+
+def test_oracle_reproduces_forced32(mo):
+    d = load("forced32_rk4.npz")
+    g = mo.Grid(32)
+    s = mo.random_spectrum_state(g, 23)
+    assert rel(compact(mo, g, s), d["s0"]) < 1e-14
+    st = mo.Stepper(g, 1e-3, 1e-3, 1e-3, "RK4", literal=False)
+    st.forcing = dict(A=mo.a99_amplitude(g, 2.0, 1e-5, 1.0), kf_used=1.0, sigma2=1.0, b=1.0, seed=1234)
+    for _ in range(2):
+        st.stepforward(s)
+    assert rel(compact(mo, g, g.dealias(s)), d["s2"]) < 1e-12
+
+
+@pytest.mark.gpu
+def test_gpu_forced32_against_golden(pkg, mo):
+    d = load("forced32_rk4.npz")
+    g = mo.Grid(32)
+    with _problem(pkg, 32, 1e-3, 1e-3, 1e-3, "RK4") as prob:
+        prob.set_sol(mo.expand_compact(32, d["s0"], np.complex64).T)
+        pkg.SetUpFk(prob, kf=2.0, P=1e-5, sigma=1.0, b=1.0, seed=1234)
+        pkg.stepforward(prob, 2)
+        err = rel(compact(mo, g, prob.sol_c()), d["s2"])
+    assert err < 1e-5, err
