@@ -688,46 +688,67 @@ def select_variant(obj, cls, idx: int):
 
 
 # ---- checkpoint / restart (src/integrator.jl:208-288, src/utils/IC.jl:245-257) ----------------
-# The reference writes HDF5 files through HDF5.jl.  No HDF5 library exists on this system, so the
-# same datasets -- i_velocity, j_velocity, k_velocity, i_mag_field, j_mag_field, k_mag_field
-# (Float32, (nx, ny, nz) in the reference's index order) and time -- go into a NumPy .npz archive
-# with the reference's file pattern <name>_t_<4-digit number>.npz.
+# The reference writes one HDF5 file per snapshot through HDF5.jl, <name>_t_<4-digit number>.h5,
+# holding i_velocity, j_velocity, k_velocity, i_mag_field, j_mag_field, k_mag_field (Float32,
+# Julia (nx, ny, nz)) and time.  The same files are written and read here by ``hdf5.py``, a small
+# implementation of the HDF5 file format (no HDF5 library exists on this system); ``fmt="npz"``
+# keeps a NumPy archive with the same datasets instead.
 _DATASETS = ("i_velocity", "j_velocity", "k_velocity", "i_mag_field", "j_mag_field", "k_mag_field")
 
 
-def checkpoint_path(file_path_and_name: str, file_number: int) -> str:
-    """<name>_t_0001.npz: the number zero-padded to four digits like savefile."""
-    return f"{file_path_and_name}_t_{int(file_number):04d}.npz"
+def checkpoint_path(file_path_and_name: str, file_number: int, fmt: str = "h5") -> str:
+    """<name>_t_0001.h5: the number zero-padded to four digits like savefile."""
+    if fmt not in ("h5", "npz"):
+        raise MHDError(_lib.MHD_ERR_INVALID, "checkpoint format must be 'h5' or 'npz'")
+    return f"{file_path_and_name}_t_{int(file_number):04d}.{fmt}"
 
 
-def savefile(prob: Problem, file_number: int, file_path_and_name: str = "") -> str:
+def savefile(prob: Problem, file_number: int, file_path_and_name: str = "", fmt: str = "h5") -> str:
     """savefile(prob, file_number; file_path_and_name) (src/integrator.jl:260-288): the physical
-    fields of the current state and the time.  Returns the path written."""
+    fields of the current state and the time, in the reference's HDF5 layout (or ``fmt="npz"``).
+    The time is stored in float64 (the library's clock); the reference's Restart! and
+    readMHDFlows read either width.  Returns the path written."""
+    from . import hdf5
+
     updatevars(prob)
-    data = {name: np.asarray(getattr(prob.vars, FIELDS[f])) for f, name in enumerate(_DATASETS[: prob.nfields])}
-    data["time"] = np.float64(prob.clock.t)
-    path = checkpoint_path(file_path_and_name, file_number)
-    with open(path, "wb") as fh:
-        np.savez(fh, **data)
+    fields = {name: np.asarray(getattr(prob.vars, FIELDS[f]), dtype=np.float32)
+              for f, name in enumerate(_DATASETS[: prob.nfields])}
+    t = np.float64(prob.clock.t)
+    path = checkpoint_path(file_path_and_name, file_number, fmt)
+    if fmt == "h5":
+        # a Julia (nx, ny, nz) array is stored with HDF5 dimensions (nz, ny, nx), the same bytes
+        hdf5.write(path, {**{k: np.ascontiguousarray(v.T) for k, v in fields.items()}, "time": t})
+    else:
+        with open(path, "wb") as fh:
+            np.savez(fh, time=t, **fields)
     return path
+
+
+def _read_checkpoint(path: str, names):
+    """{name: array in the reference's (nx, ny, nz) index order} and the time, from .h5 or .npz."""
+    from . import hdf5
+
+    with open(path, "rb") as fh:
+        head = fh.read(8)
+    if head == hdf5.SIGNATURE:
+        d = hdf5.read(path, list(names) + ["time"])
+        return {k: d[k].T for k in names}, float(d["time"])
+    with np.load(path) as f:
+        return {k: np.asarray(f[k]) for k in names}, float(f["time"])
 
 
 def readMHDFlows(path: str):
     """readMHDFlows(FileName) (src/utils/IC.jl:245-257): (iv, jv, kv, ib, jb, kb, t), Float32
     fields in the reference's (nx, ny, nz) index order."""
-    with np.load(path) as f:
-        fields = [np.asarray(f[name], dtype=np.float32) for name in _DATASETS]
-        t = float(f["time"])
-    return (*fields, t)
+    fields, t = _read_checkpoint(path, _DATASETS)
+    return (*[np.asarray(fields[k], dtype=np.float32) for k in _DATASETS], t)
 
 
 def Restart(prob: Problem, path: str):
     """Restart!(prob, file_path_and_name) (src/integrator.jl:208-258): fields -> r2c into sol,
     clock.t <- time."""
-    with np.load(path) as f:
-        kw = {FIELDS[i]: np.asarray(f[name]) for i, name in enumerate(_DATASETS[: prob.nfields])}
-        t = float(f["time"])
-    SetUpProblemIC(prob, **kw)
+    fields, t = _read_checkpoint(path, _DATASETS[: prob.nfields])
+    SetUpProblemIC(prob, **{FIELDS[i]: fields[k] for i, k in enumerate(_DATASETS[: prob.nfields])})
     prob.clock.t = t
     return None
 

@@ -94,7 +94,7 @@ def test_savefile_restart_round_trip(pkg, mo, tmp_path):
         pkg.SetUpProblemIC(a, **{k: fields[i].astype(np.float32).T for i, k in enumerate(pkg.FIELDS)})
         pkg.stepforward(a, 5)
         path = pkg.savefile(a, 7, file_path_and_name=str(tmp_path / "run"))
-        assert os.path.basename(path) == "run_t_0007.npz"
+        assert os.path.basename(path) == "run_t_0007.h5"
         sol_a = a.sol_c()
         t_a = a.clock.t
     iv, jv, kv, ib, jb, kb, t = pkg.readMHDFlows(path)
