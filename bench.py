@@ -245,14 +245,16 @@ def run_serve(args):
         r.init_state = initial_state(r.n, r.seed)
     srv = serving.Server(serving.GpuBackend(pkg, "RK4"), budget_bytes=150e9, steps_per_tick=8)
     rep = srv.run(reqs, realtime=True)
-    nat_reqs = mk()  # the same stream through the C++ scheduler (mhd_server_*)
-    for r, q in zip(nat_reqs, reqs):
-        r.init_state = q.init_state
-    nat = serving.NativeServer(pkg, budget_bytes=150e9, steps_per_tick=8)
-    try:
-        nrep = nat.run(nat_reqs, realtime=True)
-    finally:
-        nat.close()
+    nrep = None
+    if getattr(args, "native", True):
+        nat_reqs = mk()  # the same stream through the C++ scheduler (mhd_server_*)
+        for r, q in zip(nat_reqs, reqs):
+            r.init_state = q.init_state
+        nat = serving.NativeServer(pkg, budget_bytes=150e9, steps_per_tick=8)
+        try:
+            nrep = nat.run(nat_reqs, realtime=True)
+        finally:
+            nat.close()
     seq_reqs = mk()
     for r, q in zip(seq_reqs, reqs):
         r.init_state = q.init_state
@@ -266,11 +268,10 @@ def run_serve(args):
                                     "p50_latency_s": seq["p50_latency_s"], "p99_latency_s": seq["p99_latency_s"],
                                     "makespan_s": seq["makespan_s"]},
             "speedup_vs_plain": rep["grid_pt_steps_per_s"] / seq["grid_pt_steps_per_s"],
-            "native_scheduler": {"grid_pt_steps_per_s": nrep["grid_pt_steps_per_s"],
-                                 "p50_latency_s": nrep["p50_latency_s"], "p99_latency_s": nrep["p99_latency_s"],
-                                 "makespan_s": nrep["makespan_s"], "done": nrep["done"],
-                                 "peak_active": nrep.get("peak_active"),
-                                 "peak_reserved_gb": nrep.get("peak_reserved_bytes", 0) / 1e9},
+            "native_scheduler": None if nrep is None else {
+                "grid_pt_steps_per_s": nrep["grid_pt_steps_per_s"], "p50_latency_s": nrep["p50_latency_s"],
+                "p99_latency_s": nrep["p99_latency_s"], "makespan_s": nrep["makespan_s"], "done": nrep["done"],
+                "peak_active": nrep.get("peak_active"), "peak_reserved_gb": nrep.get("peak_reserved_bytes", 0) / 1e9},
             "dtype": "f32", "data": "synthetic",
             "config": {"workload": "serving loop: Poisson requests for N in {32,48,64,128,256}, continuous batching",
                        "requests": args.serve_count,
@@ -355,7 +356,8 @@ def run_gpu(args, rank, world, local, dist: Dist):
         avg = T[c] / L[c] / 1e3
         kernels[names[c]] = {"launches": int(L[c]), "avg_us": round(avg * 1e6, 2),
                              "share": round(T[c] / sum(T), 4),
-                             "gbs": round(bb.value / avg / 1e9, 1) if bb.value else None}
+                             "gbs": round(bb.value / avg / 1e9, 1) if bb.value else None,
+                             "frac_of_peak": round(bb.value / avg / 1e9 / peak, 3) if bb.value else None}
 
     # e2e through the C ABI with pinned host buffers: upload state, one step, download state
     nbytes = s0.nbytes
@@ -412,35 +414,112 @@ def run_gpu(args, rank, world, local, dist: Dist):
         p2.synchronize()
         ms2 = C.c_double()
         chk(lib.mhd_time_steps(p2.handle, 10, C.byref(ms2)))
+        chk(lib.mhd_profile_enable(p2.handle, 1))
+        prof2 = (C.c_double * 10)()
+        chk(lib.mhd_step_timed(p2.handle, 10, prof2))
+        L2 = (C.c_longlong * nc)()
+        T2 = (C.c_double * nc)()
+        chk(lib.mhd_profile_read(p2.handle, L2, T2, nc))
+        chk(lib.mhd_profile_enable(p2.handle, 0))
+        kernels2 = {}
+        for c in range(nc):
+            if L2[c] == 0:
+                continue
+            bb = C.c_double()
+            lib.mhd_kernel_class_bytes(p2.handle, c, C.byref(bb))
+            avg = T2[c] / L2[c] / 1e3
+            gbs = bb.value / avg / 1e9 if bb.value else None
+            kernels2[names[c]] = {"launches": int(L2[c]), "avg_us": round(avg * 1e6, 2), "share": round(T2[c] / sum(T2), 4),
+                                  "gbs": round(gbs, 1) if gbs else None,
+                                  "frac_of_peak": round(gbs / measured_peaks()[0], 3) if gbs else None}
         secondary = {"n": n2, "ms_per_step": round(ms2.value / 10, 3),
-                     "grid_pt_steps_per_s": n2 ** 3 / (ms2.value / 10 / 1e3), "variants": variants2}
+                     "grid_pt_steps_per_s": n2 ** 3 / (ms2.value / 10 / 1e3), "variants": variants2,
+                     "kernels": kernels2, "workload": "512^3 RK4, nu = eta = 5e-4, dt = 2.5e-4, same seeded spectrum"}
         p2.close()
+    forms = None
+    if args.extras and rank == 0:
+        forms = run_forms(args, pkg, lib, local)
     prob.close()
     return {
         "value": value, "ms_per_step": ms_per_step, "p50_ms": p50, "p99_ms": p99, "launches": launches,
         "clocks": clocks, "top": top, "achieved": achieved, "bytes": b.value, "peak": peak, "peak_kind": peak_kind,
         "kernels": kernels, "e2e": e2e_value, "e2e_bytes": nbytes, "e2e_steps": ke, "e2e_pieces": e2e_pieces, "finite": finite,
-        "secondary": secondary, "prof_ms": prof_ms, "variants": variants,
+        "secondary": secondary, "prof_ms": prof_ms, "variants": variants, "forms": forms,
     }
 
 
-def cpu_baseline(n: int, stages: int = 1):
-    """CPU restatement of the reference path (oracle, scipy FP32 literal form), all host cores."""
+def _cpu_steps(n, fields_or_state, nu, eta, dt, steps, warmup):
+    """Whole RK4 steps of the CPU restatement of the reference path (oracle literal form: 30 r2c +
+    6 c2r per right-hand side, scipy.fft float32 on every host core); per-step seconds."""
     from oracle import mhd_oracle as mo
 
     g = mo.Grid(n, dtype=np.float32)
-    s = initial_state(n)
-    st = mo.Stepper(g, NU, ETA, DT, "RK4", literal=True)
-    N = np.zeros_like(s)
-    mo.calcN_literal(N, s.copy(), g, NU, ETA)  # warm FFT plans
-    t0 = time.perf_counter()
-    for _ in range(stages):
-        mo.calcN_literal(N, s, g, NU, ETA, vars_out=st.vars)
-        s1 = s + np.float32(DT / 2) * N
-    el = (time.perf_counter() - t0) / stages
-    return {"value": n ** 3 / (4 * el), "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
-            "sample": f"{stages} RK4 stage(s) (one RHS evaluation + stage update) at {n}^3, scaled x4 to an RK4 step; "
-                      f"scipy.fft float32 with workers={os.cpu_count()}"}
+    st = mo.Stepper(g, nu, eta, dt, "RK4", literal=True)
+    s = np.array(fields_or_state, dtype=np.complex64, copy=True)
+    for _ in range(warmup):
+        st.stepforward(s)
+    times = []
+    for _ in range(steps):
+        t0 = time.perf_counter()
+        st.stepforward(s)
+        times.append(time.perf_counter() - t0)
+    return times, s
+
+
+def cpu_baseline(n: int, steps: int = 2):
+    """The CPU restatement of the reference path timed on this host's cores, on bounded samples:
+    whole RK4 steps of the benchmark workload, and the reference's own CPU case (Taylor-Green
+    32^3, nu = eta = 1e-2, dt = 1e-3, 100 RK4 steps) with per-step p50 / p99."""
+    from oracle import mhd_oracle as mo
+
+    os.environ.setdefault("MHD_ORACLE_WORKERS", str(os.cpu_count()))
+    times, _ = _cpu_steps(n, initial_state(n), NU, ETA, DT, steps, 1)
+    el = sum(times) / len(times)
+    g32 = mo.Grid(32, dtype=np.float64)
+    tg = mo.physical_to_state(g32, mo.taylor_green(g32))
+    t32, _ = _cpu_steps(32, tg, 1e-2, 1e-2, 1e-3, 100, 2)
+    return {"value": n ** 3 / el, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
+            "ms_per_step": el * 1e3, "p50_ms": 1e3 * float(np.percentile(times, 50)),
+            "p99_ms": 1e3 * float(np.percentile(times, 99)),
+            "sample": f"{steps} whole RK4 steps (4 right-hand sides each) at {n}^3 after 1 warm-up step; oracle literal "
+                      f"restatement of the reference path, scipy.fft float32, workers={os.cpu_count()}",
+            "taylor_green_32": {"steps": 100, "ms_per_step": 1e3 * sum(t32) / len(t32),
+                                "p50_ms": 1e3 * float(np.percentile(t32, 50)),
+                                "p99_ms": 1e3 * float(np.percentile(t32, 99)),
+                                "grid_pt_steps_per_s": 32 ** 3 * len(t32) / sum(t32),
+                                "reference_readme_s_per_step": 0.049}}
+
+
+def run_forms(args, pkg, lib, local):
+    """The spec forms beside the plain FP32 step, each at 256^3 on the same workload:
+    split TF32 (tcgen05) and FP16 / BF16 (mma.sync) tensor-core x rows (ms per step and relative L2 of
+    the state after 20 steps against the plain form from the same state) and LSRK4 (ms per step)."""
+    chk = pkg._lib.check
+    n, K = 256, 20
+    s0 = initial_state(n)
+    out, states = {}, {}
+    for name, prec, scheme in (("plain_fp32", "fp32", "RK4"), ("split_tf32", "split_tf32", "RK4"),
+                               ("split_fp16", "split_fp16", "RK4"), ("split_bf16", "split_bf16", "RK4"),
+                               ("lsrk4", "fp32", "LSRK4")):
+        p = pkg.Problem(pkg.GPU(local), nx=n, Lx=2 * math.pi, nu=NU, eta=ETA, dt=DT, stepper=scheme, precision=prec)
+        p.set_sol(s0.T)
+        pkg.autotune(p)
+        pkg.stepforward(p, K)  # the accuracy run from s0 (also warms up)
+        if scheme == "RK4":
+            states[name] = p.sol_c()
+        arr = (C.c_double * K)()
+        chk(lib.mhd_step_timed(p.handle, K, arr))
+        ms = list(arr)
+        out[name] = {"ms_per_step": sum(ms) / K, "p50_ms": float(np.percentile(ms, 50)),
+                     "p99_ms": float(np.percentile(ms, 99)), "grid_pt_steps_per_s": n ** 3 / (sum(ms) / K / 1e3)}
+        p.close()
+    ref = states["plain_fp32"]
+    den = float(np.linalg.norm(ref.ravel()))
+    for name in ("split_tf32", "split_fp16", "split_bf16"):
+        out[name]["rel_l2_vs_plain_after_20_steps"] = float(np.linalg.norm((states[name] - ref).ravel()) / den)
+        out[name]["speedup_vs_plain"] = out["plain_fp32"]["ms_per_step"] / out[name]["ms_per_step"]
+    out["lsrk4"]["note"] = "five right-hand sides per step"
+    return out
 
 
 def main():
@@ -450,7 +529,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--grid", dest="n", type=int, default=256, help="grid points per axis of the step workload")
-    ap.add_argument("--precision", default="fp32", choices=["fp32", "split_fp16", "split_bf16"],
+    ap.add_argument("--precision", default="fp32", choices=["fp32", "split_tf32", "split_fp16", "split_bf16"],
                     help="x-row transforms in FP32 (plain form) or as split 16-bit tensor-core DFTs")
     ap.add_argument("--scheme", default="RK4", choices=["RK4", "LSRK4"], help="time stepper of the step workload")
     ap.add_argument("--hydro", action="store_true", help="hydrodynamic problem (B_field = false)")
@@ -458,9 +537,13 @@ def main():
     ap.add_argument("--vp", action="store_true", help="volume penalisation on (VP_method, a ball obstacle)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-secondary", dest="secondary", action="store_false")
+    ap.add_argument("--no-extras", dest="extras", action="store_false",
+                    help="skip the split-precision / LSRK4 forms, the ensemble and the serving summary")
     ap.add_argument("--workload", default="step", choices=["step", "ensemble", "serve"])
     ap.add_argument("--serve-count", type=int, default=300)
     ap.add_argument("--serve-scale", type=float, default=0.2, help="scale of the 100..2000 steps range")
+    ap.add_argument("--no-native", dest="native", action="store_false",
+                    help="serving: skip the run through the C++ scheduler (mhd_server_*)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     rank, world, local = dist_env()
@@ -479,32 +562,22 @@ def main():
         if rank != 0:
             return 0
         os.environ.setdefault("MHD_ORACLE_WORKERS", str(os.cpu_count()))
-        from oracle import mhd_oracle as mo
-
         n = args.n
-        g = mo.Grid(n, dtype=np.float32)
-        s = initial_state(n)
-        N = np.zeros_like(s)
-        for _ in range(args.warmup):
-            mo.calcN_literal(N, s.copy(), g, NU, ETA)
-        times = []
-        for _ in range(args.steps):
-            t0 = time.perf_counter()
-            mo.calcN_literal(N, s, g, NU, ETA)
-            s2 = s + np.float32(DT / 2) * N
-            times.append(time.perf_counter() - t0)
-        stage = sum(times) / len(times)
-        value = n ** 3 / (4 * stage)
+        times, final = _cpu_steps(n, initial_state(n), NU, ETA, DT, args.steps, args.warmup)
+        el = sum(times)
+        value = n ** 3 * len(times) / el
         line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
-                "steps": args.steps, "warmup": args.warmup, "ms_per_step": 4 * stage * 1e3, "higher_is_better": True,
-                "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": el / len(times) * 1e3,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
                 "config": config,
                 "cpu_baseline": {"value": value, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
-                                 "sample": f"each step = one RK4 stage (RHS evaluation + stage update) at {n}^3, "
-                                           "scaled x4 to an RK4 step; oracle literal restatement, scipy.fft float32, "
+                                 "sample": f"{args.steps} whole RK4 steps (4 right-hand sides each) at {n}^3 after "
+                                           f"{args.warmup} warm-up steps; oracle literal restatement of the reference "
+                                           f"path (30 r2c + 6 c2r per right-hand side), scipy.fft float32, "
                                            f"workers={os.cpu_count()}"},
                 "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-                "p50_ms": 4e3 * float(np.percentile(times, 50)), "p99_ms": 4e3 * float(np.percentile(times, 99))}
+                "p50_ms": 1e3 * float(np.percentile(times, 50)), "p99_ms": 1e3 * float(np.percentile(times, 99)),
+                "finite": bool(np.isfinite(final).all())}
         print(json.dumps(line), flush=True)
         return 0
 
@@ -542,6 +615,21 @@ def main():
         }
         if r["secondary"]:
             line["secondary"] = r["secondary"]
+        if r["forms"]:
+            line["forms"] = r["forms"]
+        if args.extras and world == 1:
+            ens_args = argparse.Namespace(steps=200, warmup=3)
+            e = run_ensemble(ens_args)
+            line["ensemble"] = {k: e[k] for k in ("value", "unit", "steps", "ms_per_ensemble_step", "plain_one_at_a_time",
+                                                  "speedup_vs_plain", "boxes", "finite")}
+            line["ensemble"]["workload"] = e["config"]["workload"] + ", LSRK4, dt = 0.2 dx / u_rms, 200 steps"
+            sv_args = argparse.Namespace(serve_count=120, serve_scale=0.25, native=False)
+            sv = run_serve(sv_args)
+            line["serving"] = {k: sv[k] for k in ("value", "unit", "p50_latency_s", "p99_latency_s", "makespan_s", "done",
+                                                 "failed", "peak_active", "plain_one_at_a_time", "speedup_vs_plain")}
+            line["serving"]["workload"] = ("Poisson requests at 20/s, N in {32,48,64,128,256}^3 with p = "
+                                           "{.3,.25,.2,.15,.1}, 120 requests, steps U[25, 500] (the configuration's "
+                                           "[100, 2000] scaled by 0.25, so that a backlog forms), 150 GB budget")
         print(json.dumps(line), flush=True)
     dist.close()
     return 0

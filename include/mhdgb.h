@@ -52,6 +52,8 @@ extern "C" {
 #define MHD_PREC_FP32 0        /* FP32 everywhere (the reference's T = Float32) */
 #define MHD_PREC_SPLIT_FP16 1  /* x-row transforms as tensor-core DFT products, FP16 hi+lo operands */
 #define MHD_PREC_SPLIT_BF16 2  /* the same with BF16 hi+lo operands (n = 128, 256, 512 only) */
+#define MHD_PREC_SPLIT_TF32 3  /* x-row transforms as tcgen05 tensor-core DFT products with TF32 hi+lo
+                                  operands, data operand in tensor memory (n = 256 only) */
 
 typedef struct mhd_params {
   int n;          /* grid points per axis (nx = ny = nz); supported: 16,32,48,64,96,128,256,512 */
@@ -62,7 +64,7 @@ typedef struct mhd_params {
   int neta;       /* hyper-resistivity order; values > 1 are rejected */
   double dt;      /* fixed time step */
   int scheme;     /* MHD_RK4 or MHD_LSRK4 */
-  int precision;  /* MHD_PREC_FP32, MHD_PREC_SPLIT_FP16 or MHD_PREC_SPLIT_BF16 */
+  int precision;  /* MHD_PREC_FP32, MHD_PREC_SPLIT_FP16, MHD_PREC_SPLIT_BF16 or MHD_PREC_SPLIT_TF32 */
   int device;     /* CUDA device ordinal */
   int hydro_only; /* 0: MHD (B_field = true, 6 fields); 1: hydrodynamics (B_field = false,
                      HDcalcN! of src/pgen.jl:176-182: 3 fields ux, uy, uz; the state layout of
@@ -88,6 +90,17 @@ int mhd_kept_modes(int n, int* kx, int* kp, int* kn);
  * set_state keeps only the retained (de-aliased) band; get_state writes zeros in the alias band. */
 int mhd_set_state(mhd_handle h, const float* sol);
 int mhd_get_state(mhd_handle h, float* sol);
+
+/* prob.sol as a device array (a CuArray of MHDFlows' Problem(GPU(); ...), src/Problems.jl:130,
+ * whose stepforward! updates it in place, src/timestepper/timestepper.jl:4-6): the same layout as
+ * mhd_set_state, 16-byte aligned device memory, read or written by a kernel on the device.
+ * The kernel runs on `stream`, the caller's cudaStream_t (0 is the legacy default stream; pass
+ * mhd_get_stream(h) to stay on the handle's stream), after the handle's earlier work, and the
+ * handle's later work waits for it.  Neither call synchronises the host: work the caller issues
+ * on `stream` afterwards sees the transfer complete.  get_state_device writes every element
+ * (zeros in the alias band). */
+int mhd_set_state_device(mhd_handle h, const float* sol_dev, void* stream);
+int mhd_get_state_device(mhd_handle h, float* sol_dev, void* stream);
 
 /* SetUpProblemIC!: physical field (n, n, n) float32 column-major -> forward r2c into sol[:,:,:,field]. */
 int mhd_set_physical(mhd_handle h, int field, const float* phys);
@@ -162,6 +175,8 @@ int mhd_batch_info(mhd_handle h, int* capacity, int* active);
 int mhd_slot_bytes(const mhd_params* params, long long* per_slot, long long* per_class);
 int mhd_slot_set_state(mhd_handle h, int slot, const float* sol);
 int mhd_slot_get_state(mhd_handle h, int slot, float* sol);
+int mhd_slot_set_state_device(mhd_handle h, int slot, const float* sol_dev, void* stream);
+int mhd_slot_get_state_device(mhd_handle h, int slot, float* sol_dev, void* stream);
 int mhd_slot_set_physical(mhd_handle h, int slot, int field, const float* phys);
 int mhd_slot_get_physical(mhd_handle h, int slot, int field, float* phys);
 int mhd_slot_diagnostics(mhd_handle h, int slot, double* out, int nout);
@@ -307,17 +322,21 @@ int mhd_variant_count(mhd_handle h, int cls, int* count);
 int mhd_variant_name(mhd_handle h, int cls, int idx, char* buf, int len);
 int mhd_select_variant(mhd_handle h, int cls, int idx);
 
-/* Allocation-free spectral diagnostics (no counterpart in the reference).  For callers that may
- * not allocate device memory (inside a graph capture, a stream callback, a real-time loop, or a
- * host whose device memory belongs to another allocator): reads sol_dev, a device copy of
- * prob.sol (complex64, column-major (n/2+1, n, n, 6), the mhd_set_state layout), and writes to
- * out_dev[0..6) on the device: E_u, E_B, H_c (sums over the retained band times dV, like
- * mhd_diagnostics), max|k.u_hat|, max|k.B_hat|, non-finite count.  Launches on `stream`
- * (a cudaStream_t, NULL = default stream) and does not synchronise.  The only scratch is a
- * static 58,368-byte device array inside the library (partial sums of at most 1216 blocks);
- * n must be a supported size (16..512).  The first call on each device resolves that array's
- * address with cudaGetSymbolAddress, so make it before any stream capture; calls that overlap
- * on the GPU share the array and race. */
+/* Allocation-free spectral diagnostics (no counterpart in the reference).  For callers that
+ * cannot allocate device memory: a Julia program whose CuArrays come from CUDA.jl's pool or a
+ * Python program whose tensors come from PyTorch's caching allocator, where all device memory
+ * is meant to go through that pool; real-time loops that must not block on the allocator.
+ * Reads sol_dev, a device copy of prob.sol (complex64, column-major (n/2+1, n, n, 6), the
+ * mhd_set_state layout), and writes to out_dev[0..6) on the device: E_u, E_B, H_c (sums over the
+ * retained band times dV, like mhd_diagnostics), max|k.u_hat|, max|k.B_hat|, non-finite count.
+ * Launches on `stream` (a cudaStream_t, NULL = default stream) and does not synchronise.  It
+ * calls no allocator; its only scratch is a static 58,368-byte device array inside the library
+ * (partial sums of at most 1216 blocks; larger grids are covered by a grid-stride loop), which
+ * every GPU that loads the library holds until the process exits.  n must be a supported size
+ * (16, 32, 48, 64, 96, 128, 256, 512); others are rejected with MHD_ERR_INVALID.  The first call
+ * in each CUDA context (for runtime users: on each device) looks up that array's address with
+ * cudaGetSymbolAddress, so make it before any stream capture.  All calls share the array: calls
+ * that overlap on the GPU (two streams, two host threads) race on it. */
 int mhd_diagnostics_noalloc(const float* sol_dev, int n, double L, double* out_dev, void* stream);
 
 /* Last error message of the calling thread ("" if none). */

@@ -65,16 +65,17 @@ def kept_modes(n: int):
     return a.value, b.value, c.value
 
 
-PRECISIONS = {"fp32": 0, "split_fp16": 1, "split_bf16": 2}
+PRECISIONS = {"fp32": 0, "split_fp16": 1, "split_bf16": 2, "split_tf32": 3}
 
 
 def _precision(precision) -> int:
-    """Precision form: "fp32" (plain), "split_fp16" or "split_bf16" (tensor-core x-row DFTs)."""
+    """Precision form: "fp32" (plain), "split_fp16" / "split_bf16" (mma.sync tensor-core x-row DFTs) or
+    "split_tf32" (tcgen05 tensor-core x-row DFTs, n = 256)."""
     if isinstance(precision, int) and precision in PRECISIONS.values():
         return precision
     key = str(precision).lower()
     if key not in PRECISIONS:
-        raise MHDError(_lib.MHD_ERR_INVALID, f"unknown precision {precision!r} (fp32, split_fp16, split_bf16)")
+        raise MHDError(_lib.MHD_ERR_INVALID, f"unknown precision {precision!r} (fp32, split_fp16, split_bf16, split_tf32)")
     return PRECISIONS[key]
 
 

@@ -26,6 +26,7 @@ MHD_DIV_B = 2
 MHD_PREC_FP32 = 0
 MHD_PREC_SPLIT_FP16 = 1
 MHD_PREC_SPLIT_BF16 = 2
+MHD_PREC_SPLIT_TF32 = 3
 MHD_TUNE_FORCE = 1
 MHD_TUNE_NO_FILE = 2
 
@@ -113,6 +114,10 @@ _SIGS = {
     "mhd_slot_bytes": (C.c_int, [C.POINTER(MhdParams), C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)]),
     "mhd_slot_set_state": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p]),
     "mhd_slot_get_state": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p]),
+    "mhd_set_state_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    "mhd_get_state_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    "mhd_slot_set_state_device": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]),
+    "mhd_slot_get_state_device": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]),
     "mhd_slot_set_physical": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_void_p]),
     "mhd_slot_get_physical": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_void_p]),
     "mhd_slot_diagnostics": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_double), C.c_int]),

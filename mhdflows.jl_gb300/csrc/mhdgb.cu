@@ -17,6 +17,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdint>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -106,7 +107,7 @@ const double kLsB[5] = {1432997174477.0 / 9575080441755.0, 5161836677717.0 / 136
 
 struct Sizes {
   long long fs;      // one compact field (complex)
-  long long state;   // six fields (slot stride of sol / xs / acc)
+  long long state;   // six fields (slot stride of sol / xs / xs2 / acc)
   long long colbuf;  // colbuf complex elements per slot
   long long rowbuf;  // rowbuf complex elements per slot
   long long ref;     // reference-layout sol (complex)
@@ -131,7 +132,7 @@ Sizes sizes_of(const Geom& g, int ns) {
 // fields) and of the per-class staging.
 long long slot_bytes(const Geom& g, bool vp = false, bool hydro = false) {
   Sizes s = sizes_of(g, slots_of(vp && !hydro));
-  return (3 * s.state + s.fs + s.colbuf + s.rowbuf) * 8 + 16 * 4 + (vp ? 7 * s.phys * 4 : 0);
+  return (4 * s.state + s.fs + s.colbuf + s.rowbuf) * 8 + 16 * 4 + (vp ? 7 * s.phys * 4 : 0);
 }
 long long class_bytes(const Geom& g) {
   Sizes s = sizes_of(g, 8);
@@ -281,6 +282,9 @@ struct mhd_problem {
   // slot pools
   float2* sol = nullptr;
   float2* xs = nullptr;
+  // second RK4 stage-state buffer: the stages alternate xs / xs2, so no epilogue overwrites the
+  // stage state it reads, and the kx = 0 plane's Hermitian part is formed inline (no herm_kx0)
+  float2* xs2 = nullptr;
   float2* acc = nullptr;
   float2* aux = nullptr;
   float2* colbuf = nullptr;
@@ -311,7 +315,7 @@ struct mhd_problem {
   bool divcorr = false;
   // TMA sources of the column passes (used when a TMA-fed variant is selected) and the device
   // word a timed-out tile wait is recorded in
-  TmaPass tm_zinv_sol, tm_zinv_xs, tm_yinv, tm_yfwd, tm_zfwd;
+  TmaPass tm_zinv_sol, tm_zinv_xs, tm_zinv_xs2, tm_yinv, tm_yfwd, tm_zfwd;
   int* derr = nullptr;
   bool cfl = false;
   double cfl_coef = 0.3;
@@ -324,6 +328,22 @@ struct mhd_problem {
   bool list_dirty = true;
   // step graph
   cudaGraphExec_t graph = nullptr;
+  // ordering events of the device-pointer state transfers (created on first use)
+  cudaEvent_t ev_in = nullptr, ev_out = nullptr;
+  // source of the copy-engine zeros of get_state into mapped host memory (created on first use):
+  // a zeroed device buffer and the side stream its copies run on
+  void* zeros = nullptr;
+  size_t zbytes = 0;
+  cudaStream_t zstream = nullptr;
+  int ensure_zero_source() {
+    if (zeros) return MHD_OK;
+    const size_t want = size_t(16) << 20;
+    MHD_CUDA(cudaMalloc(&zeros, want));
+    MHD_CUDA(cudaMemset(zeros, 0, want));
+    zbytes = want;
+    if (!zstream) MHD_CUDA(cudaStreamCreateWithFlags(&zstream, cudaStreamNonBlocking));
+    return MHD_OK;
+  }
   // guard bands: every large buffer is allocated kGuardBytes longer and the tail filled with
   // kGuardByte, so that a kernel writing past a buffer's end shows up in mhd_check_guards
   static constexpr size_t kGuardBytes = 4096;
@@ -372,11 +392,18 @@ struct mhd_problem {
     recs.clear();
     for (auto e : pool) cudaEventDestroy(e);
     pool.clear();
-    void* ptrs[] = {sol, xs, acc, aux, colbuf, rowbuf, ref, phys, diag_partial, diag_out, maxabs, dparams, dlist, dvmax, dtime,
+    if (ev_in) cudaEventDestroy(ev_in);
+    if (ev_out) cudaEventDestroy(ev_out);
+    ev_in = ev_out = nullptr;
+    if (zstream) cudaStreamSynchronize(zstream), cudaStreamDestroy(zstream);
+    if (zeros) cudaFree(zeros);
+    zstream = nullptr;
+    zeros = nullptr;
+    void* ptrs[] = {sol, xs, xs2, acc, aux, colbuf, rowbuf, ref, phys, diag_partial, diag_out, maxabs, dparams, dlist, dvmax, dtime,
                     dstep, derr, vchi, vwall};
     for (void* q : ptrs) if (q) cudaFree(q);
     vchi = vwall = nullptr;
-    sol = xs = acc = aux = colbuf = rowbuf = ref = nullptr;
+    sol = xs = xs2 = acc = aux = colbuf = rowbuf = ref = nullptr;
     guards.clear();
     phys = nullptr; diag_partial = nullptr; diag_out = nullptr; maxabs = nullptr; dparams = nullptr; dlist = nullptr;
     dvmax = nullptr; dtime = nullptr; dstep = nullptr; derr = nullptr;
@@ -446,7 +473,9 @@ struct mhd_problem {
   int z_inverse(const float2* src, long long sI, int nf, BatchRef br) {
     ColArgs a{src, colbuf, FS(), (long long)g.kxp, (long long)g.k2 * g.kxp, (long long)g.kxp, SLK(), AZ(), sI, sz.colbuf};
     // the maps cover all six fields of a pool: only the right-hand side's call can use them
-    const TmaPass* tp = (nf == 6 && sI == ST()) ? (src == sol ? &tm_zinv_sol : src == xs ? &tm_zinv_xs : nullptr) : nullptr;
+    const TmaPass* tp = (nf == 6 && sI == ST())
+                            ? (src == sol ? &tm_zinv_sol : src == xs ? &tm_zinv_xs : src == xs2 ? &tm_zinv_xs2 : nullptr)
+                            : nullptr;
     return launch(KC_ZINV, [&] { ops->col(KC_ZINV, a, g, g.k2, nf, br, cap, stream, tp); });
   }
   int y_inverse(int nf, BatchRef br) {
@@ -476,14 +505,14 @@ struct mhd_problem {
       herm_kx0_kernel<<<gh, bxh, 0, stream>>>(X, aux, g, FS(), ST(), FS(), br);
     });
   }
-  RkArgs rk_args(const float2* X, int op, float hf, float ca, float cb, int stage) const {
+  RkArgs rk_args(const float2* X, float2* xn, int op, float hf, float ca, float cb, int stage, bool inline_herm) const {
     RkArgs a{};
     a.prod = rowbuf;
     a.X = X;
-    a.H = aux;
+    a.H = inline_herm ? nullptr : aux;
     a.sol = sol;
     a.acc = acc;
-    a.xn = (op == OP_LS_FIRST || op == OP_LS) ? sol : xs;
+    a.xn = xn;
     a.sp = dparams;
     a.fs = FS();
     a.stI = ST();
@@ -504,10 +533,14 @@ struct mhd_problem {
   // HDcalcN! (src/pgen.jl:176-182) calls addforcing! before HDcalcN_advection!, whose UᵢUpdate!
   // starts by zeroing the velocity right-hand side: a hydrodynamic problem is unforced
   bool forced() const { return forcing && !p.hydro_only; }
-  int epilogue(const float2* X, int op, float hf, float ca, float cb, BatchRef br, int stage) {
-    int rc = herm(X, br);
+  // xn: where the stage update writes (the next stage state, or sol).  When it is not the stage
+  // state X itself, X stays unchanged during the epilogue and each kx = 0 mode reads its partner
+  // mode's value directly; otherwise herm_kx0 first copies the Hermitian part of X's kx = 0 plane.
+  int epilogue(const float2* X, float2* xn, int op, float hf, float ca, float cb, BatchRef br, int stage) {
+    const bool inline_herm = xn != X;
+    int rc = inline_herm ? MHD_OK : herm(X, br);
     if (rc) return rc;
-    const RkArgs a = rk_args(X, op, hf, ca, cb, stage);
+    const RkArgs a = rk_args(X, xn, op, hf, ca, cb, stage, inline_herm);
     const int bx = g.kx <= 256 ? (g.kx + 31) / 32 * 32 : 256;
     const dim3 grid((g.kx + bx - 1) / bx, g.k2, g.k2 * cap);
     const bool f = forced(), v = p.vp != 0;
@@ -539,7 +572,7 @@ struct mhd_problem {
     return launch(KC_OTHER, [&] { div_correct_kernel<<<grid, bx, 0, stream>>>(sol, g, FS(), ST(), br, mask); });
   }
   // stage: right-hand-side evaluation within the step (7 outside a step)
-  int rhs(const float2* X, int op, float hf, float ca, float cb, BatchRef br, int stage, bool record = false) {
+  int rhs(const float2* X, float2* xn, int op, float hf, float ca, float cb, BatchRef br, int stage, bool record = false) {
     int rc;
     const int nin = hd_form() ? 3 : 6, nout = hd_form() ? (p.vp ? 8 : 5) : ns;
     if ((rc = z_inverse(X, ST(), nin, br))) return rc;
@@ -547,20 +580,21 @@ struct mhd_problem {
     if ((rc = x_fused(br, (record && cfl) ? dvmax : nullptr))) return rc;
     if ((rc = y_forward(nout, br))) return rc;
     if ((rc = z_forward(rowbuf, sz.rowbuf, nout, br))) return rc;
-    return epilogue(X, op, hf, ca, cb, br, stage);
+    return epilogue(X, xn, op, hf, ca, cb, br, stage);
   }
   // One step of every active slot (launches only; see run_steps for graphs and clocks).
   int issue_step(bool with_diag = false) {
     const BatchRef br = active_ref();
     int rc;
     if (p.scheme == MHD_RK4) {
-      if ((rc = rhs(sol, OP_RK4_FIRST, 0.5f, 0.f, 0.f, br, 0))) return rc;
-      if ((rc = rhs(xs, OP_RK4_MID, 0.5f, 0.f, 0.f, br, 1))) return rc;
-      if ((rc = rhs(xs, OP_RK4_MID, 1.0f, 0.f, 0.f, br, 2))) return rc;
-      if ((rc = rhs(xs, OP_RK4_LAST, 0.f, 0.f, 0.f, br, 3, true))) return rc;
+      // stage states alternate between xs and xs2 (the last stage writes sol)
+      if ((rc = rhs(sol, xs, OP_RK4_FIRST, 0.5f, 0.f, 0.f, br, 0))) return rc;
+      if ((rc = rhs(xs, xs2, OP_RK4_MID, 0.5f, 0.f, 0.f, br, 1))) return rc;
+      if ((rc = rhs(xs2, xs, OP_RK4_MID, 1.0f, 0.f, 0.f, br, 2))) return rc;
+      if ((rc = rhs(xs, sol, OP_RK4_LAST, 0.f, 0.f, 0.f, br, 3, true))) return rc;
     } else {
       for (int i = 0; i < 5; ++i)
-        if ((rc = rhs(sol, i == 0 ? OP_LS_FIRST : OP_LS, 0.f, (float)kLsA[i], (float)kLsB[i], br, i, i == 4))) return rc;
+        if ((rc = rhs(sol, sol, i == 0 ? OP_LS_FIRST : OP_LS, 0.f, (float)kLsA[i], (float)kLsB[i], br, i, i == 4))) return rc;
     }
     if (forcing && (rc = launch(KC_OTHER, [&] {
           step_tick_kernel<<<(cap + 127) / 128, 128, 0, stream>>>(br, dstep);
@@ -643,7 +677,7 @@ struct mhd_problem {
             if ((rc = fold_records())) break;
             for (int c = 0; c < KC_COUNT; ++c) { prof_launches[c] = 0; prof_ms[c] = 0; }
           }
-          rc = rhs(sol, OP_RHS, 0.f, 0.f, 0.f, br, 7);
+          rc = rhs(sol, acc, OP_RHS, 0.f, 0.f, 0.f, br, 7);
         }
         if (rc == MHD_OK) rc = fold_records();
         for (int c = 0; c < kTunedClasses && rc == MHD_OK; ++c)
@@ -785,6 +819,7 @@ struct mhd_problem {
     const cuuint32_t bz[5] = {16, 1, kp, 1, 1};
     set(tm_zinv_sol, sol, dz, sz5, bz, TmaCoords{2, 1, 3, 4, (int)kp});
     set(tm_zinv_xs, xs, dz, sz5, bz, TmaCoords{2, 1, 3, 4, (int)kp});
+    set(tm_zinv_xs2, xs2, dz, sz5, bz, TmaCoords{2, 1, 3, 4, (int)kp});
     // colbuf [slot][z][ky'][ns][kx] and rowbuf [slot][z][y][ns][kx]
     const cuuint64_t S = ns;
     const cuuint64_t dc[5] = {kxp, S, k2, n, C};
@@ -803,6 +838,7 @@ struct mhd_problem {
     int e = 0;
     MHD_CUDA(cudaMemcpy(&e, derr, sizeof(int), cudaMemcpyDeviceToHost));
     if (e) return fail(MHD_ERR_CUDA, e == 2 ? "TMA buffer misaligned in shared memory" : "a TMA tile wait timed out on the device");
+    if (ops->x_device_error()) return fail(MHD_ERR_CUDA, "a tensor-core completion wait of the x rows timed out on the device");
     return MHD_OK;
   }
   // Hydrodynamics runs the MHD kernels with B = 0: the epilogue sets the induction right-hand
@@ -842,10 +878,15 @@ int validate(const mhd_params* p) {
   if (!std::isfinite(p->dt)) return fail(MHD_ERR_INVALID, "dt must be finite");
   if (p->scheme != MHD_RK4 && p->scheme != MHD_LSRK4) return fail(MHD_ERR_INVALID, "scheme must be MHD_RK4 or MHD_LSRK4");
   if (p->hydro_only != 0 && p->hydro_only != 1) return fail(MHD_ERR_INVALID, "hydro_only must be 0 or 1");
-  if (p->precision != MHD_PREC_FP32 && p->precision != MHD_PREC_SPLIT_FP16 && p->precision != MHD_PREC_SPLIT_BF16)
-    return fail(MHD_ERR_INVALID, "precision must be MHD_PREC_FP32, MHD_PREC_SPLIT_FP16 or MHD_PREC_SPLIT_BF16");
-  if (p->precision != MHD_PREC_FP32 && p->n != 128 && p->n != 256 && p->n != 512)
-    return fail(MHD_ERR_INVALID, "the split-precision tensor-core forms exist for n = 128, 256, 512");
+  if (p->precision != MHD_PREC_FP32 && p->precision != MHD_PREC_SPLIT_FP16 && p->precision != MHD_PREC_SPLIT_BF16 &&
+      p->precision != MHD_PREC_SPLIT_TF32)
+    return fail(MHD_ERR_INVALID,
+                "precision must be MHD_PREC_FP32, MHD_PREC_SPLIT_FP16, MHD_PREC_SPLIT_BF16 or MHD_PREC_SPLIT_TF32");
+  if ((p->precision == MHD_PREC_SPLIT_FP16 || p->precision == MHD_PREC_SPLIT_BF16) && p->n != 128 && p->n != 256 &&
+      p->n != 512)
+    return fail(MHD_ERR_INVALID, "the split FP16 / BF16 tensor-core forms exist for n = 128, 256, 512");
+  if (p->precision == MHD_PREC_SPLIT_TF32 && p->n != 256)
+    return fail(MHD_ERR_INVALID, "the split TF32 tcgen05 form exists for n = 256");
   if (p->vp != 0 && p->vp != 1) return fail(MHD_ERR_INVALID, "vp must be 0 or 1");
   if (p->vp && p->precision != MHD_PREC_FP32)
     return fail(MHD_ERR_INVALID, "volume penalisation runs in the FP32 form only");
@@ -892,6 +933,7 @@ int create_class(const mhd_params* params, int cap, mhd_handle* out) {
   const size_t c = (size_t)cap;
   MHD_CUDA(h->alloc_guarded(&h->sol, c * s.state * sizeof(float2)));
   MHD_CUDA(h->alloc_guarded(&h->xs, c * s.state * sizeof(float2)));
+  MHD_CUDA(h->alloc_guarded(&h->xs2, c * s.state * sizeof(float2)));
   MHD_CUDA(h->alloc_guarded(&h->acc, c * s.state * sizeof(float2)));
   MHD_CUDA(h->alloc_guarded(&h->aux, c * s.fs * sizeof(float2)));
   MHD_CUDA(h->alloc_guarded(&h->colbuf, c * s.colbuf * sizeof(float2)));
@@ -913,6 +955,7 @@ int create_class(const mhd_params* params, int cap, mhd_handle* out) {
   MHD_CUDA(cudaMemsetAsync(h->dtime, 0, c * sizeof(double), h->stream));
   MHD_CUDA(cudaMemsetAsync(h->sol, 0, c * s.state * sizeof(float2), h->stream));
   MHD_CUDA(cudaMemsetAsync(h->xs, 0, c * s.state * sizeof(float2), h->stream));
+  MHD_CUDA(cudaMemsetAsync(h->xs2, 0, c * s.state * sizeof(float2), h->stream));
   MHD_CUDA(cudaMemsetAsync(h->acc, 0, c * s.state * sizeof(float2), h->stream));
   if (params->vp) {
     MHD_CUDA(h->alloc_guarded(&h->vchi, c * s.phys * sizeof(float)));
@@ -1053,26 +1096,24 @@ void* mapped_host(const void* p, size_t bytes) {
   return a0.devicePointer;
 }
 
-// Zero every element of a reference-layout state (nf, n, n, nkr) outside the retained band (the
-// complement of scatter_retained_kernel), on up to 16 host threads, plane by plane.  The alias
-// band of an axis is the contiguous frequency range [kp, n - kn): a plane with kz in it is all
-// zero; a kept plane has one block of alias rows and, in each kept row, the tail kx >= Kx.
-void zero_outside_retained(float2* ref, const Geom& g, int nf) {
+// The alias band of a reference-layout state (nf, n, n, nkr) outside the retained band (the
+// complement of scatter_retained_kernel) has three parts per field: the z-planes of the alias
+// band [kp, n - kn), a block of alias rows [kp, n - kn) in every kept z-plane, and the tail
+// kx >= Kx of every kept row.  zero_row_tails zeroes the tails on host threads; the planes and
+// row blocks go to the copy engine (zero_alias_blocks).
+void zero_row_tails(float2* ref, const Geom& g, int nf) {
   const size_t nkr = g.n / 2 + 1, row = nkr * sizeof(float2), plane = (size_t)g.n * row;
-  const size_t za = (size_t)(g.n - g.kp - g.kn), tail = (nkr - g.kx) * sizeof(float2);
-  const int planes = nf * g.n;
+  const size_t tail = (nkr - g.kx) * sizeof(float2);
+  const int planes = nf * g.k2;  // kept z-planes of every field
   auto zero_plane = [&](int q) {
-    char* p = reinterpret_cast<char*>(ref) + (size_t)q * plane;
-    const int fz = q % g.n;
-    if (kept_of_freq(g, fz) < 0) { std::memset(p, 0, plane); return; }
-    std::memset(p + (size_t)g.kp * row, 0, za * row);
+    const int f = q / g.k2, jz = q % g.k2;
+    char* p = reinterpret_cast<char*>(ref) + ((size_t)f * g.n + freq_of_kept(g, jz)) * plane;
     for (int j = 0; j < g.k2; ++j) std::memset(p + (size_t)freq_of_kept(g, j) * row + g.kx * sizeof(float2), 0, tail);
   };
-  // one thread per 16 MB to zero, at most 16 and at most the hardware threads
-  const size_t zero_bytes = (size_t)nf * g.n * plane - (size_t)nf * g.k2 * g.k2 * g.kx * sizeof(float2);
+  // one thread per 4 MB of tails, at most 16 and at most the hardware threads
+  const size_t bytes = (size_t)planes * g.k2 * tail;
   const unsigned hw = std::thread::hardware_concurrency();
-  const size_t want = std::max<size_t>(1, std::min<size_t>(16, zero_bytes >> 24));
-  const int nt = (int)std::min<size_t>(want, hw ? hw : 1);
+  const int nt = (int)std::min<size_t>(std::max<size_t>(1, std::min<size_t>(16, bytes >> 22)), hw ? hw : 1);
   auto work = [&](int t) {
     for (int q = t; q < planes; q += nt) zero_plane(q);
   };
@@ -1080,6 +1121,90 @@ void zero_outside_retained(float2* ref, const Geom& g, int nf) {
   for (int t = 1; t < nt; ++t) pool.emplace_back(work, t);
   work(0);
   for (auto& th : pool) th.join();
+}
+
+// Copy-engine writes of zeros from `zeros` (zbytes of zeroed device memory) into the alias planes
+// and the alias row blocks of a host reference-layout state, on stream s.
+cudaError_t zero_alias_blocks(float2* ref, const Geom& g, int nf, const void* zeros, size_t zbytes, cudaStream_t s) {
+  const size_t nkr = g.n / 2 + 1, row = nkr * sizeof(float2), plane = (size_t)g.n * row;
+  const size_t na = (size_t)(g.n - g.kp - g.kn);
+  char* base = reinterpret_cast<char*>(ref);
+  for (int f = 0; f < nf; ++f) {
+    // the alias z-planes of field f: one contiguous block, in pieces of at most zbytes
+    char* p = base + ((size_t)f * g.n + g.kp) * plane;
+    for (size_t left = na * plane; left > 0;) {
+      const size_t b = std::min(left, zbytes);
+      const cudaError_t e = cudaMemcpyAsync(p, zeros, b, cudaMemcpyDeviceToHost, s);
+      if (e != cudaSuccess) return e;
+      p += b;
+      left -= b;
+    }
+    // the alias row block of every kept z-plane: width na rows, one plane apart, in groups of
+    // planes that fit the zero buffer
+    const size_t width = na * row;
+    const size_t per = std::max<size_t>(1, zbytes / width);
+    const int z0[2] = {0, g.n - g.kn}, zc[2] = {g.kp, g.kn};
+    for (int r = 0; r < 2; ++r)
+      for (int z = 0; z < zc[r]; z += (int)per) {
+        const size_t h = std::min<size_t>(per, (size_t)(zc[r] - z));
+        char* d = base + (((size_t)f * g.n + z0[r] + z) * g.n + g.kp) * row;
+        const cudaError_t e = cudaMemcpy2DAsync(d, plane, zeros, width, width, h, cudaMemcpyDeviceToHost, s);
+        if (e != cudaSuccess) return e;
+      }
+  }
+  return cudaSuccess;
+}
+
+// How state transfers to and from page-locked host buffers mapped into the device address space
+// move their bytes ($MHDGB_HOST_TRANSFER, read once; other host memory always takes the copy path):
+//   mapped (default) kernels read and write the caller's array directly: set_state gathers the
+//          retained band over the link; get_state writes the retained band from the device while
+//          the alias-band zeros land at the same time from the copy engine (whole planes and row
+//          blocks, from a zeroed device buffer) and from host threads (the tail of each kept row).
+//          Measured on GB300 at 256^3: set 0.66 ms, and the zeros overlap the step before it.
+//   copy   the copy engines only (about 200 GB/s over the host link): set_state copies the
+//          retained band of the caller's array into the device staging array (one 3-D copy per
+//          field and ky / kz range) and gathers it there; get_state scatters into the staging
+//          array at HBM speed and brings the whole array back in one contiguous copy.
+bool mapped_transfers() {
+  static const bool m = [] {
+    const char* e = std::getenv("MHDGB_HOST_TRANSFER");
+    return !(e && std::strcmp(e, "copy") == 0);
+  }();
+  return m;
+}
+
+// The retained band of a reference-layout state (nf, n, n, nkr) between two arrays of that
+// layout: for each field, the kept ky and kz ranges [0, kp) and [n - kn, n) form four boxes of
+// kx < Kx rows (one cudaMemcpy3DAsync each).
+cudaError_t copy_retained(void* dst, const void* src, const Geom& g, int nf, cudaMemcpyKind kind, cudaStream_t s) {
+  const size_t pitch = (size_t)(g.n / 2 + 1) * sizeof(float2);
+  const int r0[2] = {0, g.n - g.kn}, rc[2] = {g.kp, g.kn};
+  for (int f = 0; f < nf; ++f)
+    for (int bz = 0; bz < 2; ++bz)
+      for (int by = 0; by < 2; ++by) {
+        if (rc[bz] == 0 || rc[by] == 0) continue;
+        cudaMemcpy3DParms p = {};
+        p.srcPtr = make_cudaPitchedPtr(const_cast<void*>(src), pitch, pitch, g.n);
+        p.dstPtr = make_cudaPitchedPtr(dst, pitch, pitch, g.n);
+        p.srcPos = make_cudaPos(0, r0[by], (size_t)f * g.n + r0[bz]);
+        p.dstPos = p.srcPos;
+        p.extent = make_cudaExtent((size_t)g.kx * sizeof(float2), rc[by], rc[bz]);
+        p.kind = kind;
+        const cudaError_t e = cudaMemcpy3DAsync(&p, s);
+        if (e != cudaSuccess) return e;
+      }
+  return cudaSuccess;
+}
+
+// Device memory (or managed memory) that kernels of the current device can use, of `bytes`.
+bool is_device_memory(const void* p) {
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
 }
 
 }  // namespace
@@ -1091,11 +1216,11 @@ int mhd_slot_set_state(mhd_handle h, int slot, const float* sol) {
   if (rc) return rc;
   if (!sol) return fail(MHD_ERR_INVALID, "null sol");
   const size_t bytes = h->ref_elems() * sizeof(float2);
-  // mapped host memory: the gather kernel reads only the retained band straight from the
-  // caller's array; otherwise the whole array is staged first
-  const float2* src = static_cast<const float2*>(mapped_host(sol, bytes));
+  const float2* src = mapped_transfers() ? static_cast<const float2*>(mapped_host(sol, bytes)) : nullptr;
   if (!src) {
-    MHD_CUDA(cudaMemcpyAsync(h->ref, sol, bytes, cudaMemcpyHostToDevice, h->stream));
+    // only the retained band crosses the link (29% of the array), into the staging array
+    const cudaError_t e = copy_retained(h->ref, sol, h->g, h->nfields(), cudaMemcpyHostToDevice, h->stream);
+    if (e != cudaSuccess) return fail(MHD_ERR_CUDA, std::string("set_state copy: ") + cudaGetErrorString(e));
     src = h->ref;
   }
   float2* dst = h->sol + slot * h->sz.state;
@@ -1110,7 +1235,7 @@ int mhd_slot_get_state(mhd_handle h, int slot, float* sol) {
   if (!sol) return fail(MHD_ERR_INVALID, "null sol");
   const float2* src = h->sol + slot * h->sz.state;
   const size_t bytes = h->ref_elems() * sizeof(float2);
-  float2* out = static_cast<float2*>(mapped_host(sol, bytes));
+  float2* out = mapped_transfers() ? static_cast<float2*>(mapped_host(sol, bytes)) : nullptr;
   if (out && bytes < (size_t(16) << 20)) {
     // small mapped buffers: the device writes every element
     if ((rc = h->launch(KC_OTHER, [&] {
@@ -1119,13 +1244,20 @@ int mhd_slot_get_state(mhd_handle h, int slot, float* sol) {
       return rc;
   } else if (out) {
     // mapped memory: the device writes the retained elements straight into it (29% of the bytes
-    // at any n) while host threads zero the rest, overlapping with whatever the stream still runs
+    // at any n).  The zeros of the alias band do not wait for the step: the copy engine writes
+    // the alias planes and row blocks from a zeroed device buffer on a side stream, and host
+    // threads zero the row tails, both while the handle's stream still runs.
+    if ((rc = h->ensure_zero_source())) return rc;
+    MHD_CUDA(zero_alias_blocks(reinterpret_cast<float2*>(sol), h->g, h->nfields(), h->zeros, h->zbytes, h->zstream));
     if ((rc = h->launch(KC_OTHER, [&] {
            scatter_retained_kernel<<<1216, 256, 0, h->stream>>>(src, out, h->g, h->nfields());
          })))
       return rc;
-    zero_outside_retained(reinterpret_cast<float2*>(sol), h->g, h->nfields());
+    zero_row_tails(reinterpret_cast<float2*>(sol), h->g, h->nfields());
+    MHD_CUDA(cudaStreamSynchronize(h->zstream));
   } else {
+    // the full array is assembled in the staging buffer at HBM speed, zeros included, and comes
+    // back in one contiguous copy
     if ((rc = h->launch(KC_OTHER, [&] {
            scatter_state_kernel<<<1216, 256, 0, h->stream>>>(src, h->ref, h->g, h->nfields());
          })))
@@ -1134,6 +1266,49 @@ int mhd_slot_get_state(mhd_handle h, int slot, float* sol) {
   }
   MHD_CUDA(cudaStreamSynchronize(h->stream));
   return MHD_OK;
+}
+
+// prob.sol as a device array: the gather / scatter kernels read or write the caller's array
+// directly, ordered on `stream` after the handle's earlier work and before its later work.
+static int state_device(mhd_handle h, int slot, float* sol_dev, void* stream, bool to_state) {
+  int rc = check_slot(h, slot);
+  if (rc) return rc;
+  if (!sol_dev) return fail(MHD_ERR_INVALID, "null device array");
+  if (reinterpret_cast<uintptr_t>(sol_dev) % 16 != 0) return fail(MHD_ERR_INVALID, "the device array must be 16-byte aligned");
+  if (!is_device_memory(sol_dev)) return fail(MHD_ERR_INVALID, "sol_dev is not device memory");
+  // the caller's stream as given: 0 is the legacy default stream (torch's default, CUDA C's
+  // default), which the handle's non-blocking stream does not synchronise with by itself
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if (s != h->stream) {
+    if (!h->ev_in) MHD_CUDA(cudaEventCreateWithFlags(&h->ev_in, cudaEventDisableTiming));
+    if (!h->ev_out) MHD_CUDA(cudaEventCreateWithFlags(&h->ev_out, cudaEventDisableTiming));
+    MHD_CUDA(cudaEventRecord(h->ev_in, h->stream));
+    MHD_CUDA(cudaStreamWaitEvent(s, h->ev_in, 0));
+  }
+  float2* st = h->sol + slot * h->sz.state;
+  float2* ref = reinterpret_cast<float2*>(sol_dev);
+  if (to_state) gather_state_kernel<<<1216, 256, 0, s>>>(ref, st, h->g, h->nfields());
+  else scatter_state_kernel<<<1216, 256, 0, s>>>(st, ref, h->g, h->nfields());
+  const cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return fail(MHD_ERR_CUDA, std::string(to_state ? "gather" : "scatter") + " launch: " + cudaGetErrorString(e));
+  if (s != h->stream) {
+    MHD_CUDA(cudaEventRecord(h->ev_out, s));
+    MHD_CUDA(cudaStreamWaitEvent(h->stream, h->ev_out, 0));
+  }
+  return MHD_OK;
+}
+
+int mhd_slot_set_state_device(mhd_handle h, int slot, const float* sol_dev, void* stream) {
+  return state_device(h, slot, const_cast<float*>(sol_dev), stream, true);
+}
+int mhd_slot_get_state_device(mhd_handle h, int slot, float* sol_dev, void* stream) {
+  return state_device(h, slot, sol_dev, stream, false);
+}
+int mhd_set_state_device(mhd_handle h, const float* sol_dev, void* stream) {
+  return mhd_slot_set_state_device(h, 0, sol_dev, stream);
+}
+int mhd_get_state_device(mhd_handle h, float* sol_dev, void* stream) {
+  return mhd_slot_get_state_device(h, 0, sol_dev, stream);
 }
 
 int mhd_slot_set_physical(mhd_handle h, int slot, int field, const float* phys) {
@@ -1494,7 +1669,7 @@ int mhd_compute_rhs(mhd_handle h, float* rhs_out) {
   int rc = check_slot(h, 0);
   if (rc) return rc;
   if (!rhs_out) return fail(MHD_ERR_INVALID, "null output");
-  if ((rc = h->rhs(h->sol, OP_RHS, 0.f, 0.f, 0.f, h->slot_ref(0), 7))) return rc;
+  if ((rc = h->rhs(h->sol, h->acc, OP_RHS, 0.f, 0.f, 0.f, h->slot_ref(0), 7))) return rc;
   if ((rc = h->launch(KC_OTHER, [&] { scatter_state_kernel<<<1216, 256, 0, h->stream>>>(h->acc, h->ref, h->g, h->nfields()); }))) return rc;
   MHD_CUDA(cudaMemcpyAsync(rhs_out, h->ref, h->ref_elems() * sizeof(float2), cudaMemcpyDeviceToHost, h->stream));
   MHD_CUDA(cudaStreamSynchronize(h->stream));
@@ -1780,12 +1955,15 @@ int mhd_ensemble_step(mhd_ensemble e, int nsteps) {
 // ------------------------------------------------------------------------------------------
 // Allocation-free diagnostics.
 //
-// Some callers cannot call cudaMalloc: code running inside a CUDA-graph capture or another
-// library's stream callback, real-time loops that must not block on the allocator, and hosts
-// whose memory is owned by a pool they do not control (a Julia or Python array library that
-// hands out device pointers but not allocation rights).  mhd_diagnostics_noalloc serves them:
-// it reads a caller-owned device copy of prob.sol and writes six doubles to caller-owned device
-// memory, and the only scratch it uses is the fixed array below, compiled into the library.
+// Some callers of this code cannot call cudaMalloc.  A Julia program whose CuArrays come from
+// CUDA.jl's memory pool, or a Python program whose tensors come from PyTorch's caching
+// allocator, hands the library device pointers but expects all device memory to go through
+// that pool: a raw cudaMalloc behind the pool's back can fail once the pool has reserved the
+// free memory, and it makes the process's memory use invisible to the pool's accounting.
+// Real-time loops that must not block on the allocator, and code running where the driver
+// forbids allocation, are in the same position.  mhd_diagnostics_noalloc serves them: it reads
+// a caller-owned device copy of prob.sol, writes six doubles to caller-owned device memory, and
+// the only scratch it uses is the fixed array below, compiled into the library.
 // ------------------------------------------------------------------------------------------
 namespace {
 
@@ -1797,9 +1975,36 @@ namespace {
 constexpr int kNoAllocBlocks = 1216;
 static __device__ __align__(256) double g_noalloc_partials[kNoAllocBlocks * kDiagSlots];
 
-// Device address of g_noalloc_partials on each device, looked up once per device.
+// Device address of g_noalloc_partials, looked up once per CUDA context.  A __device__ variable
+// has its own address in every context that loads the module (a caller's own context on a
+// device as well as the device's primary context, and a new one after cudaDeviceReset), so the
+// cache is keyed by the unique id of the context current at the call (cuCtxGetId: never reused
+// within a process, unlike a context handle), not by the device ordinal.
 std::mutex g_noalloc_mtx;
-double* g_noalloc_ptr[256] = {nullptr};
+std::map<unsigned long long, double*> g_noalloc_ptr;
+
+// Driver entry points through the runtime (the library does not link libcuda).
+template <class F>
+F driver_fn(const char* name, int version) {
+  void* p = nullptr;
+  cudaDriverEntryPointQueryResult q;
+  if (cudaGetDriverEntryPointByVersion(name, &p, version, cudaEnableDefault, &q) != cudaSuccess ||
+      q != cudaDriverEntryPointSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  return reinterpret_cast<F>(p);
+}
+
+// Id of the context current on this thread; 0 if there is none or the query fails.
+unsigned long long current_ctx_id() {
+  static const auto get_ctx = driver_fn<PFN_cuCtxGetCurrent_v4000>("cuCtxGetCurrent", 4000);
+  static const auto get_id = driver_fn<PFN_cuCtxGetId_v12000>("cuCtxGetId", 12000);
+  CUcontext ctx = nullptr;
+  unsigned long long id = 0;
+  if (!get_ctx || !get_id || get_ctx(&ctx) != CUDA_SUCCESS || !ctx || get_id(ctx, &id) != CUDA_SUCCESS) return 0;
+  return id;
+}
 
 // Partial sums over a reference-layout half spectrum sol[f][kz][ky][kx] (nkr = n/2+1 fastest),
 // restricted to the retained band, with the weights and sums of diag_partial_kernel.
@@ -1869,20 +2074,30 @@ extern "C" int mhd_diagnostics_noalloc(const float* sol_dev, int n, double L, do
     return fail(MHD_ERR_INVALID, "n=" + std::to_string(n) + " is beyond what this entry point handles (n in 16,32,48,64,96,128,256,512)");
   }
   if (!(L > 0) || !std::isfinite(L)) return fail(MHD_ERR_INVALID, "box size L must be positive");
-  int dev = 0;
-  MHD_CUDA(cudaGetDevice(&dev));
-  if (dev < 0 || dev >= 256) return fail(MHD_ERR_INVALID, "device ordinal out of range");
+  {
+    // an error left by earlier work on this thread is reported as such, not blamed on the
+    // launches below (their check would otherwise return and clear it)
+    const cudaError_t pre = cudaGetLastError();
+    if (pre != cudaSuccess)
+      return fail(MHD_ERR_CUDA, std::string("a CUDA error was pending before mhd_diagnostics_noalloc: ") + cudaGetErrorString(pre));
+  }
   double* partials = nullptr;
   {
     std::lock_guard<std::mutex> lock(g_noalloc_mtx);
-    if (!g_noalloc_ptr[dev]) {
-      // first call on this device (the current one): resolve the scratch array's device address
+    unsigned long long ctx = current_ctx_id();
+    auto it = ctx ? g_noalloc_ptr.find(ctx) : g_noalloc_ptr.end();
+    if (it == g_noalloc_ptr.end()) {
+      // first call in this context: resolve the scratch array's device address here.  With no
+      // context current yet, this runtime call makes the current device's primary context
+      // current, and the address belongs to that context.
       void* p = nullptr;
       cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_partials);
       if (e != cudaSuccess) return fail(MHD_ERR_CUDA, std::string("cudaGetSymbolAddress(g_noalloc_partials): ") + cudaGetErrorString(e));
-      g_noalloc_ptr[dev] = static_cast<double*>(p);
+      if (!ctx) ctx = current_ctx_id();
+      if (!ctx) return fail(MHD_ERR_CUDA, "no current CUDA context (cuCtxGetCurrent / cuCtxGetId)");
+      it = g_noalloc_ptr.emplace(ctx, static_cast<double*>(p)).first;
     }
-    partials = g_noalloc_ptr[dev];
+    partials = it->second;
   }
   const Geom g = make_geom(n, L);
   const long long plane = (long long)n * n * (n / 2 + 1);

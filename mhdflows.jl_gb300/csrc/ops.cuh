@@ -14,6 +14,7 @@
 #include <vector>
 
 #include "passes.cuh"
+#include "tc5_rows.cuh"
 #include "tc_rows.cuh"
 
 namespace mhdgb {
@@ -59,6 +60,7 @@ struct XVariant {
   size_t table_words = 0;
   int (*build_table)(uint32_t* table) = nullptr;
   uint32_t* table = nullptr;
+  int err_word = -1;  // index of a device error word in the table (bounded waits), -1: none
 };
 
 struct ColVariant {
@@ -84,6 +86,9 @@ class OpsBase {
                int cap, unsigned int* vmax, VpRef vp, cudaStream_t s) const;
   void x_c2r(const float2* src, float* dst, const Geom& g, long long srow, float scale, cudaStream_t s) const;
   void x_r2c(const float* src, float2* dst, const Geom& g, long long drow, cudaStream_t s) const;
+  // a bounded device wait of the selected x-row kernel that ran out (its table's error word);
+  // 0 when none (reads device memory: call where the library synchronises)
+  int x_device_error() const;
 
   int n = 0;
   int prec = 0;  // precision form of the x rows (mhd_params.precision)
@@ -240,6 +245,23 @@ class Ops : public OpsBase {
     v.prec = KIND == SPLIT_F16 ? 1 : 2;
     v.table_words = TcLayout<N>::WORDS;
     v.build_table = &tc_build_table<N, KIND>;
+    xv.push_back(v);
+  }
+
+  // x rows on the fifth-generation tensor cores (tcgen05, split TF32 operands, n = 256 only)
+  void add_x_tc5() {
+    static_assert(N == 256, "the tcgen05 x rows are built for n = 256");
+    XVariant v;
+    v.name = "xtc5:tf32/16x16/m128";
+    v.fn = x_fused_tc5_kernel<N>;
+    v.threads = Tc5Layout::THREADS;
+    v.rpg = Tc5Layout::TILE_ROWS;
+    v.groups = 1;
+    v.group_words = &tc5_group_words;
+    v.prec = 3;
+    v.table_words = Tc5Layout::WORDS;
+    v.build_table = &tc5_build_table<N>;
+    v.err_word = Tc5Layout::ERR;
     xv.push_back(v);
   }
 

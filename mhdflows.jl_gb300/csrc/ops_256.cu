@@ -28,6 +28,7 @@ OpsBase* make_ops_256() {
   o->add_x_hdvp<Plan<256, 32, 8, 8, 4>, 4, 3>();
   o->add_x_tc<SPLIT_F16, 4, 2>();
   o->add_x_tc<SPLIT_BF16, 4, 2>();
+  o->add_x_tc5();
   o->set_rows<Plan<256, 32, 8, 8, 4>, 4>();
   return o;
 }

@@ -160,6 +160,14 @@ void OpsBase::x_fused(float2* pool, const Geom& g, long long rowstride, long lon
   x.fn<<<grid, x.threads, x.smem, s>>>(pool, g, rowstride, slot, istride, br, t1, t2, vmax, vp);
 }
 
+int OpsBase::x_device_error() const {
+  const XVariant& x = xv[sel[KC_XFUSED]];
+  if (!x.table || x.err_word < 0) return 0;
+  uint32_t e = 0;
+  if (cudaMemcpy(&e, x.table + x.err_word, sizeof(e), cudaMemcpyDeviceToHost) != cudaSuccess) return 1;
+  return e != 0;
+}
+
 void OpsBase::x_c2r(const float2* src, float* dst, const Geom& g, long long srow, float scale, cudaStream_t s) const {
   const long long pairs = (long long)n * n / 2;
   c2r<<<(unsigned)(pairs / rows), row_threads, row_smem, s>>>(src, dst, g, srow, scale, tw_dev + row_tw);

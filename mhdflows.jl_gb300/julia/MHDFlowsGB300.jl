@@ -3,17 +3,21 @@
 # Provides a time stepper that plugs into MHDFlows the same way HM89TimeStepper does
 # (src/timestepper/HM89.jl:6-31 of MHDFlows.jl): a struct <: FourierFlows.AbstractTimeStepper
 # plus a stepforward! method, selected in MHDFLowsProblem (src/Problems.jl:124-129) by
-# stepper = "GB300RK4" or "GB300LSRK4".  The device state lives in the library; prob.sol is
-# refreshed from it on demand (sync_sol!) so savefile / Restart! / Diagnostic keep working.
+# stepper = "GB300RK4" or "GB300LSRK4".  prob.sol stays authoritative: every stepforward! pushes
+# the caller's array into the library, steps, and writes the result back into it, so
+# Diagnostic, DivVCorrection!, savefile and user code that read or edit prob.sol between steps
+# see and change the current state.  For a CuArray (Problem(GPU(); ...)) the push and the
+# write-back are device-to-device kernels ordered on the array's stream.
 #
 # Not exercised in this repository's test suite (no Julia toolchain is available here); the
 # same C ABI is exercised from Python through ctypes with identical signatures.
 module MHDFlowsGB300
 
 using FourierFlows
+using CUDA
 import FourierFlows: stepforward!
 
-export GB300TimeStepper, gb300_updatevars!, sync_sol!, push_sol!, gb300_diagnostics, gb300_autotune!,
+export GB300TimeStepper, gb300_updatevars!, sync_sol!, push_sol!, gb300_diagnostics, gb300_autotune!, gb300_set_cfl!,
        gb300_SetUpFk!, gb300_set_vp!, gb300_DivVCorrection!, gb300_DivBCorrection!, gb300_div_correction!,
        gb300_record_diagnostics!, gb300_diagnostic_history, MhdServerParams, MhdRequest, GB300Server,
        gb300_submit!, gb300_tick!, gb300_poll, gb300_result
@@ -40,6 +44,7 @@ check(rc) = rc == 0 ? nothing : error(unsafe_string(ccall((:mhd_last_error, libm
 mutable struct GB300TimeStepper{T} <: FourierFlows.AbstractTimeStepper{T}
   handle::Ptr{Cvoid}
   n::Int
+  cfl::Bool   # the on-device getCFL! owns dt and t (gb300_set_cfl!)
 end
 
 function GB300TimeStepper(grid, params, dt; scheme::Symbol = :RK4, device::Integer = 0,
@@ -53,30 +58,64 @@ function GB300TimeStepper(grid, params, dt; scheme::Symbol = :RK4, device::Integ
                 scheme == :RK4 ? 0 : 1, prec, device, B_field ? 0 : 1, VP_method ? 1 : 0)
   h = Ref{Ptr{Cvoid}}(C_NULL)
   check(ccall((:mhd_create, libmhdgb), Cint, (Ref{MhdParams}, Ref{Ptr{Cvoid}}), p, h))
-  ts = GB300TimeStepper{Array{ComplexF32,4}}(h[], grid.nx)
+  ts = GB300TimeStepper{Array{ComplexF32,4}}(h[], grid.nx, false)
   finalizer(t -> ccall((:mhd_destroy, libmhdgb), Cint, (Ptr{Cvoid},), t.handle), ts)
   return ts
 end
 
-# prob.sol (host or device array, (nkr, n, n, 6) ComplexF32) <-> library state
-push_sol!(ts::GB300TimeStepper, sol) =
-  check(ccall((:mhd_set_state, libmhdgb), Cint, (Ptr{Cvoid}, Ptr{ComplexF32}), ts.handle, Array(sol)))
+# prob.sol ((nkr, n, n, 6) ComplexF32) <-> library state.  A CuArray moves by a device kernel on
+# the task's stream (mhd_set_state_device / mhd_get_state_device); a host Array by copies.
+devptr(a::CuArray) = Ptr{Cvoid}(UInt(pointer(a)))
+streamptr() = reinterpret(Ptr{Cvoid}, CUDA.stream().handle)
 
+push_sol!(ts::GB300TimeStepper, sol::CuArray) =
+  check(ccall((:mhd_set_state_device, libmhdgb), Cint, (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}),
+              ts.handle, devptr(sol), streamptr()))
+push_sol!(ts::GB300TimeStepper, sol::Array{ComplexF32}) =
+  check(ccall((:mhd_set_state, libmhdgb), Cint, (Ptr{Cvoid}, Ptr{ComplexF32}), ts.handle, sol))
+push_sol!(ts::GB300TimeStepper, sol) = push_sol!(ts, Array{ComplexF32}(sol))
+
+sync_sol!(sol::CuArray, ts::GB300TimeStepper) =
+  check(ccall((:mhd_get_state_device, libmhdgb), Cint, (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}),
+              ts.handle, devptr(sol), streamptr()))
+sync_sol!(sol::Array{ComplexF32}, ts::GB300TimeStepper) =
+  check(ccall((:mhd_get_state, libmhdgb), Cint, (Ptr{Cvoid}, Ptr{ComplexF32}), ts.handle, sol))
 function sync_sol!(sol, ts::GB300TimeStepper)
   host = Array{ComplexF32}(undef, size(sol))
-  check(ccall((:mhd_get_state, libmhdgb), Cint, (Ptr{Cvoid}, Ptr{ComplexF32}), ts.handle, host))
+  sync_sol!(host, ts)
   copyto!(sol, host)
   return nothing
 end
 
-# stepforward!(sol, clock, ts, equation, vars, params, grid): one step on the GPU; the host
-# sol is not touched (call sync_sol! before reading it), clock advances like FourierFlows'.
+# stepforward!(sol, clock, ts, equation, vars, params, grid): one step of the library on the
+# caller's current sol, written back into sol.  With a fixed step the clock is the caller's (it
+# is handed to the library first, so edits of clock.t / clock.dt take effect); with the
+# on-device getCFL! (gb300_set_cfl!) the library owns dt and t and the clock is read back.
 function stepforward!(sol, clock, ts::GB300TimeStepper, equation, vars, params, grid)
-  check(ccall((:mhd_set_clock, libmhdgb), Cint, (Ptr{Cvoid}, Cdouble, Clonglong, Cdouble),
-              ts.handle, clock.t, clock.step, clock.dt))
+  if !ts.cfl
+    check(ccall((:mhd_set_clock, libmhdgb), Cint, (Ptr{Cvoid}, Cdouble, Clonglong, Cdouble),
+                ts.handle, clock.t, clock.step, clock.dt))
+  end
+  push_sol!(ts, sol)
   check(ccall((:mhd_step, libmhdgb), Cint, (Ptr{Cvoid}, Cint), ts.handle, 1))
-  clock.t += clock.dt
+  sync_sol!(sol, ts)
+  if ts.cfl
+    t, step, dt = Ref{Cdouble}(0), Ref{Clonglong}(0), Ref{Cdouble}(0)
+    check(ccall((:mhd_get_clock, libmhdgb), Cint, (Ptr{Cvoid}, Ref{Cdouble}, Ref{Clonglong}, Ref{Cdouble}),
+                ts.handle, t, step, dt))
+    clock.t, clock.dt = t[], dt[]
+  else
+    clock.t += clock.dt
+  end
   clock.step += 1
+  return nothing
+end
+
+# getCFL! of TimeIntegrator! (src/integrator.jl:54-58, 158-198) on the device: every step ends
+# with dt = min(CFL_Coef dx / max(|u|, |B|), t_diff) and the library advances t.
+function gb300_set_cfl!(ts::GB300TimeStepper, enable::Bool; CFL_Coef = 0.25)
+  check(ccall((:mhd_set_cfl, libmhdgb), Cint, (Ptr{Cvoid}, Cint, Cdouble), ts.handle, enable ? 1 : 0, CFL_Coef))
+  ts.cfl = enable
   return nothing
 end
 

@@ -1,10 +1,16 @@
 """State transfer through page-locked host buffers (mhd_host_alloc): the gather / scatter kernels
 read and write the mapped buffer directly.  Results must equal the pageable-memory path bit for
 bit; a pageable buffer goes through the staging copy.  From 16 MB up, get_state into mapped
-memory writes only the retained band from the device and zeroes the rest on host threads
-(n = 96 and the HD n = 128 case); smaller buffers are written whole by the device (n = 32)."""
+memory writes only the retained band from the device, the copy engine writes the zeros of the
+alias planes and row blocks, and host threads zero the row tails (n = 96 and the HD n = 128
+case); smaller buffers are written whole by the device (n = 32).  MHDGB_HOST_TRANSFER=copy
+selects the copy-engine path for mapped buffers too (checked in a child process)."""
 import ctypes as C
 import math
+import os
+import subprocess
+import sys
+import textwrap
 
 import numpy as np
 import pytest
@@ -75,3 +81,36 @@ def test_pinned_hydrodynamic_state_overwrites_every_element(pkg, mo, lib):
         assert np.array_equal(got, g.dealias(full)[:3])
     finally:
         lib.mhd_host_free(pin)
+
+
+def test_copy_engine_transfer_mode(pkg):
+    """The same round trip with MHDGB_HOST_TRANSFER=copy (read once per process: a child process)."""
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    code = textwrap.dedent("""
+        import ctypes as C, sys
+        import numpy as np
+        sys.path.insert(0, %r)
+        import __graft_entry__ as ge
+        from oracle import mhd_oracle as mo
+        pkg = ge.load_package(); lib = pkg._lib.load()
+        n = 96
+        g = mo.Grid(n)
+        s = mo.random_spectrum_state(g, seed=54).astype(np.complex64)
+        nb = s.nbytes
+        pin = C.c_void_p(); pkg._lib.check(lib.mhd_host_alloc(nb, C.byref(pin)))
+        C.memmove(pin, s.ctypes.data, nb)
+        with pkg.Problem(pkg.GPU(0), nx=n, nu=1e-3, eta=1e-3, dt=1e-3) as prob:
+            pkg._lib.check(lib.mhd_set_state(prob.handle, pin))
+            pkg.stepforward(prob, 2)
+            ref = prob.sol_c()
+            C.memset(pin, 0x7f, nb)
+            pkg._lib.check(lib.mhd_get_state(prob.handle, pin))
+            got = np.frombuffer((C.c_char * nb).from_address(pin.value), dtype=np.complex64).reshape(s.shape).copy()
+        lib.mhd_host_free(pin)
+        assert np.array_equal(got, ref)
+        assert np.array_equal(np.where(g.retained_mask(), 0, got), np.zeros_like(got))
+        print("copy mode ok")
+    """) % root
+    env = dict(os.environ, MHDGB_HOST_TRANSFER="copy")
+    res = subprocess.run([sys.executable, "-c", code], env=env, capture_output=True, text=True, timeout=600)
+    assert res.returncode == 0 and "copy mode ok" in res.stdout, res.stdout + res.stderr

@@ -7,6 +7,7 @@ hi+lo operands and FP32 accumulation; everything else is the plain FP32 path.  T
   split BF16  RHS 3e-4 and one RK4 step 3e-4 (8-bit mantissas: hi+lo carries 16 bits, so the
               form sits near 1e-4 and cannot reach FP32-level accuracy);
   512^3       RHS of each split form against the plain FP32 RHS, 1e-5 (FP16) / 3e-4 (BF16).
+  split TF32  (tcgen05, n = 256) RHS 1e-5 against the FP64 oracle and one RK4 step 1e-5 against FP64.
 Each test prints the measured error.
 """
 import math
@@ -16,7 +17,7 @@ import pytest
 
 pytestmark = pytest.mark.gpu
 
-TOL = {"split_fp16": 1e-5, "split_bf16": 3e-4}
+TOL = {"split_fp16": 1e-5, "split_bf16": 3e-4, "split_tf32": 1e-5}
 
 
 def _state(pkg, n, seed):
@@ -100,3 +101,25 @@ def test_split_512_twenty_steps_vs_plain(pkg, prec):
     err = float(np.linalg.norm((got - ref).ravel()) / np.linalg.norm(ref.ravel()))
     print(f"{prec} n=512 20 RK4 steps rel L2 vs plain FP32: {err:.3e}")
     assert err < TOL[prec], err
+
+
+def test_tf32_rhs_vs_fp64_oracle(pkg, mo):
+    """The tcgen05 x rows (TF32 hi + lo, data operand in tensor memory) at 256^3: one RHS."""
+    n = 256
+    s0 = _state(pkg, n, 25)
+    g = mo.Grid(n)
+    ref = np.zeros(s0.shape, dtype=np.complex128)
+    mo.calcN_fast(ref, s0.astype(np.complex128), g, 1e-3, 2e-3)
+    with pkg.Problem(pkg.GPU(0), nx=n, Lx=2 * math.pi, nu=1e-3, eta=2e-3, dt=5e-4, precision="split_tf32") as prob:
+        prob.set_sol(s0.T)
+        got = prob.rhs_c()
+        prob.synchronize()
+    err = mo.rel_l2(got, ref, g.retained_mask())
+    print(f"split_tf32 n=256 RHS rel L2 vs FP64 oracle: {err:.3e}")
+    assert err < TOL["split_tf32"], err
+
+
+def test_tf32_rejected_off_256(pkg):
+    for n in (128, 512):
+        with pytest.raises(pkg.MHDError):
+            pkg.Problem(pkg.GPU(0), nx=n, nu=1e-3, eta=1e-3, dt=1e-3, precision="split_tf32")
