@@ -107,7 +107,7 @@ const double kLsB[5] = {1432997174477.0 / 9575080441755.0, 5161836677717.0 / 136
 
 struct Sizes {
   long long fs;      // one compact field (complex)
-  long long state;   // six fields (slot stride of sol / xs / xs2 / acc)
+  long long state;   // six fields (slot stride of sol / xs / acc)
   long long colbuf;  // colbuf complex elements per slot
   long long rowbuf;  // rowbuf complex elements per slot
   long long ref;     // reference-layout sol (complex)
@@ -132,7 +132,7 @@ Sizes sizes_of(const Geom& g, int ns) {
 // fields) and of the per-class staging.
 long long slot_bytes(const Geom& g, bool vp = false, bool hydro = false) {
   Sizes s = sizes_of(g, slots_of(vp && !hydro));
-  return (4 * s.state + s.fs + s.colbuf + s.rowbuf) * 8 + 16 * 4 + (vp ? 7 * s.phys * 4 : 0);
+  return (3 * s.state + s.fs + s.colbuf + s.rowbuf) * 8 + 16 * 4 + (vp ? 7 * s.phys * 4 : 0);
 }
 long long class_bytes(const Geom& g) {
   Sizes s = sizes_of(g, 8);
@@ -282,9 +282,6 @@ struct mhd_problem {
   // slot pools
   float2* sol = nullptr;
   float2* xs = nullptr;
-  // second RK4 stage-state buffer: the stages alternate xs / xs2, so no epilogue overwrites the
-  // stage state it reads, and the kx = 0 plane's Hermitian part is formed inline (no herm_kx0)
-  float2* xs2 = nullptr;
   float2* acc = nullptr;
   float2* aux = nullptr;
   float2* colbuf = nullptr;
@@ -315,7 +312,7 @@ struct mhd_problem {
   bool divcorr = false;
   // TMA sources of the column passes (used when a TMA-fed variant is selected) and the device
   // word a timed-out tile wait is recorded in
-  TmaPass tm_zinv_sol, tm_zinv_xs, tm_zinv_xs2, tm_yinv, tm_yfwd, tm_zfwd;
+  TmaPass tm_zinv_sol, tm_zinv_xs, tm_yinv, tm_yfwd, tm_zfwd;
   int* derr = nullptr;
   bool cfl = false;
   double cfl_coef = 0.3;
@@ -335,6 +332,7 @@ struct mhd_problem {
   void* zeros = nullptr;
   size_t zbytes = 0;
   cudaStream_t zstream = nullptr;
+  cudaEvent_t ev_z = nullptr;  // orders the copy-engine side stream against the handle's stream
   int ensure_zero_source() {
     if (zeros) return MHD_OK;
     const size_t want = size_t(16) << 20;
@@ -342,6 +340,7 @@ struct mhd_problem {
     MHD_CUDA(cudaMemset(zeros, 0, want));
     zbytes = want;
     if (!zstream) MHD_CUDA(cudaStreamCreateWithFlags(&zstream, cudaStreamNonBlocking));
+    if (!ev_z) MHD_CUDA(cudaEventCreateWithFlags(&ev_z, cudaEventDisableTiming));
     return MHD_OK;
   }
   // guard bands: every large buffer is allocated kGuardBytes longer and the tail filled with
@@ -397,13 +396,15 @@ struct mhd_problem {
     ev_in = ev_out = nullptr;
     if (zstream) cudaStreamSynchronize(zstream), cudaStreamDestroy(zstream);
     if (zeros) cudaFree(zeros);
+    if (ev_z) cudaEventDestroy(ev_z);
     zstream = nullptr;
     zeros = nullptr;
-    void* ptrs[] = {sol, xs, xs2, acc, aux, colbuf, rowbuf, ref, phys, diag_partial, diag_out, maxabs, dparams, dlist, dvmax, dtime,
+    ev_z = nullptr;
+    void* ptrs[] = {sol, xs, acc, aux, colbuf, rowbuf, ref, phys, diag_partial, diag_out, maxabs, dparams, dlist, dvmax, dtime,
                     dstep, derr, vchi, vwall};
     for (void* q : ptrs) if (q) cudaFree(q);
     vchi = vwall = nullptr;
-    sol = xs = xs2 = acc = aux = colbuf = rowbuf = ref = nullptr;
+    sol = xs = acc = aux = colbuf = rowbuf = ref = nullptr;
     guards.clear();
     phys = nullptr; diag_partial = nullptr; diag_out = nullptr; maxabs = nullptr; dparams = nullptr; dlist = nullptr;
     dvmax = nullptr; dtime = nullptr; dstep = nullptr; derr = nullptr;
@@ -473,9 +474,7 @@ struct mhd_problem {
   int z_inverse(const float2* src, long long sI, int nf, BatchRef br) {
     ColArgs a{src, colbuf, FS(), (long long)g.kxp, (long long)g.k2 * g.kxp, (long long)g.kxp, SLK(), AZ(), sI, sz.colbuf};
     // the maps cover all six fields of a pool: only the right-hand side's call can use them
-    const TmaPass* tp = (nf == 6 && sI == ST())
-                            ? (src == sol ? &tm_zinv_sol : src == xs ? &tm_zinv_xs : src == xs2 ? &tm_zinv_xs2 : nullptr)
-                            : nullptr;
+    const TmaPass* tp = (nf == 6 && sI == ST()) ? (src == sol ? &tm_zinv_sol : src == xs ? &tm_zinv_xs : nullptr) : nullptr;
     return launch(KC_ZINV, [&] { ops->col(KC_ZINV, a, g, g.k2, nf, br, cap, stream, tp); });
   }
   int y_inverse(int nf, BatchRef br) {
@@ -505,11 +504,11 @@ struct mhd_problem {
       herm_kx0_kernel<<<gh, bxh, 0, stream>>>(X, aux, g, FS(), ST(), FS(), br);
     });
   }
-  RkArgs rk_args(const float2* X, float2* xn, int op, float hf, float ca, float cb, int stage, bool inline_herm) const {
+  RkArgs rk_args(const float2* X, float2* xn, int op, float hf, float ca, float cb, int stage) const {
     RkArgs a{};
     a.prod = rowbuf;
     a.X = X;
-    a.H = inline_herm ? nullptr : aux;
+    a.H = aux;
     a.sol = sol;
     a.acc = acc;
     a.xn = xn;
@@ -533,14 +532,12 @@ struct mhd_problem {
   // HDcalcN! (src/pgen.jl:176-182) calls addforcing! before HDcalcN_advection!, whose UᵢUpdate!
   // starts by zeroing the velocity right-hand side: a hydrodynamic problem is unforced
   bool forced() const { return forcing && !p.hydro_only; }
-  // xn: where the stage update writes (the next stage state, or sol).  When it is not the stage
-  // state X itself, X stays unchanged during the epilogue and each kx = 0 mode reads its partner
-  // mode's value directly; otherwise herm_kx0 first copies the Hermitian part of X's kx = 0 plane.
+  // xn: where the stage update writes (the next stage state, or sol; it may be X itself, so the
+  // Hermitian part of X's kx = 0 plane is copied out first by herm_kx0)
   int epilogue(const float2* X, float2* xn, int op, float hf, float ca, float cb, BatchRef br, int stage) {
-    const bool inline_herm = xn != X;
-    int rc = inline_herm ? MHD_OK : herm(X, br);
+    int rc = herm(X, br);
     if (rc) return rc;
-    const RkArgs a = rk_args(X, xn, op, hf, ca, cb, stage, inline_herm);
+    const RkArgs a = rk_args(X, xn, op, hf, ca, cb, stage);
     const int bx = g.kx <= 256 ? (g.kx + 31) / 32 * 32 : 256;
     const dim3 grid((g.kx + bx - 1) / bx, g.k2, g.k2 * cap);
     const bool f = forced(), v = p.vp != 0;
@@ -587,10 +584,9 @@ struct mhd_problem {
     const BatchRef br = active_ref();
     int rc;
     if (p.scheme == MHD_RK4) {
-      // stage states alternate between xs and xs2 (the last stage writes sol)
       if ((rc = rhs(sol, xs, OP_RK4_FIRST, 0.5f, 0.f, 0.f, br, 0))) return rc;
-      if ((rc = rhs(xs, xs2, OP_RK4_MID, 0.5f, 0.f, 0.f, br, 1))) return rc;
-      if ((rc = rhs(xs2, xs, OP_RK4_MID, 1.0f, 0.f, 0.f, br, 2))) return rc;
+      if ((rc = rhs(xs, xs, OP_RK4_MID, 0.5f, 0.f, 0.f, br, 1))) return rc;
+      if ((rc = rhs(xs, xs, OP_RK4_MID, 1.0f, 0.f, 0.f, br, 2))) return rc;
       if ((rc = rhs(xs, sol, OP_RK4_LAST, 0.f, 0.f, 0.f, br, 3, true))) return rc;
     } else {
       for (int i = 0; i < 5; ++i)
@@ -819,7 +815,6 @@ struct mhd_problem {
     const cuuint32_t bz[5] = {16, 1, kp, 1, 1};
     set(tm_zinv_sol, sol, dz, sz5, bz, TmaCoords{2, 1, 3, 4, (int)kp});
     set(tm_zinv_xs, xs, dz, sz5, bz, TmaCoords{2, 1, 3, 4, (int)kp});
-    set(tm_zinv_xs2, xs2, dz, sz5, bz, TmaCoords{2, 1, 3, 4, (int)kp});
     // colbuf [slot][z][ky'][ns][kx] and rowbuf [slot][z][y][ns][kx]
     const cuuint64_t S = ns;
     const cuuint64_t dc[5] = {kxp, S, k2, n, C};
@@ -933,7 +928,6 @@ int create_class(const mhd_params* params, int cap, mhd_handle* out) {
   const size_t c = (size_t)cap;
   MHD_CUDA(h->alloc_guarded(&h->sol, c * s.state * sizeof(float2)));
   MHD_CUDA(h->alloc_guarded(&h->xs, c * s.state * sizeof(float2)));
-  MHD_CUDA(h->alloc_guarded(&h->xs2, c * s.state * sizeof(float2)));
   MHD_CUDA(h->alloc_guarded(&h->acc, c * s.state * sizeof(float2)));
   MHD_CUDA(h->alloc_guarded(&h->aux, c * s.fs * sizeof(float2)));
   MHD_CUDA(h->alloc_guarded(&h->colbuf, c * s.colbuf * sizeof(float2)));
@@ -955,7 +949,6 @@ int create_class(const mhd_params* params, int cap, mhd_handle* out) {
   MHD_CUDA(cudaMemsetAsync(h->dtime, 0, c * sizeof(double), h->stream));
   MHD_CUDA(cudaMemsetAsync(h->sol, 0, c * s.state * sizeof(float2), h->stream));
   MHD_CUDA(cudaMemsetAsync(h->xs, 0, c * s.state * sizeof(float2), h->stream));
-  MHD_CUDA(cudaMemsetAsync(h->xs2, 0, c * s.state * sizeof(float2), h->stream));
   MHD_CUDA(cudaMemsetAsync(h->acc, 0, c * s.state * sizeof(float2), h->stream));
   if (params->vp) {
     MHD_CUDA(h->alloc_guarded(&h->vchi, c * s.phys * sizeof(float)));
@@ -1158,10 +1151,10 @@ cudaError_t zero_alias_blocks(float2* ref, const Geom& g, int nf, const void* ze
 // How state transfers to and from page-locked host buffers mapped into the device address space
 // move their bytes ($MHDGB_HOST_TRANSFER, read once; other host memory always takes the copy path):
 //   mapped (default) kernels read and write the caller's array directly: set_state gathers the
-//          retained band over the link; get_state writes the retained band from the device while
-//          the alias-band zeros land at the same time from the copy engine (whole planes and row
-//          blocks, from a zeroed device buffer) and from host threads (the tail of each kept row).
-//          Measured on GB300 at 256^3: set 0.66 ms, and the zeros overlap the step before it.
+//          retained band of half the fields over the link while the copy engine brings the other
+//          half; get_state writes the alias-band zeros from the copy engine (whole planes and row
+//          blocks, from a zeroed device buffer) and from host threads (the tail of each kept row)
+//          while the step still runs, then the retained band crosses on both paths at once.
 //   copy   the copy engines only (about 200 GB/s over the host link): set_state copies the
 //          retained band of the caller's array into the device staging array (one 3-D copy per
 //          field and ky / kz range) and gathers it there; get_state scatters into the staging
@@ -1215,16 +1208,35 @@ int mhd_slot_set_state(mhd_handle h, int slot, const float* sol) {
   int rc = check_slot(h, slot);
   if (rc) return rc;
   if (!sol) return fail(MHD_ERR_INVALID, "null sol");
+  const int nf = h->nfields();
   const size_t bytes = h->ref_elems() * sizeof(float2);
-  const float2* src = mapped_transfers() ? static_cast<const float2*>(mapped_host(sol, bytes)) : nullptr;
-  if (!src) {
-    // only the retained band crosses the link (29% of the array), into the staging array
-    const cudaError_t e = copy_retained(h->ref, sol, h->g, h->nfields(), cudaMemcpyHostToDevice, h->stream);
-    if (e != cudaSuccess) return fail(MHD_ERR_CUDA, std::string("set_state copy: ") + cudaGetErrorString(e));
-    src = h->ref;
-  }
+  const long long fref = h->ref_elems() / nf;  // one field of the reference layout
   float2* dst = h->sol + slot * h->sz.state;
-  if ((rc = h->launch(KC_OTHER, [&] { gather_state_kernel<<<1216, 256, 0, h->stream>>>(src, dst, h->g, h->nfields()); }))) return rc;
+  const float2* mapped = mapped_transfers() ? static_cast<const float2*>(mapped_host(sol, bytes)) : nullptr;
+  if (mapped) {
+    // the retained band crosses the host link on two paths at once: the gather kernel reads the
+    // first half of the fields straight from the mapped array, while the copy engine brings the
+    // retained band of the other half into the staging array, gathered from there
+    if ((rc = h->ensure_zero_source())) return rc;
+    const int hf = nf / 2;
+    MHD_CUDA(cudaEventRecord(h->ev_z, h->stream));  // the staging array is free once earlier work is done
+    MHD_CUDA(cudaStreamWaitEvent(h->zstream, h->ev_z, 0));
+    const cudaError_t e = copy_retained(h->ref + hf * fref, reinterpret_cast<const float2*>(sol) + hf * fref, h->g,
+                                        nf - hf, cudaMemcpyHostToDevice, h->zstream);
+    if (e != cudaSuccess) return fail(MHD_ERR_CUDA, std::string("set_state copy: ") + cudaGetErrorString(e));
+    MHD_CUDA(cudaEventRecord(h->ev_z, h->zstream));
+    if ((rc = h->launch(KC_OTHER, [&] { gather_state_kernel<<<1216, 256, 0, h->stream>>>(mapped, dst, h->g, hf); }))) return rc;
+    MHD_CUDA(cudaStreamWaitEvent(h->stream, h->ev_z, 0));
+    if ((rc = h->launch(KC_OTHER, [&] {
+           gather_state_kernel<<<1216, 256, 0, h->stream>>>(h->ref + hf * fref, dst + hf * h->sz.fs, h->g, nf - hf);
+         })))
+      return rc;
+  } else {
+    // only the retained band crosses the link (29% of the array), into the staging array
+    const cudaError_t e = copy_retained(h->ref, sol, h->g, nf, cudaMemcpyHostToDevice, h->stream);
+    if (e != cudaSuccess) return fail(MHD_ERR_CUDA, std::string("set_state copy: ") + cudaGetErrorString(e));
+    if ((rc = h->launch(KC_OTHER, [&] { gather_state_kernel<<<1216, 256, 0, h->stream>>>(h->ref, dst, h->g, nf); }))) return rc;
+  }
   MHD_CUDA(cudaStreamSynchronize(h->stream));
   return MHD_OK;
 }
@@ -1233,33 +1245,46 @@ int mhd_slot_get_state(mhd_handle h, int slot, float* sol) {
   int rc = check_slot(h, slot);
   if (rc) return rc;
   if (!sol) return fail(MHD_ERR_INVALID, "null sol");
+  const int nf = h->nfields();
   const float2* src = h->sol + slot * h->sz.state;
   const size_t bytes = h->ref_elems() * sizeof(float2);
+  const long long fref = h->ref_elems() / nf;
   float2* out = mapped_transfers() ? static_cast<float2*>(mapped_host(sol, bytes)) : nullptr;
   if (out && bytes < (size_t(16) << 20)) {
     // small mapped buffers: the device writes every element
     if ((rc = h->launch(KC_OTHER, [&] {
-           scatter_state_kernel<<<1216, 256, 0, h->stream>>>(src, out, h->g, h->nfields());
+           scatter_state_kernel<<<1216, 256, 0, h->stream>>>(src, out, h->g, nf);
          })))
       return rc;
   } else if (out) {
-    // mapped memory: the device writes the retained elements straight into it (29% of the bytes
-    // at any n).  The zeros of the alias band do not wait for the step: the copy engine writes
-    // the alias planes and row blocks from a zeroed device buffer on a side stream, and host
-    // threads zero the row tails, both while the handle's stream still runs.
+    // mapped memory.  The zeros of the alias band do not wait for the step: the copy engine
+    // writes the alias planes and row blocks from a zeroed device buffer on a side stream, and
+    // host threads zero the row tails, both while the handle's stream still runs.  After the
+    // step the retained band (29% of the bytes) crosses on two paths at once: the device writes
+    // the first half of the fields straight into the mapping, and the other half is scattered
+    // into the staging array and brought over by the copy engine.
     if ((rc = h->ensure_zero_source())) return rc;
-    MHD_CUDA(zero_alias_blocks(reinterpret_cast<float2*>(sol), h->g, h->nfields(), h->zeros, h->zbytes, h->zstream));
+    const int hf = nf / 2;
+    float2* host = reinterpret_cast<float2*>(sol);
+    MHD_CUDA(zero_alias_blocks(host, h->g, nf, h->zeros, h->zbytes, h->zstream));
     if ((rc = h->launch(KC_OTHER, [&] {
-           scatter_retained_kernel<<<1216, 256, 0, h->stream>>>(src, out, h->g, h->nfields());
+           scatter_retained_kernel<<<1216, 256, 0, h->stream>>>(src + hf * h->sz.fs, h->ref + hf * fref, h->g, nf - hf);
          })))
       return rc;
-    zero_row_tails(reinterpret_cast<float2*>(sol), h->g, h->nfields());
+    MHD_CUDA(cudaEventRecord(h->ev_z, h->stream));
+    MHD_CUDA(cudaStreamWaitEvent(h->zstream, h->ev_z, 0));
+    MHD_CUDA(copy_retained(host + hf * fref, h->ref + hf * fref, h->g, nf - hf, cudaMemcpyDeviceToHost, h->zstream));
+    if ((rc = h->launch(KC_OTHER, [&] {
+           scatter_retained_kernel<<<1216, 256, 0, h->stream>>>(src, out, h->g, hf);
+         })))
+      return rc;
+    zero_row_tails(host, h->g, nf);
     MHD_CUDA(cudaStreamSynchronize(h->zstream));
   } else {
     // the full array is assembled in the staging buffer at HBM speed, zeros included, and comes
     // back in one contiguous copy
     if ((rc = h->launch(KC_OTHER, [&] {
-           scatter_state_kernel<<<1216, 256, 0, h->stream>>>(src, h->ref, h->g, h->nfields());
+           scatter_state_kernel<<<1216, 256, 0, h->stream>>>(src, h->ref, h->g, nf);
          })))
       return rc;
     MHD_CUDA(cudaMemcpyAsync(sol, h->ref, bytes, cudaMemcpyDeviceToHost, h->stream));

@@ -25,7 +25,7 @@ enum StageOp : int {
 struct RkArgs {
   const float2* prod;   // 8 compact product planes, then 6 penalty planes with VP (slot stride prodI)
   const float2* X;      // stage state (6 fields, slot stride stI)
-  const float2* H;      // Hermitian part of X on the kx = 0 plane, [f][kz'][ky'] (slot stride hI); nullptr: formed from X
+  const float2* H;      // Hermitian part of X on the kx = 0 plane, [f][kz'][ky'] (slot stride hI)
   float2* sol;          // RK4 step-start state
   float2* acc;          // RK4 accumulator / LSRK4 du / OP_RHS output
   float2* xn;           // RK4 next stage state / LSRK4 u
@@ -144,23 +144,11 @@ __device__ __forceinline__ void finish_mode(const RkArgs& a, const Geom& geo, in
   float2 xv[6], xd[6];
 #pragma unroll
   for (int c = 0; c < 6; ++c) xv[c] = xd[c] = c < NF ? X[c * fs + i] : make_float2(0.f, 0.f);
-  if (x == 0 && a.H) {
+  if (x == 0) {
     const long long p = (long long)jz * geo.k2 + jy, pl = (long long)geo.k2 * geo.k2;
     const float2* H = a.H + slot * a.hI;
 #pragma unroll
     for (int c = 0; c < NF; ++c) xd[c] = H[c * pl + p];
-  } else if (x == 0) {
-    // no stage update writes X in this launch: the Hermitian part (X(k) + conj X(-k)) / 2 from
-    // the partner mode directly (zero partner in the alias band), as herm_kx0_kernel forms it
-    const int py = kept_of_signed(geo, -signed_of_kept(geo, jy));
-    const int pz = kept_of_signed(geo, -signed_of_kept(geo, jz));
-    const bool partner = py >= 0 && pz >= 0;
-    const long long par = partner ? ((long long)pz * geo.k2 + py) * geo.kxp : i;
-#pragma unroll
-    for (int c = 0; c < NF; ++c) {
-      const float2 q = partner ? X[c * fs + par] : make_float2(0.f, 0.f);
-      xd[c] = make_float2(0.5f * (xv[c].x + q.x), 0.5f * (xv[c].y - q.y));
-    }
   }
   const float ik2 = k2 > 0.f ? 1.0f / k2 : 0.f;
   const float kvx = (kxv * m.Vx.x + kyv * m.Vy.x + kzv * m.Vz.x) * ik2;
