@@ -61,6 +61,7 @@ struct XVariant {
   int (*build_table)(uint32_t* table) = nullptr;
   uint32_t* table = nullptr;
   int err_word = -1;  // index of a device error word in the table (bounded waits), -1: none
+  bool max_carveout = false;  // ask for the largest shared-memory carveout of the L1 array
 };
 
 struct ColVariant {
@@ -262,6 +263,7 @@ class Ops : public OpsBase {
     v.table_words = Tc5Layout::WORDS;
     v.build_table = &tc5_build_table<N>;
     v.err_word = Tc5Layout::ERR;
+    v.max_carveout = true;
     xv.push_back(v);
   }
 

@@ -59,6 +59,11 @@ int OpsBase::setup(const Geom& g) {
       if (x.build_table(x.table)) return report_error(MHD_ERR_CUDA, "building the tensor-core DFT tables failed");
     }
     if ((rc = set_smem((const void*)x.fn, x.smem))) return rc;
+    if (x.max_carveout) {
+      // the whole unified L1 / shared array as shared memory: two CTAs per SM fit only then
+      e = cudaFuncSetAttribute((const void*)x.fn, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+      if (e != cudaSuccess) return report_error(MHD_ERR_CUDA, std::string("cudaFuncSetAttribute: ") + cudaGetErrorString(e));
+    }
     if ((rc = resident_ctas((const void*)x.fn, x.threads, x.smem, sms, &x.ctas))) return rc;
   }
   for (auto& c : cv) {

@@ -160,7 +160,8 @@ __device__ __forceinline__ void tc5_store_operand(uint32_t tlane, const float (&
 
 // One 16-point stage for the whole CTA: every thread has stored its A row; the elected thread
 // issues D = A_hi B_hi + A_hi B_lo + A_lo B_hi (four K = 8 steps each) into column dcol and
-// commits to the barrier; everyone waits for the phase (bounded).  Returns false on a timeout.
+// commits to the barrier; that thread waits for the phase (bounded) and the CTA barrier releases
+// the others.  Returns false on a timeout.
 __device__ __forceinline__ bool tc5_stage(uint32_t tbase, uint32_t dcol, uint32_t bhi, uint32_t blo, uint32_t bar,
                                           uint32_t phase) {
   tc5_fence_before();
@@ -185,9 +186,11 @@ __device__ __forceinline__ bool tc5_stage(uint32_t tbase, uint32_t dcol, uint32_
     }
     asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
   }
-  const bool ok = mbar_wait(bar, phase & 1u);
+  // one thread polls the barrier (bounded); the others wait at the CTA barrier without issuing
+  const bool ok = threadIdx.x == 0 ? mbar_wait(bar, phase & 1u) : true;
+  const bool all = __syncthreads_and(ok ? 1 : 0) != 0;
   tc5_fence_after();
-  return __syncthreads_and(ok ? 1 : 0) != 0;
+  return all;
 }
 
 // Transpose of a 16 x 16 complex block between the 16 lanes of a row (inside one warp): lane j
