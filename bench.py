@@ -241,8 +241,13 @@ def run_serve(args):
     mk = lambda: serving.poisson_requests(args.serve_count, 20.0, [32, 48, 64, 128, 256],  # noqa: E731
                                          [0.3, 0.25, 0.2, 0.15, 0.1], (lo, hi), (5e-4, 5e-3), seed=11)
     reqs = mk()
-    for r in reqs:  # inputs are built before the clock starts
-        r.init_state = initial_state(r.n, r.seed)
+    # inputs are built before the clock starts, on host threads (numpy releases the GIL in the
+    # array work)
+    from concurrent.futures import ThreadPoolExecutor
+
+    with ThreadPoolExecutor(max_workers=min(16, os.cpu_count() or 1)) as ex:
+        for r, st in zip(reqs, ex.map(lambda q: initial_state(q.n, q.seed), reqs)):
+            r.init_state = st
     srv = serving.Server(serving.GpuBackend(pkg, "RK4"), budget_bytes=150e9, steps_per_tick=8)
     rep = srv.run(reqs, realtime=True)
     nrep = None
