@@ -97,7 +97,7 @@ Geom make_geom(int n, double L) {
 
 // Kernel classes for per-launch timing (KClass of ops.cuh).
 const char* kClassNames[KC_COUNT] = {"z_inverse", "y_inverse", "x_fused", "y_forward", "z_forward", "rk_epilogue",
-                                     "other"};
+                                     "herm_kx0", "other"};
 
 const double kLsA[5] = {0.0, -567301805773.0 / 1357537059087.0, -2404267990393.0 / 2016746695238.0,
                         -3550918686646.0 / 2091501179385.0, -1275806237668.0 / 842570457699.0};
@@ -501,10 +501,18 @@ struct mhd_problem {
   }
   // Stage epilogue: RHS from the 8 compact product planes (in rowbuf; 14 with the VP penalty
   // fields) and the stage state X.
+  int herm(const float2* X, BatchRef br) {
+    return launch(KC_HERM, [&] {
+      const int bxh = g.k2 <= 256 ? (g.k2 + 31) / 32 * 32 : 256;
+      const dim3 gh((g.k2 + bxh - 1) / bxh, g.k2, cap);
+      herm_kx0_kernel<<<gh, bxh, 0, stream>>>(X, aux, g, FS(), ST(), FS(), br);
+    });
+  }
   RkArgs rk_args(const float2* X, float2* xn, int op, float hf, float ca, float cb, int stage) const {
     RkArgs a{};
     a.prod = rowbuf;
     a.X = X;
+    a.H = aux;
     a.sol = sol;
     a.acc = acc;
     a.xn = xn;
@@ -512,6 +520,7 @@ struct mhd_problem {
     a.fs = FS();
     a.stI = ST();
     a.prodI = sz.rowbuf;
+    a.hI = FS();
     a.hf = hf;
     a.ca = ca;
     a.cb = cb;
@@ -527,9 +536,11 @@ struct mhd_problem {
   // HDcalcN! (src/pgen.jl:176-182) calls addforcing! before HDcalcN_advection!, whose UᵢUpdate!
   // starts by zeroing the velocity right-hand side: a hydrodynamic problem is unforced
   bool forced() const { return forcing && !p.hydro_only; }
-  // xn: where the stage update writes (the next stage state, or sol; it may be X itself: the
-  // epilogue reads each kx = 0 mode pair before it writes it)
+  // xn: where the stage update writes (the next stage state, or sol; it may be X itself, so the
+  // Hermitian part of X's kx = 0 plane is copied out first by herm_kx0)
   int epilogue(const float2* X, float2* xn, int op, float hf, float ca, float cb, BatchRef br, int stage) {
+    int rc = herm(X, br);
+    if (rc) return rc;
     const RkArgs a = rk_args(X, xn, op, hf, ca, cb, stage);
     const int bx = g.kx <= 256 ? (g.kx + 31) / 32 * 32 : 256;
     const dim3 grid((g.kx + bx - 1) / bx, g.k2, g.k2 * cap);
@@ -1779,6 +1790,7 @@ int mhd_kernel_class_bytes(mhd_handle h, int cls, double* bytes) {
     case KC_YFWD: b = ns * (n * n * kx * c + n * k2 * kx * c); break;
     case KC_ZFWD: b = ns * (n * k2 * kx * c + state_field); break;
     case KC_RKEPI: b = ns * state_field + arrays * nin * state_field + nin * k2 * k2 * c; break;
+    case KC_HERM: b = 2 * 6 * k2 * k2 * c; break;
     default: b = 0;
   }
   *bytes = b * inst;

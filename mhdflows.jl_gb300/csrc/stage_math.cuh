@@ -25,12 +25,13 @@ enum StageOp : int {
 struct RkArgs {
   const float2* prod;   // 8 compact product planes, then 6 penalty planes with VP (slot stride prodI)
   const float2* X;      // stage state (6 fields, slot stride stI)
+  const float2* H;      // Hermitian part of X on the kx = 0 plane, [f][kz'][ky'] (slot stride hI)
   float2* sol;          // RK4 step-start state
   float2* acc;          // RK4 accumulator / LSRK4 du / OP_RHS output
   float2* xn;           // RK4 next stage state / LSRK4 u
   const SlotParams* sp; // per-slot nu, eta, dt
   long long fs;         // compact field stride (complex elements)
-  long long stI, prodI;
+  long long stI, prodI, hI;
   float hf;             // RK4 stage fraction of dt (1/2 or 1)
   float ca, cb;         // LSRK4 coefficients of the stage
   float pscale;         // 1/n^6: the column and row passes are unnormalised in both directions
@@ -128,19 +129,27 @@ struct ModeSums {
 };
 
 // The right-hand side of one retained mode (jz, jy, x) of a slot from its sums, the stage state
-// xv and the state its diffusion acts on xd (xv itself, or on the kx = 0 plane its Hermitian
-// part), volume penalisation, forcing, and the stage update.  i is the mode's offset in a compact
-// field; prod the slot's product planes (VPEN only).
+// (the kx = 0 plane diffuses its Hermitian part), volume penalisation, forcing, and the stage
+// update.  i is the mode's offset in a compact field; prod the slot's product planes (VPEN only).
 template <int OP, bool FORCED, bool VPEN, bool HD>
 __device__ __forceinline__ void finish_mode(const RkArgs& a, const Geom& geo, int slot, int jz, int jy, int x, long long i,
-                                            float kxv, float kyv, float kzv, const ModeSums& m, const float2* prod,
-                                            const float2 (&xv)[6], const float2 (&xd)[6]) {
+                                            float kxv, float kyv, float kzv, const ModeSums& m, const float2* prod) {
   constexpr int NF = HD ? 3 : 6;
   const long long fs = a.fs;
   const SlotParams sp = a.sp[slot];
   const long long so = slot * a.stI;
   RkSlot rs{a.sol + so, a.acc + so, a.xn + so, a.hf * sp.dt, sp.dt, a.ca, a.cb};
+  const float2* X = a.X + so;
   const float k2 = kxv * kxv + kyv * kyv + kzv * kzv;
+  float2 xv[6], xd[6];
+#pragma unroll
+  for (int c = 0; c < 6; ++c) xv[c] = xd[c] = c < NF ? X[c * fs + i] : make_float2(0.f, 0.f);
+  if (x == 0) {
+    const long long p = (long long)jz * geo.k2 + jy, pl = (long long)geo.k2 * geo.k2;
+    const float2* H = a.H + slot * a.hI;
+#pragma unroll
+    for (int c = 0; c < NF; ++c) xd[c] = H[c * pl + p];
+  }
   const float ik2 = k2 > 0.f ? 1.0f / k2 : 0.f;
   const float kvx = (kxv * m.Vx.x + kyv * m.Vy.x + kzv * m.Vz.x) * ik2;
   const float kvy = (kxv * m.Vx.y + kyv * m.Vy.y + kzv * m.Vz.y) * ik2;

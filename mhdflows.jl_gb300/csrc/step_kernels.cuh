@@ -6,35 +6,10 @@
 
 namespace mhdgb {
 
-// The stress and induction sums of the mode at offset i of a slot's product planes.
-template <bool HD>
-__device__ __forceinline__ ModeSums mode_sums(const float2* prod, long long fs, long long i, float pscale, float kxv,
-                                              float kyv, float kzv) {
-  float2 p[8];
-#pragma unroll
-  for (int q = 0; q < 8; ++q) p[q] = (HD && q >= 5) ? make_float2(0.f, 0.f) : cscale(__ldcs(prod + q * fs + i), pscale);
-  const float2 dxz = p[0], dyz = p[1], txy = p[2], txz = p[3], tyz = p[4];
-  const float2 axy = p[5], axz = p[6], ayz = p[7];
-  ModeSums m;
-  m.Vx = make_float2(kxv * dxz.x + kyv * txy.x + kzv * txz.x, kxv * dxz.y + kyv * txy.y + kzv * txz.y);
-  m.Vy = make_float2(kxv * txy.x + kyv * dyz.x + kzv * tyz.x, kxv * txy.y + kyv * dyz.y + kzv * tyz.y);
-  m.Vz = make_float2(kxv * txz.x + kyv * tyz.x, kxv * txz.y + kyv * tyz.y);
-  m.Wx = make_float2(kyv * axy.x + kzv * axz.x, kyv * axy.y + kzv * axz.y);
-  m.Wy = make_float2(kzv * ayz.x - kxv * axy.x, kzv * ayz.y - kxv * axy.y);
-  m.Wz = make_float2(-(kxv * axz.x + kyv * ayz.x), -(kxv * axz.y + kyv * ayz.y));
-  return m;
-}
-
 // grid (ceil(kx / blockDim.x), k2, k2): one thread per retained mode, no index division.
 // HD: the hydrodynamic form (three fields, five product planes; B is neither read nor written).
-// The kx = 0 plane diffuses the Hermitian part (X(k) + conj X(-k)) / 2 of the stage state (what
-// the reference's rfft(irfft(X)) does there), with X(-k) = 0 when -k is in the alias band.  The
-// stage update may write X in place, so the two modes k and -k of that plane are handled by one
-// thread, the one of the lower plane index: it reads both old values before it writes either,
-// and the other thread of the pair does nothing.
 template <int OP, bool FORCED, bool VPEN, bool HD = false>
 __global__ void __launch_bounds__(256) rk_epilogue_kernel(RkArgs a, Geom geo, BatchRef br) {
-  constexpr int NF = HD ? 3 : 6;
   const int x = blockIdx.x * blockDim.x + threadIdx.x;
   if (x >= geo.kx) return;
   const int inst = blockIdx.z / geo.k2;
@@ -44,36 +19,54 @@ __global__ void __launch_bounds__(256) rk_epilogue_kernel(RkArgs a, Geom geo, Ba
   const long long fs = a.fs;
   const long long i = ((long long)jz * geo.k2 + jy) * geo.kxp + x;
   const float2* prod = a.prod + slot * a.prodI;
-  const float2* X = a.X + slot * a.stI;
   const float kxv = geo.kscale * (float)x;
   const float kyv = geo.kscale * (float)signed_of_kept(geo, jy);
   const float kzv = geo.kscale * (float)signed_of_kept(geo, jz);
-  float2 xv[6];
+  float2 p[8];
 #pragma unroll
-  for (int c = 0; c < 6; ++c) xv[c] = c < NF ? X[c * fs + i] : make_float2(0.f, 0.f);
-  if (x != 0) {
-    finish_mode<OP, FORCED, VPEN, HD>(a, geo, slot, jz, jy, x, i, kxv, kyv, kzv,
-                                      mode_sums<HD>(prod, fs, i, a.pscale, kxv, kyv, kzv), prod, xv, xv);
-    return;
-  }
+  for (int q = 0; q < 8; ++q) p[q] = (HD && q >= 5) ? make_float2(0.f, 0.f) : cscale(__ldcs(prod + q * fs + i), a.pscale);
+  const float2 dxz = p[0], dyz = p[1], txy = p[2], txz = p[3], tyz = p[4];
+  const float2 axy = p[5], axz = p[6], ayz = p[7];
+  ModeSums m;
+  m.Vx = make_float2(kxv * dxz.x + kyv * txy.x + kzv * txz.x, kxv * dxz.y + kyv * txy.y + kzv * txz.y);
+  m.Vy = make_float2(kxv * txy.x + kyv * dyz.x + kzv * tyz.x, kxv * txy.y + kyv * dyz.y + kzv * tyz.y);
+  m.Vz = make_float2(kxv * txz.x + kyv * tyz.x, kxv * txz.y + kyv * tyz.y);
+  m.Wx = make_float2(kyv * axy.x + kzv * axz.x, kyv * axy.y + kzv * axz.y);
+  m.Wy = make_float2(kzv * ayz.x - kxv * axy.x, kzv * ayz.y - kxv * axy.y);
+  m.Wz = make_float2(-(kxv * axz.x + kyv * ayz.x), -(kxv * axz.y + kyv * ayz.y));
+  finish_mode<OP, FORCED, VPEN, HD>(a, geo, slot, jz, jy, x, i, kxv, kyv, kzv, m, prod);
+}
+
+// Hermitian part of the kx = 0 plane of the six fields: H(k) = (X(k) + conj X(-k)) / 2, with
+// X(-k) = 0 when -k is in the alias band.  The reference's diffusion term is computed from the
+// re-transformed physical field, rfft(irfft(X)), which is exactly this on the kx = 0 plane.
+__global__ void herm_kx0_kernel(const float2* __restrict__ Xpool, float2* __restrict__ Hpool, Geom geo, long long fs,
+                                long long stI, long long hI, BatchRef br) {
+  // grid (ceil(K2 / blockDim.x), K2, cap): one thread per (ky', kz') of one instance, all six
+  // fields in flight
+  const int jy = blockIdx.x * blockDim.x + threadIdx.x;
+  const int jz = blockIdx.y;
+  const int inst = blockIdx.z;
+  if (jy >= geo.k2 || inst >= *br.count) return;
+  const int slot = br.list[inst];
+  const float2* X = Xpool + slot * stI;
+  float2* H = Hpool + slot * hI;
   const int py = kept_of_signed(geo, -signed_of_kept(geo, jy));
   const int pz = kept_of_signed(geo, -signed_of_kept(geo, jz));
   const bool partner = py >= 0 && pz >= 0;
-  const long long own = (long long)jz * geo.k2 + jy, par = (long long)pz * geo.k2 + py;
-  if (partner && par < own) return;  // the partner's thread handles both modes
-  const long long ip = partner ? par * geo.kxp : i;
-  float2 xp[6], hd[6], hp[6];
+  const long long own = ((long long)jz * geo.k2 + jy) * geo.kxp;
+  const long long par = partner ? ((long long)pz * geo.k2 + py) * geo.kxp : own;
+  const long long pl = (long long)geo.k2 * geo.k2;
+  float2 xk[6], xp[6];
 #pragma unroll
   for (int c = 0; c < 6; ++c) {
-    xp[c] = (c < NF && partner) ? X[c * fs + ip] : make_float2(0.f, 0.f);
-    hd[c] = make_float2(0.5f * (xv[c].x + xp[c].x), 0.5f * (xv[c].y - xp[c].y));
-    hp[c] = make_float2(0.5f * (xp[c].x + xv[c].x), 0.5f * (xp[c].y - xv[c].y));
+    xk[c] = X[c * fs + own];
+    xp[c] = X[c * fs + par];
   }
-  finish_mode<OP, FORCED, VPEN, HD>(a, geo, slot, jz, jy, 0, i, 0.f, kyv, kzv,
-                                    mode_sums<HD>(prod, fs, i, a.pscale, 0.f, kyv, kzv), prod, xv, hd);
-  if (partner && par != own) {
-    finish_mode<OP, FORCED, VPEN, HD>(a, geo, slot, pz, py, 0, ip, 0.f, -kyv, -kzv,
-                                      mode_sums<HD>(prod, fs, ip, a.pscale, 0.f, -kyv, -kzv), prod, xp, hp);
+#pragma unroll
+  for (int c = 0; c < 6; ++c) {
+    const float2 q = partner ? xp[c] : make_float2(0.f, 0.f);
+    H[c * pl + (long long)jz * geo.k2 + jy] = make_float2(0.5f * (xk[c].x + q.x), 0.5f * (xk[c].y - q.y));
   }
 }
 
