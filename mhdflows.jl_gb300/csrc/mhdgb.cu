@@ -331,8 +331,8 @@ struct mhd_problem {
   // a zeroed device buffer and the side stream its copies run on
   void* zeros = nullptr;
   size_t zbytes = 0;
-  cudaStream_t zstream = nullptr, zstream2 = nullptr;  // copy-engine side streams
-  cudaEvent_t ev_z = nullptr, ev_z2 = nullptr;          // order them against the handle's stream
+  cudaStream_t zstream = nullptr;
+  cudaEvent_t ev_z = nullptr;  // orders the copy-engine side stream against the handle's stream
   int ensure_zero_source() {
     if (zeros) return MHD_OK;
     const size_t want = size_t(16) << 20;
@@ -340,9 +340,7 @@ struct mhd_problem {
     MHD_CUDA(cudaMemset(zeros, 0, want));
     zbytes = want;
     if (!zstream) MHD_CUDA(cudaStreamCreateWithFlags(&zstream, cudaStreamNonBlocking));
-    if (!zstream2) MHD_CUDA(cudaStreamCreateWithFlags(&zstream2, cudaStreamNonBlocking));
     if (!ev_z) MHD_CUDA(cudaEventCreateWithFlags(&ev_z, cudaEventDisableTiming));
-    if (!ev_z2) MHD_CUDA(cudaEventCreateWithFlags(&ev_z2, cudaEventDisableTiming));
     return MHD_OK;
   }
   // guard bands: every large buffer is allocated kGuardBytes longer and the tail filled with
@@ -397,13 +395,11 @@ struct mhd_problem {
     if (ev_out) cudaEventDestroy(ev_out);
     ev_in = ev_out = nullptr;
     if (zstream) cudaStreamSynchronize(zstream), cudaStreamDestroy(zstream);
-    if (zstream2) cudaStreamSynchronize(zstream2), cudaStreamDestroy(zstream2);
     if (zeros) cudaFree(zeros);
     if (ev_z) cudaEventDestroy(ev_z);
-    if (ev_z2) cudaEventDestroy(ev_z2);
-    zstream = zstream2 = nullptr;
+    zstream = nullptr;
     zeros = nullptr;
-    ev_z = ev_z2 = nullptr;
+    ev_z = nullptr;
     void* ptrs[] = {sol, xs, acc, aux, colbuf, rowbuf, ref, phys, diag_partial, diag_out, maxabs, dparams, dlist, dvmax, dtime,
                     dstep, derr, vchi, vwall};
     for (void* q : ptrs) if (q) cudaFree(q);
@@ -1093,17 +1089,40 @@ void* mapped_host(const void* p, size_t bytes) {
   return a0.devicePointer;
 }
 
-// Copy-engine writes of zeros from `zeros` (zbytes of zeroed device memory) into everything of a
-// host reference-layout state outside the retained band, for fields [f0, f1), on stream s: the
-// alias z-planes, the alias row block of every kept z-plane, and the tail kx >= Kx of every kept
-// row (3-D copies over the kept ky and kz ranges).
-cudaError_t zero_outside_retained(float2* ref, const Geom& g, int f0, int f1, const void* zeros, size_t zbytes,
-                                  cudaStream_t s) {
+// The alias band of a reference-layout state (nf, n, n, nkr) outside the retained band (the
+// complement of scatter_retained_kernel) has three parts per field: the z-planes of the alias
+// band [kp, n - kn), a block of alias rows [kp, n - kn) in every kept z-plane, and the tail
+// kx >= Kx of every kept row.  zero_row_tails zeroes the tails on host threads; the planes and
+// row blocks go to the copy engine (zero_alias_blocks).
+void zero_row_tails(float2* ref, const Geom& g, int nf) {
   const size_t nkr = g.n / 2 + 1, row = nkr * sizeof(float2), plane = (size_t)g.n * row;
-  const size_t na = (size_t)(g.n - g.kp - g.kn), tail = (nkr - g.kx) * sizeof(float2);
-  const int r0[2] = {0, g.n - g.kn}, rc[2] = {g.kp, g.kn};
+  const size_t tail = (nkr - g.kx) * sizeof(float2);
+  const int planes = nf * g.k2;  // kept z-planes of every field
+  auto zero_plane = [&](int q) {
+    const int f = q / g.k2, jz = q % g.k2;
+    char* p = reinterpret_cast<char*>(ref) + ((size_t)f * g.n + freq_of_kept(g, jz)) * plane;
+    for (int j = 0; j < g.k2; ++j) std::memset(p + (size_t)freq_of_kept(g, j) * row + g.kx * sizeof(float2), 0, tail);
+  };
+  // one thread per 4 MB of tails, at most 16 and at most the hardware threads
+  const size_t bytes = (size_t)planes * g.k2 * tail;
+  const unsigned hw = std::thread::hardware_concurrency();
+  const int nt = (int)std::min<size_t>(std::max<size_t>(1, std::min<size_t>(16, bytes >> 22)), hw ? hw : 1);
+  auto work = [&](int t) {
+    for (int q = t; q < planes; q += nt) zero_plane(q);
+  };
+  std::vector<std::thread> pool;
+  for (int t = 1; t < nt; ++t) pool.emplace_back(work, t);
+  work(0);
+  for (auto& th : pool) th.join();
+}
+
+// Copy-engine writes of zeros from `zeros` (zbytes of zeroed device memory) into the alias planes
+// and the alias row blocks of a host reference-layout state, on stream s.
+cudaError_t zero_alias_blocks(float2* ref, const Geom& g, int nf, const void* zeros, size_t zbytes, cudaStream_t s) {
+  const size_t nkr = g.n / 2 + 1, row = nkr * sizeof(float2), plane = (size_t)g.n * row;
+  const size_t na = (size_t)(g.n - g.kp - g.kn);
   char* base = reinterpret_cast<char*>(ref);
-  for (int f = f0; f < f1; ++f) {
+  for (int f = 0; f < nf; ++f) {
     // the alias z-planes of field f: one contiguous block, in pieces of at most zbytes
     char* p = base + ((size_t)f * g.n + g.kp) * plane;
     for (size_t left = na * plane; left > 0;) {
@@ -1117,32 +1136,13 @@ cudaError_t zero_outside_retained(float2* ref, const Geom& g, int f0, int f1, co
     // planes that fit the zero buffer
     const size_t width = na * row;
     const size_t per = std::max<size_t>(1, zbytes / width);
+    const int z0[2] = {0, g.n - g.kn}, zc[2] = {g.kp, g.kn};
     for (int r = 0; r < 2; ++r)
-      for (int z = 0; z < rc[r]; z += (int)per) {
-        const size_t h = std::min<size_t>(per, (size_t)(rc[r] - z));
-        char* d = base + (((size_t)f * g.n + r0[r] + z) * g.n + g.kp) * row;
+      for (int z = 0; z < zc[r]; z += (int)per) {
+        const size_t h = std::min<size_t>(per, (size_t)(zc[r] - z));
+        char* d = base + (((size_t)f * g.n + z0[r] + z) * g.n + g.kp) * row;
         const cudaError_t e = cudaMemcpy2DAsync(d, plane, zeros, width, width, h, cudaMemcpyDeviceToHost, s);
         if (e != cudaSuccess) return e;
-      }
-    // the tails of the kept rows: for each kept ky range and kz range a box of rows, in groups of
-    // planes whose zeros fit the zero buffer
-    if (tail == 0) continue;
-    for (int bz = 0; bz < 2; ++bz)
-      for (int by = 0; by < 2; ++by) {
-        if (rc[bz] == 0 || rc[by] == 0) continue;
-        const size_t pl = tail * (size_t)rc[by];
-        const int dz = (int)std::max<size_t>(1, zbytes / pl);
-        for (int z = 0; z < rc[bz]; z += dz) {
-          cudaMemcpy3DParms q = {};
-          q.srcPtr = make_cudaPitchedPtr(const_cast<void*>(zeros), tail, tail, rc[by]);
-          q.dstPtr = make_cudaPitchedPtr(ref, row, row, g.n);
-          q.srcPos = make_cudaPos(0, 0, 0);
-          q.dstPos = make_cudaPos((size_t)g.kx * sizeof(float2), r0[by], (size_t)f * g.n + r0[bz] + z);
-          q.extent = make_cudaExtent(tail, rc[by], std::min(dz, rc[bz] - z));
-          q.kind = cudaMemcpyDeviceToHost;
-          const cudaError_t e = cudaMemcpy3DAsync(&q, s);
-          if (e != cudaSuccess) return e;
-        }
       }
   }
   return cudaSuccess;
@@ -1150,11 +1150,11 @@ cudaError_t zero_outside_retained(float2* ref, const Geom& g, int f0, int f1, co
 
 // How state transfers to and from page-locked host buffers mapped into the device address space
 // move their bytes ($MHDGB_HOST_TRANSFER, read once; other host memory always takes the copy path):
-//   mapped (default) the retained band crosses on three paths at once: the gather / scatter
-//          kernels read or write a third of the fields straight in the caller's array, and two
-//          copy-engine streams move the other two thirds through the device staging array;
-//          get_state writes the zeros outside the retained band from a zeroed device buffer on
-//          the two copy-engine streams while the step still runs.
+//   mapped (default) kernels read and write the caller's array directly: set_state gathers the
+//          retained band of half the fields over the link while the copy engine brings the other
+//          half; get_state writes the alias-band zeros from the copy engine (whole planes and row
+//          blocks, from a zeroed device buffer) and from host threads (the tail of each kept row)
+//          while the step still runs, then the retained band crosses on both paths at once.
 //   copy   the copy engines only (about 200 GB/s over the host link): set_state copies the
 //          retained band of the caller's array into the device staging array (one 3-D copy per
 //          field and ky / kz range) and gathers it there; get_state scatters into the staging
@@ -1214,26 +1214,21 @@ int mhd_slot_set_state(mhd_handle h, int slot, const float* sol) {
   float2* dst = h->sol + slot * h->sz.state;
   const float2* mapped = mapped_transfers() ? static_cast<const float2*>(mapped_host(sol, bytes)) : nullptr;
   if (mapped) {
-    // the retained band crosses the host link on three paths at once: the gather kernel reads
-    // the first third of the fields straight from the mapped array, and two copy-engine streams
-    // bring the retained band of the other two thirds into the staging array, gathered from there
+    // the retained band crosses the host link on two paths at once: the gather kernel reads the
+    // first half of the fields straight from the mapped array, while the copy engine brings the
+    // retained band of the other half into the staging array, gathered from there
     if ((rc = h->ensure_zero_source())) return rc;
-    const int fa = nf / 3, fb = 2 * nf / 3;
-    const float2* host = reinterpret_cast<const float2*>(sol);
+    const int hf = nf / 2;
     MHD_CUDA(cudaEventRecord(h->ev_z, h->stream));  // the staging array is free once earlier work is done
     MHD_CUDA(cudaStreamWaitEvent(h->zstream, h->ev_z, 0));
-    MHD_CUDA(cudaStreamWaitEvent(h->zstream2, h->ev_z, 0));
-    cudaError_t e = copy_retained(h->ref + fa * fref, host + fa * fref, h->g, fb - fa, cudaMemcpyHostToDevice, h->zstream);
-    if (e == cudaSuccess)
-      e = copy_retained(h->ref + fb * fref, host + fb * fref, h->g, nf - fb, cudaMemcpyHostToDevice, h->zstream2);
+    const cudaError_t e = copy_retained(h->ref + hf * fref, reinterpret_cast<const float2*>(sol) + hf * fref, h->g,
+                                        nf - hf, cudaMemcpyHostToDevice, h->zstream);
     if (e != cudaSuccess) return fail(MHD_ERR_CUDA, std::string("set_state copy: ") + cudaGetErrorString(e));
     MHD_CUDA(cudaEventRecord(h->ev_z, h->zstream));
-    MHD_CUDA(cudaEventRecord(h->ev_z2, h->zstream2));
-    if ((rc = h->launch(KC_OTHER, [&] { gather_state_kernel<<<1216, 256, 0, h->stream>>>(mapped, dst, h->g, fa); }))) return rc;
+    if ((rc = h->launch(KC_OTHER, [&] { gather_state_kernel<<<1216, 256, 0, h->stream>>>(mapped, dst, h->g, hf); }))) return rc;
     MHD_CUDA(cudaStreamWaitEvent(h->stream, h->ev_z, 0));
-    MHD_CUDA(cudaStreamWaitEvent(h->stream, h->ev_z2, 0));
     if ((rc = h->launch(KC_OTHER, [&] {
-           gather_state_kernel<<<1216, 256, 0, h->stream>>>(h->ref + fa * fref, dst + fa * h->sz.fs, h->g, nf - fa);
+           gather_state_kernel<<<1216, 256, 0, h->stream>>>(h->ref + hf * fref, dst + hf * h->sz.fs, h->g, nf - hf);
          })))
       return rc;
   } else {
@@ -1262,31 +1257,29 @@ int mhd_slot_get_state(mhd_handle h, int slot, float* sol) {
          })))
       return rc;
   } else if (out) {
-    // mapped memory.  The zeros outside the retained band (71% of the bytes) do not wait for the
-    // step: two copy-engine streams write them from a zeroed device buffer while the handle's
-    // stream still runs.  After the step the retained band crosses on three paths at once: the
-    // device writes the first third of the fields straight into the mapping, and the other two
-    // thirds are scattered into the staging array and brought over by the two copy-engine streams.
+    // mapped memory.  The zeros of the alias band do not wait for the step: the copy engine
+    // writes the alias planes and row blocks from a zeroed device buffer on a side stream, and
+    // host threads zero the row tails, both while the handle's stream still runs.  After the
+    // step the retained band (29% of the bytes) crosses on two paths at once: the device writes
+    // the first half of the fields straight into the mapping, and the other half is scattered
+    // into the staging array and brought over by the copy engine.
     if ((rc = h->ensure_zero_source())) return rc;
-    const int fa = nf / 3, fb = 2 * nf / 3, fh = nf / 2;
+    const int hf = nf / 2;
     float2* host = reinterpret_cast<float2*>(sol);
-    MHD_CUDA(zero_outside_retained(host, h->g, 0, fh, h->zeros, h->zbytes, h->zstream));
-    MHD_CUDA(zero_outside_retained(host, h->g, fh, nf, h->zeros, h->zbytes, h->zstream2));
+    MHD_CUDA(zero_alias_blocks(host, h->g, nf, h->zeros, h->zbytes, h->zstream));
     if ((rc = h->launch(KC_OTHER, [&] {
-           scatter_retained_kernel<<<1216, 256, 0, h->stream>>>(src + fa * h->sz.fs, h->ref + fa * fref, h->g, nf - fa);
+           scatter_retained_kernel<<<1216, 256, 0, h->stream>>>(src + hf * h->sz.fs, h->ref + hf * fref, h->g, nf - hf);
          })))
       return rc;
     MHD_CUDA(cudaEventRecord(h->ev_z, h->stream));
     MHD_CUDA(cudaStreamWaitEvent(h->zstream, h->ev_z, 0));
-    MHD_CUDA(cudaStreamWaitEvent(h->zstream2, h->ev_z, 0));
-    MHD_CUDA(copy_retained(host + fa * fref, h->ref + fa * fref, h->g, fb - fa, cudaMemcpyDeviceToHost, h->zstream));
-    MHD_CUDA(copy_retained(host + fb * fref, h->ref + fb * fref, h->g, nf - fb, cudaMemcpyDeviceToHost, h->zstream2));
+    MHD_CUDA(copy_retained(host + hf * fref, h->ref + hf * fref, h->g, nf - hf, cudaMemcpyDeviceToHost, h->zstream));
     if ((rc = h->launch(KC_OTHER, [&] {
-           scatter_retained_kernel<<<1216, 256, 0, h->stream>>>(src, out, h->g, fa);
+           scatter_retained_kernel<<<1216, 256, 0, h->stream>>>(src, out, h->g, hf);
          })))
       return rc;
+    zero_row_tails(host, h->g, nf);
     MHD_CUDA(cudaStreamSynchronize(h->zstream));
-    MHD_CUDA(cudaStreamSynchronize(h->zstream2));
   } else {
     // the full array is assembled in the staging buffer at HBM speed, zeros included, and comes
     // back in one contiguous copy
