@@ -3,7 +3,8 @@
 // A length-N transform is spread over G cooperating threads that each hold V = N/G complex
 // values in registers.  N = R0*R1*R2 (R2 may be 1) and every radix divides V, so each stage is
 // V/R_s small DFTs per thread, done fully unrolled in registers (Cooley-Tukey codelets built from
-// radix-2/3/4 butterflies).  Between stages the values are exchanged through shared memory; the
+// radix-2/3/4 butterflies, in the paired FP32 instructions of the sm_100 family where the inputs
+// are run-time values).  Between stages the values are exchanged through shared memory; the
 // stage twiddles W_N^j come from a per-size table computed in double precision on the host.
 //
 // Index conventions (DIR = -1 forward, +1 inverse, X[k] = sum_n x[n] exp(DIR*2*pi*i*n*k/N)):
@@ -90,6 +91,24 @@ __device__ __forceinline__ float2 cmul_diri(float2 a) {
   return DIR > 0 ? make_float2(-a.y, a.x) : make_float2(a.y, -a.x);
 }
 
+// Paired FP32 arithmetic of the sm_100 family: one instruction updates both components of a
+// complex value, each component rounded exactly like the scalar operation.  The codelets below
+// use it wherever their inputs are run-time values (PK = true); a stage whose inputs include
+// compile-time zeros (the pruned first stage of an inverse transform) keeps the scalar forms,
+// which fold those zeros away.
+__device__ __forceinline__ float2 padd(float2 a, float2 b) { return __fadd2_rn(a, b); }
+// a - b: b * (-1) is exact, so the fused form rounds once, like a - b
+__device__ __forceinline__ float2 psub(float2 a, float2 b) { return __ffma2_rn(b, make_float2(-1.f, -1.f), a); }
+// a + m * b, componentwise, one rounding per component
+__device__ __forceinline__ float2 paxpy(float2 b, float2 m, float2 a) { return __ffma2_rn(b, m, a); }
+template <bool PK>
+__device__ __forceinline__ float2 kadd(float2 a, float2 b) { return PK ? padd(a, b) : cadd(a, b); }
+template <bool PK>
+__device__ __forceinline__ float2 ksub(float2 a, float2 b) { return PK ? psub(a, b) : csub(a, b); }
+// (a.y - b.y, a.x - b.x): the difference with its components exchanged, as two scalar
+// subtractions that write the pair in exchanged order (no register moves)
+__device__ __forceinline__ float2 csub_swapped(float2 a, float2 b) { return make_float2(a.y - b.y, a.x - b.x); }
+
 // ------------------------------------------------------------------------------------------
 // Small in-register DFT codelets: x[0..R) in place, natural-order output.
 // ------------------------------------------------------------------------------------------
@@ -98,59 +117,107 @@ struct FirstFactor {
   static constexpr int value = (R % 4 == 0 && R != 4) ? 4 : (R % 2 == 0 && R != 2) ? 2 : (R % 3 == 0 && R != 3) ? 3 : R;
 };
 
-template <int R, int DIR>
+template <int R, int DIR, bool PK = true>
 struct Dft;
 
-template <int DIR>
-struct Dft<1, DIR> {
+template <int DIR, bool PK>
+struct Dft<1, DIR, PK> {
   template <int S, int O, int A>
   __device__ __forceinline__ static void run(float2 (&)[A]) {}
 };
 
-template <int DIR>
-struct Dft<2, DIR> {
+template <int DIR, bool PK>
+struct Dft<2, DIR, PK> {
   // operates on x[O], x[O+S]
   template <int S, int O, int A>
   __device__ __forceinline__ static void run(float2 (&x)[A]) {
     float2 a = x[O], b = x[O + S];
-    x[O] = cadd(a, b);
-    x[O + S] = csub(a, b);
+    x[O] = kadd<PK>(a, b);
+    x[O + S] = ksub<PK>(a, b);
   }
 };
 
-template <int DIR>
-struct Dft<3, DIR> {
+template <int DIR, bool PK>
+struct Dft<3, DIR, PK> {
   template <int S, int O, int A>
   __device__ __forceinline__ static void run(float2 (&x)[A]) {
     const float h = 0.86602540378443864676f;  // sqrt(3)/2
     float2 x0 = x[O], x1 = x[O + S], x2 = x[O + 2 * S];
-    float2 t1 = cadd(x1, x2);
-    float2 t2 = make_float2(fmaf(-0.5f, t1.x, x0.x), fmaf(-0.5f, t1.y, x0.y));
-    float2 d = csub(x1, x2);
-    float2 t3 = cmul_diri<DIR>(cscale(d, h));
-    x[O] = cadd(x0, t1);
-    x[O + S] = cadd(t2, t3);
-    x[O + 2 * S] = csub(t2, t3);
+    if constexpr (PK) {
+      // X1,2 = t2 +- DIR i h (x1 - x2) = t2 + (-+DIR h (x1-x2).y, +-DIR h (x1-x2).x)
+      const float2 t1 = padd(x1, x2);
+      const float2 t2 = paxpy(t1, make_float2(-0.5f, -0.5f), x0);
+      const float2 ds = csub_swapped(x1, x2);
+      x[O] = padd(x0, t1);
+      x[O + S] = paxpy(ds, make_float2(-DIR * h, DIR * h), t2);
+      x[O + 2 * S] = paxpy(ds, make_float2(DIR * h, -DIR * h), t2);
+    } else {
+      float2 t1 = cadd(x1, x2);
+      float2 t2 = make_float2(fmaf(-0.5f, t1.x, x0.x), fmaf(-0.5f, t1.y, x0.y));
+      float2 d = csub(x1, x2);
+      float2 t3 = cmul_diri<DIR>(cscale(d, h));
+      x[O] = cadd(x0, t1);
+      x[O + S] = cadd(t2, t3);
+      x[O + 2 * S] = csub(t2, t3);
+    }
   }
 };
 
-template <int DIR>
-struct Dft<4, DIR> {
+template <int DIR, bool PK>
+struct Dft<4, DIR, PK> {
   template <int S, int O, int A>
   __device__ __forceinline__ static void run(float2 (&x)[A]) {
     float2 x0 = x[O], x1 = x[O + S], x2 = x[O + 2 * S], x3 = x[O + 3 * S];
-    float2 a = cadd(x0, x2), b = csub(x0, x2);
-    float2 c = cadd(x1, x3), d = cmul_diri<DIR>(csub(x1, x3));
-    x[O] = cadd(a, c);
-    x[O + 2 * S] = csub(a, c);
-    x[O + S] = cadd(b, d);
-    x[O + 3 * S] = csub(b, d);
+    if constexpr (PK) {
+      // X1,3 = b +- DIR i e with e = x1 - x3: (b.x -+ DIR e.y, b.y +- DIR e.x)
+      const float2 a = padd(x0, x2), b = psub(x0, x2), c = padd(x1, x3);
+      const float2 es = csub_swapped(x1, x3);
+      x[O] = padd(a, c);
+      x[O + 2 * S] = psub(a, c);
+      x[O + S] = paxpy(es, make_float2((float)-DIR, (float)DIR), b);
+      x[O + 3 * S] = paxpy(es, make_float2((float)DIR, (float)-DIR), b);
+    } else {
+      float2 a = cadd(x0, x2), b = csub(x0, x2);
+      float2 c = cadd(x1, x3), d = cmul_diri<DIR>(csub(x1, x3));
+      x[O] = cadd(a, c);
+      x[O + 2 * S] = csub(a, c);
+      x[O + S] = cadd(b, d);
+      x[O + 3 * S] = csub(b, d);
+    }
+  }
+};
+
+// Radix 8 in paired arithmetic: X[k] = E[k] + W^k O[k], X[k+4] = E[k] - W^k O[k] with E, O the
+// 4-point DFTs of the even and odd inputs and W = exp(DIR 2 pi i / 8).  The odd-side products
+// W^k O[k] are formed componentwise before the last fused step:
+//   W^1 O = c (O.x - DIR O.y, O.y + DIR O.x),   W^3 O = c (-O.x - DIR O.y, DIR O.x - O.y),
+//   W^2 O = DIR i O,  c = sqrt(1/2).
+template <int DIR>
+struct Dft<8, DIR, true> {
+  template <int S, int O, int A>
+  __device__ __forceinline__ static void run(float2 (&x)[A]) {
+    constexpr float c = 0.70710678118654752440f;
+    float2 e[4] = {x[O], x[O + 2 * S], x[O + 4 * S], x[O + 6 * S]};
+    float2 o[4] = {x[O + S], x[O + 3 * S], x[O + 5 * S], x[O + 7 * S]};
+    Dft<4, DIR, true>::template run<1, 0>(e);
+    Dft<4, DIR, true>::template run<1, 0>(o);
+    x[O] = padd(e[0], o[0]);
+    x[O + 4 * S] = psub(e[0], o[0]);
+    const float2 u1 = make_float2(o[1].x - DIR * o[1].y, o[1].y + DIR * o[1].x);
+    x[O + S] = paxpy(u1, make_float2(c, c), e[1]);
+    x[O + 5 * S] = paxpy(u1, make_float2(-c, -c), e[1]);
+    const float2 o2s = make_float2(o[2].y, o[2].x);
+    x[O + 2 * S] = paxpy(o2s, make_float2((float)-DIR, (float)DIR), e[2]);
+    x[O + 6 * S] = paxpy(o2s, make_float2((float)DIR, (float)-DIR), e[2]);
+    const float2 u3 = make_float2(-o[3].x - DIR * o[3].y, DIR * o[3].x - o[3].y);
+    x[O + 3 * S] = paxpy(u3, make_float2(c, c), e[3]);
+    x[O + 7 * S] = paxpy(u3, make_float2(-c, -c), e[3]);
   }
 };
 
 // Composite R = P*Q (P = FirstFactor): x[n], n = Q*a + b;  X[k], k = ka + P*kb.
 // The element set is x[O + S*i], i = 0..R-1 (strided view inside a register array).
-template <int R, int DIR>
+template <int R, int DIR, bool PK>
 struct Dft {
   static constexpr int P = FirstFactor<R>::value;
   static constexpr int Q = R / P;
@@ -165,7 +232,7 @@ struct Dft {
       float2 t[P];
 #pragma unroll
       for (int a = 0; a < P; ++a) t[a] = x[O + S * (Q * a + b)];
-      Dft<P, DIR>::template run<1, 0>(t);
+      Dft<P, DIR, PK>::template run<1, 0>(t);
       // twiddle W_R^{b*ka}; multiples of a quarter turn are exact sign/swap operations
 #pragma unroll
       for (int ka = 0; ka < P; ++ka) {
@@ -190,7 +257,7 @@ struct Dft {
       float2 t[Q];
 #pragma unroll
       for (int b = 0; b < Q; ++b) t[b] = x[O + S * (Q * ka + b)];
-      Dft<Q, DIR>::template run<1, 0>(t);
+      Dft<Q, DIR, PK>::template run<1, 0>(t);
 #pragma unroll
       for (int kb = 0; kb < Q; ++kb) out[ka + P * kb] = t[kb];
     }
@@ -200,7 +267,7 @@ struct Dft {
 };
 
 // Run DFT-R on each of the D = A/R contiguous groups of a register array.
-template <int R, int DIR, int A>
+template <int R, int DIR, bool PK, int A>
 __device__ __forceinline__ void dft_groups(float2 (&x)[A]) {
   static_assert(A % R == 0, "radix must divide the per-thread count");
 #pragma unroll
@@ -208,7 +275,7 @@ __device__ __forceinline__ void dft_groups(float2 (&x)[A]) {
     float2 t[R];
 #pragma unroll
     for (int r = 0; r < R; ++r) t[r] = x[d * R + r];
-    Dft<R, DIR>::template run<1, 0>(t);
+    Dft<R, DIR, PK>::template run<1, 0>(t);
 #pragma unroll
     for (int r = 0; r < R; ++r) x[d * R + r] = t[r];
   }
@@ -286,15 +353,17 @@ struct PlanTw {
 // Executes stages of plan P on NT independent transforms held as v[t][V] by this thread.
 // Shared memory word address of logical element a for transform t is  buf[t*TS + a*STR + OFF].
 // SYNC() must be a barrier over every thread that shares buf.  tw is the plan's PlanTw table.
+// PK1: the first stage in paired arithmetic; false where its inputs hold compile-time zeros
+// (pruned alias-band inputs), which fold away only in scalar code.
 // Input: v[t][d*R0 + n0] = x[l1 + LI*n0] with l1 = g + G*d.
 // Output: v[t][d*RF + e] = X[lF + LF*e] with lF = g + G*d.
-template <class P, int DIR, int NT, int TS, int STR, class SyncF>
+template <class P, int DIR, int NT, int TS, int STR, bool PK1 = true, class SyncF>
 __device__ __forceinline__ void fft_run(float2 (&v)[NT][P::V], float2* buf, int off, int g,
                                         const float2* __restrict__ tw, SyncF SYNC) {
   constexpr int V = P::V, G = P::G, R0 = P::R0, R1 = P::R1, R2 = P::R2;
   // ---- stage 1: DFT-R0 over n0
 #pragma unroll
-  for (int t = 0; t < NT; ++t) dft_groups<R0, DIR>(v[t]);
+  for (int t = 0; t < NT; ++t) dft_groups<R0, DIR, PK1>(v[t]);
   // ---- exchange 1: write Y1[k0; l1] at k0*E1S + l1
 #pragma unroll
   for (int t = 0; t < NT; ++t)
@@ -324,7 +393,7 @@ __device__ __forceinline__ void fft_run(float2 (&v)[NT][P::V], float2* buf, int 
   }
   // ---- stage 2: DFT-R1 over n1
 #pragma unroll
-  for (int t = 0; t < NT; ++t) dft_groups<R1, DIR>(v[t]);
+  for (int t = 0; t < NT; ++t) dft_groups<R1, DIR, true>(v[t]);
   if constexpr (P::STAGES == 3) {
     SYNC();  // every thread finished reading exchange 1
     // twiddle W_N^{n2 (k0 + R0 k1)} and exchange 2: write at n2*E2S + l3, l3 = k0 + R0*k1
@@ -353,7 +422,7 @@ __device__ __forceinline__ void fft_run(float2 (&v)[NT][P::V], float2* buf, int 
         for (int n2 = 0; n2 < R2; ++n2) v[t][d * R2 + n2] = buf[t * TS + (n2 * P::E2S + l3) * STR + off];
       }
 #pragma unroll
-    for (int t = 0; t < NT; ++t) dft_groups<R2, DIR>(v[t]);
+    for (int t = 0; t < NT; ++t) dft_groups<R2, DIR, true>(v[t]);
   }
 }
 

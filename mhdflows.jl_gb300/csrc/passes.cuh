@@ -228,7 +228,7 @@ __global__ void __launch_bounds__(TX * P0::G, MINB)
           v[0][d * P::R0 + n0] = cur[(g + rmin) * TX + tx];
       }
     __syncthreads();  // cur is now free: reuse it as the exchange buffer
-    fft_run<P, DIR, 1, 0, TX>(v, cur, tx, g, tw, BlockSync{});
+    fft_run<P, DIR, 1, 0, TX, !PIN>(v, cur, tx, g, tw, BlockSync{});
     if (kxg < geo.kx) {
       float2* dst = a.dst + br.list[inst] * a.dI + f * a.dF + (long long)o * a.dO + kxg;
 #pragma unroll
@@ -419,7 +419,7 @@ __global__ void __launch_bounds__(TX * P0::G, MINB)
           v[0][d * P::R0 + n0] = cur[(g + rmin) * TX + tx];
       }
     __syncthreads();  // cur is now free: reuse it as the exchange buffer
-    fft_run<P, DIR, 1, 0, TX>(v, cur, tx, g, tw, BlockSync{});
+    fft_run<P, DIR, 1, 0, TX, !PIN>(v, cur, tx, g, tw, BlockSync{});
     if (kxg < geo.kx) {
       float2* dst = a.dst + br.list[inst] * a.dI + f * a.dF + (long long)o * a.dO + kxg;
 #pragma unroll
@@ -631,12 +631,12 @@ __global__ void __launch_bounds__(GROUPS * XCfg<P>::TPG, MINB)
       else load_herm_pair<P, KX>(v[t], rin + (2 * t) * kxp, rin + (2 * t + 1) * kxp, g);
     }
     if constexpr (NTI == 3) {
-      fft_run<P, +1, 3, TS, 1>(v, sb, 0, g, tw, sync);
+      fft_run<P, +1, 3, TS, 1, false>(v, sb, 0, g, tw, sync);
       sync();
     } else {
 #pragma unroll
       for (int t = 0; t < NINV; ++t) {
-        fft_run<P, +1, 1, TS, 1>(reinterpret_cast<float2(&)[1][V]>(v[t]), sb, 0, g, tw, sync);
+        fft_run<P, +1, 1, TS, 1, false>(reinterpret_cast<float2(&)[1][V]>(v[t]), sb, 0, g, tw, sync);
         sync();
       }
     }
@@ -769,7 +769,7 @@ __global__ void __launch_bounds__(ROWS * P::G) x_c2r_kernel(const float2* src, f
   const long long q = (long long)blockIdx.x * ROWS + r;
   float2 v[1][V];
   load_herm_pair<P, kept_kx_of(P::N)>(v[0], src + (2 * q) * srow, src + (2 * q + 1) * srow, g);
-  fft_run<P, +1, 1, TS, 1>(v, smem + r * TS, 0, g, tw, RowSync<G>{1 + r});
+  fft_run<P, +1, 1, TS, 1, false>(v, smem + r * TS, 0, g, tw, RowSync<G>{1 + r});
   float* da = dst + (2 * q) * N;
   float* db = dst + (2 * q + 1) * N;
 #pragma unroll
