@@ -79,3 +79,31 @@ def test_autotune_selects_and_steps_alike(pkg, n):
         got = b.sol_c()
         assert pkg.autotune(b, persist=False) == chosen  # known result: applied without timing
     assert _rel(got, ref) < TOL
+
+
+def test_x_variants_give_the_same_cfl_dt(pkg):
+    """The x-row kernels also reduce max|u| and max|B| for the on-device CFL step: every x
+    variant at 256^3 (the paired-transform ones included) yields the default variant's dt."""
+    from importlib import import_module
+
+    ic = import_module(pkg.__name__ + ".ic")
+    n = 256
+    s0 = ic.random_spectrum_state(n, seed=13)
+    with pkg.Problem(pkg.GPU(0), nx=n, Lx=2 * math.pi, nu=1e-4, eta=1e-4, dt=1e-3, stepper="RK4") as prob:
+        names = pkg.variants(prob)["x_fused"][1]
+        dts = {}
+        for i, name in enumerate(names):
+            try:
+                pkg.select_variant(prob, "x_fused", i)
+            except pkg.MHDError:
+                continue
+            prob.set_sol(s0.T)
+            prob.clock.t, prob.clock.step, prob.clock.dt = 0.0, 0, 1e-3
+            pkg._lib.check(prob._lib.mhd_set_cfl(prob.handle, 1, 0.3))
+            pkg.stepforward(prob, 1)
+            dts[name] = prob.clock.dt
+            pkg._lib.check(prob._lib.mhd_set_cfl(prob.handle, 0, 0.3))
+        ref = dts[names[0]]
+        assert len(dts) >= 3
+        for name, dt in dts.items():
+            assert dt == pytest.approx(ref, rel=1e-5), name
