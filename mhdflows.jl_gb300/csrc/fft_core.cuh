@@ -353,11 +353,12 @@ struct PlanTw {
 // Executes stages of plan P on NT independent transforms held as v[t][V] by this thread.
 // Shared memory word address of logical element a for transform t is  buf[t*TS + a*STR + OFF].
 // SYNC() must be a barrier over every thread that shares buf.  tw is the plan's PlanTw table.
+// TWS: tw lies in shared memory (plain loads).
 // PK1: the first stage in paired arithmetic; false where its inputs hold compile-time zeros
 // (pruned alias-band inputs), which fold away only in scalar code.
 // Input: v[t][d*R0 + n0] = x[l1 + LI*n0] with l1 = g + G*d.
 // Output: v[t][d*RF + e] = X[lF + LF*e] with lF = g + G*d.
-template <class P, int DIR, int NT, int TS, int STR, bool PK1 = true, class SyncF>
+template <class P, int DIR, int NT, int TS, int STR, bool PK1 = true, bool TWS = false, class SyncF>
 __device__ __forceinline__ void fft_run(float2 (&v)[NT][P::V], float2* buf, int off, int g,
                                         const float2* __restrict__ tw, SyncF SYNC) {
   constexpr int V = P::V, G = P::G, R0 = P::R0, R1 = P::R1, R2 = P::R2;
@@ -382,7 +383,7 @@ __device__ __forceinline__ void fft_run(float2 (&v)[NT][P::V], float2* buf, int 
 #pragma unroll
     for (int n1 = 0; n1 < R1; ++n1) {
       float2 w = make_float2(1.f, 0.f);
-      if (n1 != 0) w = ldtw(tw, n1 * R0 + k0);  // W_{R0R1}^{n1 k0}
+      if (n1 != 0) w = TWS ? tw[n1 * R0 + k0] : ldtw(tw, n1 * R0 + k0);  // W_{R0R1}^{n1 k0}
 #pragma unroll
       for (int t = 0; t < NT; ++t) {
         float2 a = buf[t * TS + (k0 * P::E1S + n1 * R2 + n2) * STR + off];
@@ -404,7 +405,8 @@ __device__ __forceinline__ void fft_run(float2 (&v)[NT][P::V], float2* buf, int 
 #pragma unroll
       for (int k1 = 0; k1 < R1; ++k1) {
         const int l3 = k0 + R0 * k1;
-        const float2 w = ldtw(tw, PlanTw<P>::T2 + k1 * (R0 * R2) + l2);  // W_N^{n2 l3}
+        const int j = PlanTw<P>::T2 + k1 * (R0 * R2) + l2;
+        const float2 w = TWS ? tw[j] : ldtw(tw, j);  // W_N^{n2 l3}
 #pragma unroll
         for (int t = 0; t < NT; ++t) {
           const float2 a = cmul_cs<DIR>(v[t][d * R1 + k1], w.x, w.y);

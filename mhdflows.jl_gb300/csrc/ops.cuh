@@ -268,16 +268,17 @@ class Ops : public OpsBase {
   }
 
   // column passes (y and z): plan C, TX kx columns per tile, MINB CTAs per SM, NBUF tile buffers
-  template <class C, int TX, int MINB, int NBUF = 2>
+  // TWS: stage twiddles in shared memory (behind the tiles)
+  template <class C, int TX, int MINB, int NBUF = 2, bool TWS = false>
   void add_col() {
     ColVariant c;
     c.name = "col:" + plan_name<C>() + "/tx" + std::to_string(TX) + "/b" + std::to_string(MINB) +
-             (NBUF == 2 ? std::string() : "/q" + std::to_string(NBUF));
-    c.inv = col_pass_kernel<C, TX, +1, true, false, MINB, NBUF>;
-    c.fwd = col_pass_kernel<C, TX, -1, false, true, MINB, NBUF>;
+             (NBUF == 2 ? std::string() : "/q" + std::to_string(NBUF)) + (TWS ? "/ts" : "");
+    c.inv = col_pass_kernel<C, TX, +1, true, false, MINB, NBUF, TWS>;
+    c.fwd = col_pass_kernel<C, TX, -1, false, true, MINB, NBUF, TWS>;
     c.threads = TX * C::G;
     c.tx = TX;
-    c.smem = sizeof(float2) * NBUF * (size_t)N * TX;
+    c.smem = sizeof(float2) * (NBUF * (size_t)N * TX + (TWS ? PlanTw<C>::SIZE : 0));
     c.tw = twiddles<C>();
     cv.push_back(c);
   }

@@ -143,8 +143,10 @@ __device__ __forceinline__ void col_prefetch(float2* buf, const float2* src, lon
   }
 }
 
-// NBUF tile buffers: NBUF - 1 tiles are being fetched while one is transformed.
-template <class P0, int TX, int DIR, bool PIN, bool POUT, int MINB, int NBUF>
+// NBUF tile buffers: NBUF - 1 tiles are being fetched while one is transformed.  TWS: the
+// stage twiddles are copied into shared memory behind the tile buffers (plain shared loads in
+// the exchanges instead of read-only global loads).
+template <class P0, int TX, int DIR, bool PIN, bool POUT, int MINB, int NBUF, bool TWS = false>
 __global__ void __launch_bounds__(TX * P0::G, MINB)
     col_pass_kernel(ColArgs a, Geom geo, ColWork w, BatchRef br, const float2* __restrict__ tw) {
   static_assert(NBUF >= 2 && NBUF <= 4, "two to four tile buffers");
@@ -186,9 +188,20 @@ __global__ void __launch_bounds__(TX * P0::G, MINB)
     c.inst += gstep.inst + carry;
     return c;
   };
+  // instance offsets: list lookups only when the instance changes (a dependent global load on
+  // every tile's address otherwise)
+  int src_inst = -1, dst_inst = -1;
+  long long src_off = 0, dst_off = 0;
   auto tile_src = [&](const Cur& c) {
-    return a.src + br.list[c.inst] * a.sI + c.f * a.sF + (long long)c.o * a.sO;
+    if (c.inst != src_inst) {
+      src_inst = c.inst;
+      src_off = br.list[c.inst] * a.sI;
+    }
+    return a.src + src_off + c.f * a.sF + (long long)c.o * a.sO;
   };
+  float2* tws = smem + NBUF * (N * TX);
+  if constexpr (TWS)
+    for (int i = threadIdx.x; i < PlanTw<P0>::SIZE; i += NT) tws[i] = __ldg(tw + i);
   int t = blockIdx.x;
   Cur cur_t = decompose(t);
   // prologue: the first NBUF - 1 tiles of this CTA (one commit group each, empty past the end)
@@ -228,9 +241,13 @@ __global__ void __launch_bounds__(TX * P0::G, MINB)
           v[0][d * P::R0 + n0] = cur[(g + rmin) * TX + tx];
       }
     __syncthreads();  // cur is now free: reuse it as the exchange buffer
-    fft_run<P, DIR, 1, 0, TX, !PIN>(v, cur, tx, g, tw, BlockSync{});
+    fft_run<P, DIR, 1, 0, TX, !PIN, TWS>(v, cur, tx, g, TWS ? tws : tw, BlockSync{});
     if (kxg < geo.kx) {
-      float2* dst = a.dst + br.list[inst] * a.dI + f * a.dF + (long long)o * a.dO + kxg;
+      if (inst != dst_inst) {
+        dst_inst = inst;
+        dst_off = br.list[inst] * a.dI;
+      }
+      float2* dst = a.dst + dst_off + f * a.dF + (long long)o * a.dO + kxg;
 #pragma unroll
       for (int d = 0; d < P::DF; ++d) {
         const int base = (g + G * d) * dR;
@@ -392,6 +409,8 @@ __global__ void __launch_bounds__(TX * P0::G, MINB)
     tp += gridDim.x;
     pre_t = advance(pre_t);
   }
+  int dst_inst = -1;
+  long long dst_off = 0;
   int it = 0;
   for (; t < total; t += gridDim.x, ++it) {
     if (tp < total) { issue(pre_t, (it + NBUF - 1) % NBUF); ++issued; }
@@ -421,7 +440,11 @@ __global__ void __launch_bounds__(TX * P0::G, MINB)
     __syncthreads();  // cur is now free: reuse it as the exchange buffer
     fft_run<P, DIR, 1, 0, TX, !PIN>(v, cur, tx, g, tw, BlockSync{});
     if (kxg < geo.kx) {
-      float2* dst = a.dst + br.list[inst] * a.dI + f * a.dF + (long long)o * a.dO + kxg;
+      if (inst != dst_inst) {  // list lookup only when the instance changes
+        dst_inst = inst;
+        dst_off = br.list[inst] * a.dI;
+      }
+      float2* dst = a.dst + dst_off + f * a.dF + (long long)o * a.dO + kxg;
 #pragma unroll
       for (int d = 0; d < P::DF; ++d) {
         const int base = (g + G * d) * dR;
