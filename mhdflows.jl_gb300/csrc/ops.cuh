@@ -284,17 +284,18 @@ class Ops : public OpsBase {
   }
 
   // TMA-fed column passes (16 kx columns: 128-byte box rows keep every box destination aligned)
-  template <class C, int MINB, int NBUF>
+  template <class C, int MINB, int NBUF, bool TWS = false>
   void add_col_tma() {
     constexpr int TX = 16;
     ColVariant c;
     c.name = "coltma:" + plan_name<C>() + "/tx" + std::to_string(TX) + "/b" + std::to_string(MINB) + "/q" +
-             std::to_string(NBUF);
-    c.inv_tma = col_pass_tma_kernel<C, TX, +1, true, false, MINB, NBUF>;
-    c.fwd_tma = col_pass_tma_kernel<C, TX, -1, false, true, MINB, NBUF>;
+             std::to_string(NBUF) + (TWS ? "/ts" : "");
+    c.inv_tma = col_pass_tma_kernel<C, TX, +1, true, false, MINB, NBUF, TWS>;
+    c.fwd_tma = col_pass_tma_kernel<C, TX, -1, false, true, MINB, NBUF, TWS>;
     c.threads = TX * C::G;
     c.tx = TX;
-    c.smem = sizeof(float2) * NBUF * (size_t)N * TX + NBUF * sizeof(unsigned long long) + 16;
+    c.smem = sizeof(float2) * NBUF * (size_t)N * TX + NBUF * sizeof(unsigned long long) + 16 +
+             (TWS ? sizeof(float2) * PlanTw<C>::SIZE : 0);
     c.tw = twiddles<C>();
     cv.push_back(c);
   }

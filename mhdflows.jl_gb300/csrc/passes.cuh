@@ -314,18 +314,22 @@ __device__ __forceinline__ void tma_load5(unsigned int dst, const void* map, int
       : "memory");
 }
 
-template <class P0, int TX, int DIR, bool PIN, bool POUT, int MINB, int NBUF>
+// TWS: the stage twiddles are copied into shared memory behind the barriers.
+template <class P0, int TX, int DIR, bool PIN, bool POUT, int MINB, int NBUF, bool TWS = false>
 __global__ void __launch_bounds__(TX * P0::G, MINB)
     col_pass_tma_kernel(ColArgs a, Geom geo, ColWork w, BatchRef br, const float2* __restrict__ tw,
                         const __grid_constant__ CUtensorMap map, TmaCoords tc, int* err) {
   static_assert(NBUF >= 2 && NBUF <= 4, "two to four tile buffers");
   using P = Unpadded<P0>;
   // dynamic shared memory only (its base is then 1024-byte aligned): NBUF tile buffers, then the
-  // NBUF mbarriers and the abort flag
+  // NBUF mbarriers and the abort flag (16 bytes), then with TWS the stage twiddles
   extern __shared__ __align__(128) float2 smem[];
   constexpr int G = P::G, V = P::V, N = P::N, NT = TX * P0::G;
   unsigned long long* bars = reinterpret_cast<unsigned long long*>(smem + NBUF * N * TX);
   volatile int& abort_flag = *reinterpret_cast<volatile int*>(bars + NBUF);
+  float2* tws = smem + NBUF * N * TX + NBUF + 2;
+  if constexpr (TWS)
+    for (int i = threadIdx.x; i < PlanTw<P0>::SIZE; i += NT) tws[i] = __ldg(tw + i);
   constexpr int KP = kept_kx_of(N), KN = kept_kn_of(N);
   const int tx = threadIdx.x % TX, g = threadIdx.x / TX;
   const int per = w.tiles_x * w.outer * w.nf;
@@ -438,7 +442,7 @@ __global__ void __launch_bounds__(TX * P0::G, MINB)
           v[0][d * P::R0 + n0] = cur[(g + rmin) * TX + tx];
       }
     __syncthreads();  // cur is now free: reuse it as the exchange buffer
-    fft_run<P, DIR, 1, 0, TX, !PIN>(v, cur, tx, g, tw, BlockSync{});
+    fft_run<P, DIR, 1, 0, TX, !PIN, TWS>(v, cur, tx, g, TWS ? tws : tw, BlockSync{});
     if (kxg < geo.kx) {
       if (inst != dst_inst) {  // list lookup only when the instance changes
         dst_inst = inst;
