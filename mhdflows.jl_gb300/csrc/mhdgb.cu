@@ -16,7 +16,10 @@
 #include <sys/stat.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
+#include <condition_variable>
+#include <functional>
 #include <cstdint>
 #include <cstdio>
 #include <cstdlib>
@@ -500,7 +503,7 @@ struct mhd_problem {
   int herm(const float2* X, BatchRef br) {
     return launch(KC_HERM, [&] {
       const int bxh = g.k2 <= 256 ? (g.k2 + 31) / 32 * 32 : 256;
-      const dim3 gh((g.k2 + bxh - 1) / bxh, g.k2, cap);
+      const dim3 gh((g.k2 + bxh - 1) / bxh, g.k2, 6 * cap);
       herm_kx0_kernel<<<gh, bxh, 0, stream>>>(X, aux, g, FS(), ST(), FS(), br);
     });
   }
@@ -1089,36 +1092,131 @@ void* mapped_host(const void* p, size_t bytes) {
   return a0.devicePointer;
 }
 
+// Host worker threads for zeroing host memory (created on first use and kept: starting threads
+// on every call costs tens of microseconds each).  run(n, fn) calls fn(i) for i in [0, n) on
+// the workers and the calling thread and returns when every call has finished; one run at a time.
+class HostPool {
+ public:
+  static HostPool& get() {
+    static HostPool* pool = [] {
+      const unsigned hw = std::thread::hardware_concurrency();
+      return new HostPool((int)std::min<unsigned>(16, hw ? hw : 1) - 1);
+    }();
+    return *pool;  // never destroyed: the workers sleep until the process ends
+  }
+  int threads() const { return (int)workers_.size() + 1; }
+  void run(int n, const std::function<void(int)>& fn) {
+    std::lock_guard<std::mutex> one(call_);
+    {
+      std::lock_guard<std::mutex> lk(m_);
+      fn_ = &fn;
+      n_ = n;
+      next_.store(0);
+      busy_ = (int)workers_.size();
+      ++gen_;
+    }
+    cv_.notify_all();
+    drain();
+    std::unique_lock<std::mutex> lk(m_);
+    done_.wait(lk, [&] { return busy_ == 0; });
+    fn_ = nullptr;
+  }
+
+ private:
+  explicit HostPool(int workers) {
+    for (int i = 0; i < workers; ++i) workers_.emplace_back([this] { loop(); });
+    for (auto& t : workers_) t.detach();
+  }
+  void drain() {
+    for (int i = next_.fetch_add(1); i < n_; i = next_.fetch_add(1)) (*fn_)(i);
+  }
+  void loop() {
+    unsigned seen = 0;
+    for (;;) {
+      {
+        std::unique_lock<std::mutex> lk(m_);
+        cv_.wait(lk, [&] { return gen_ != seen; });
+        seen = gen_;
+      }
+      drain();
+      std::lock_guard<std::mutex> lk(m_);
+      if (--busy_ == 0) done_.notify_all();
+    }
+  }
+  std::vector<std::thread> workers_;
+  std::mutex call_, m_;
+  std::condition_variable cv_, done_;
+  const std::function<void(int)>* fn_ = nullptr;
+  int n_ = 0, busy_ = 0;
+  unsigned gen_ = 0;
+  std::atomic<int> next_{0};
+};
+
 // The alias band of a reference-layout state (nf, n, n, nkr) outside the retained band (the
 // complement of scatter_retained_kernel) has three parts per field: the z-planes of the alias
-// band [kp, n - kn), a block of alias rows [kp, n - kn) in every kept z-plane, and the tail
-// kx >= Kx of every kept row.  zero_row_tails zeroes the tails on host threads; the planes and
-// row blocks go to the copy engine (zero_alias_blocks).
-void zero_row_tails(float2* ref, const Geom& g, int nf) {
+// band [kp, n - kn) (one contiguous block), a block of alias rows [kp, n - kn) in every kept
+// z-plane, and the tail kx >= Kx of every kept row.  zero_alias_host zeroes the tails on the
+// host pool, and the alias z-planes (planes_too) and row blocks (blocks) when asked, in pieces
+// of about 1 MB; zero_alias_blocks writes the others from the copy engine.
+void zero_alias_host(float2* ref, const Geom& g, int nf, bool planes_too, bool blocks) {
   const size_t nkr = g.n / 2 + 1, row = nkr * sizeof(float2), plane = (size_t)g.n * row;
   const size_t tail = (nkr - g.kx) * sizeof(float2);
-  const int planes = nf * g.k2;  // kept z-planes of every field
-  auto zero_plane = [&](int q) {
+  const size_t na = (size_t)(g.n - g.kp - g.kn);
+  char* base = reinterpret_cast<char*>(ref);
+  struct Piece { char* p; size_t bytes; };
+  std::vector<Piece> big;                 // contiguous pieces
+  constexpr size_t kChunk = size_t(1) << 20;
+  if (planes_too)
+    for (int f = 0; f < nf; ++f) {
+      char* p = base + ((size_t)f * g.n + g.kp) * plane;  // alias z-planes
+      for (size_t left = na * plane; left > 0;) {
+        const size_t b = std::min(left, kChunk);
+        big.push_back({p, b});
+        p += b;
+        left -= b;
+      }
+    }
+  const int planes = nf * g.k2;  // kept z-planes: alias row block and row tails
+  const int per_task = std::max(1, (int)(kChunk / (na * row + (size_t)g.k2 * tail)));
+  const int ptasks = (planes + per_task - 1) / per_task;
+  auto kept_plane = [&](int q) {
     const int f = q / g.k2, jz = q % g.k2;
-    char* p = reinterpret_cast<char*>(ref) + ((size_t)f * g.n + freq_of_kept(g, jz)) * plane;
+    char* p = base + ((size_t)f * g.n + freq_of_kept(g, jz)) * plane;
+    if (blocks) std::memset(p + (size_t)g.kp * row, 0, na * row);
     for (int j = 0; j < g.k2; ++j) std::memset(p + (size_t)freq_of_kept(g, j) * row + g.kx * sizeof(float2), 0, tail);
   };
-  // one thread per 4 MB of tails, at most 16 and at most the hardware threads
-  const size_t bytes = (size_t)planes * g.k2 * tail;
-  const unsigned hw = std::thread::hardware_concurrency();
-  const int nt = (int)std::min<size_t>(std::max<size_t>(1, std::min<size_t>(16, bytes >> 22)), hw ? hw : 1);
-  auto work = [&](int t) {
-    for (int q = t; q < planes; q += nt) zero_plane(q);
-  };
-  std::vector<std::thread> pool;
-  for (int t = 1; t < nt; ++t) pool.emplace_back(work, t);
-  work(0);
-  for (auto& th : pool) th.join();
+  const int nbig = (int)big.size();
+  HostPool::get().run(nbig + ptasks, [&](int i) {
+    if (i < nbig) {
+      std::memset(big[i].p, 0, big[i].bytes);
+    } else {
+      const int q0 = (i - nbig) * per_task, q1 = std::min(planes, q0 + per_task);
+      for (int q = q0; q < q1; ++q) kept_plane(q);
+    }
+  });
+}
+
+// Which path writes the alias-band zeros of get_state into mapped host memory
+// ($MHDGB_HOST_ZEROS, read once).  The copy engine's zeros share the host link with the retained
+// band (about 193 GB/s device to host); the host pool writes at about 120 GB/s on its own.
+//   split (default) copy engine: the alias z-planes; host pool: the row blocks and row tails
+//   ce     copy engine: the z-planes and the row blocks; host pool: the row tails
+//   host   host pool: everything
+enum class ZeroPath { Split, CopyEngine, Host };
+ZeroPath zero_path() {
+  static const ZeroPath z = [] {
+    const char* e = std::getenv("MHDGB_HOST_ZEROS");
+    if (e && std::strcmp(e, "ce") == 0) return ZeroPath::CopyEngine;
+    if (e && std::strcmp(e, "host") == 0) return ZeroPath::Host;
+    return ZeroPath::Split;
+  }();
+  return z;
 }
 
 // Copy-engine writes of zeros from `zeros` (zbytes of zeroed device memory) into the alias planes
-// and the alias row blocks of a host reference-layout state, on stream s.
-cudaError_t zero_alias_blocks(float2* ref, const Geom& g, int nf, const void* zeros, size_t zbytes, cudaStream_t s) {
+// and (blocks) the alias row blocks of a host reference-layout state, on stream s.
+cudaError_t zero_alias_blocks(float2* ref, const Geom& g, int nf, const void* zeros, size_t zbytes, cudaStream_t s,
+                              bool blocks) {
   const size_t nkr = g.n / 2 + 1, row = nkr * sizeof(float2), plane = (size_t)g.n * row;
   const size_t na = (size_t)(g.n - g.kp - g.kn);
   char* base = reinterpret_cast<char*>(ref);
@@ -1132,6 +1230,7 @@ cudaError_t zero_alias_blocks(float2* ref, const Geom& g, int nf, const void* ze
       p += b;
       left -= b;
     }
+    if (!blocks) continue;
     // the alias row block of every kept z-plane: width na rows, one plane apart, in groups of
     // planes that fit the zero buffer
     const size_t width = na * row;
@@ -1152,9 +1251,9 @@ cudaError_t zero_alias_blocks(float2* ref, const Geom& g, int nf, const void* ze
 // move their bytes ($MHDGB_HOST_TRANSFER, read once; other host memory always takes the copy path):
 //   mapped (default) kernels read and write the caller's array directly: set_state gathers the
 //          retained band of half the fields over the link while the copy engine brings the other
-//          half; get_state writes the alias-band zeros from the copy engine (whole planes and row
-//          blocks, from a zeroed device buffer) and from host threads (the tail of each kept row)
-//          while the step still runs, then the retained band crosses on both paths at once.
+//          half; get_state writes the alias-band zeros from the copy engine (the alias z-planes,
+//          from a zeroed device buffer) and from the host pool (row blocks and row tails) while
+//          the step still runs, then the retained band crosses on both paths at once.
 //   copy   the copy engines only (about 200 GB/s over the host link): set_state copies the
 //          retained band of the caller's array into the device staging array (one 3-D copy per
 //          field and ky / kz range) and gathers it there; get_state scatters into the staging
@@ -1258,15 +1357,17 @@ int mhd_slot_get_state(mhd_handle h, int slot, float* sol) {
       return rc;
   } else if (out) {
     // mapped memory.  The zeros of the alias band do not wait for the step: the copy engine
-    // writes the alias planes and row blocks from a zeroed device buffer on a side stream, and
-    // host threads zero the row tails, both while the handle's stream still runs.  After the
-    // step the retained band (29% of the bytes) crosses on two paths at once: the device writes
-    // the first half of the fields straight into the mapping, and the other half is scattered
-    // into the staging array and brought over by the copy engine.
+    // writes the alias z-planes from a zeroed device buffer on a side stream, and the host pool
+    // zeroes the alias row blocks and row tails, both while the handle's stream still runs
+    // (zero_path).  After the step the retained band (29% of the bytes) crosses on two paths at
+    // once: the device writes the first half of the fields straight into the mapping, and the
+    // other half is scattered into the staging array and brought over by the copy engine.
     if ((rc = h->ensure_zero_source())) return rc;
     const int hf = nf / 2;
     float2* host = reinterpret_cast<float2*>(sol);
-    MHD_CUDA(zero_alias_blocks(host, h->g, nf, h->zeros, h->zbytes, h->zstream));
+    const ZeroPath zp = zero_path();
+    if (zp != ZeroPath::Host)
+      MHD_CUDA(zero_alias_blocks(host, h->g, nf, h->zeros, h->zbytes, h->zstream, zp == ZeroPath::CopyEngine));
     if ((rc = h->launch(KC_OTHER, [&] {
            scatter_retained_kernel<<<1216, 256, 0, h->stream>>>(src + hf * h->sz.fs, h->ref + hf * fref, h->g, nf - hf);
          })))
@@ -1278,7 +1379,7 @@ int mhd_slot_get_state(mhd_handle h, int slot, float* sol) {
            scatter_retained_kernel<<<1216, 256, 0, h->stream>>>(src, out, h->g, hf);
          })))
       return rc;
-    zero_row_tails(host, h->g, nf);
+    zero_alias_host(host, h->g, nf, zp == ZeroPath::Host, zp != ZeroPath::CopyEngine);
     MHD_CUDA(cudaStreamSynchronize(h->zstream));
   } else {
     // the full array is assembled in the staging buffer at HBM speed, zeros included, and comes

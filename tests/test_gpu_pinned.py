@@ -2,9 +2,10 @@
 read and write the mapped buffer directly.  Results must equal the pageable-memory path bit for
 bit; a pageable buffer goes through the staging copy.  From 16 MB up, get_state into mapped
 memory writes only the retained band from the device, the copy engine writes the zeros of the
-alias planes and row blocks, and host threads zero the row tails (n = 96 and the HD n = 128
-case); smaller buffers are written whole by the device (n = 32).  MHDGB_HOST_TRANSFER=copy
-selects the copy-engine path for mapped buffers too (checked in a child process)."""
+alias z-planes, and host threads zero the alias row blocks and row tails (n = 96 and the HD
+n = 128 case); smaller buffers are written whole by the device (n = 32).
+MHDGB_HOST_TRANSFER=copy selects the copy-engine path for mapped buffers too (checked in a child
+process)."""
 import ctypes as C
 import math
 import os
