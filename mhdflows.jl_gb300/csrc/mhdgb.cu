@@ -14,6 +14,7 @@
 #include <cudaTypedefs.h>
 
 #include <sys/stat.h>
+#include <unistd.h>
 
 #include <algorithm>
 #include <atomic>
@@ -1095,14 +1096,20 @@ void* mapped_host(const void* p, size_t bytes) {
 // Host worker threads for zeroing host memory (created on first use and kept: starting threads
 // on every call costs tens of microseconds each).  run(n, fn) calls fn(i) for i in [0, n) on
 // the workers and the calling thread and returns when every call has finished; one run at a time.
+// A forked child has none of its parent's workers, so a process gets its own pool.
 class HostPool {
  public:
   static HostPool& get() {
-    static HostPool* pool = [] {
+    static std::mutex mk;
+    static HostPool* pool = nullptr;
+    static pid_t owner = 0;
+    std::lock_guard<std::mutex> lk(mk);
+    if (!pool || owner != getpid()) {
       const unsigned hw = std::thread::hardware_concurrency();
-      return new HostPool((int)std::min<unsigned>(16, hw ? hw : 1) - 1);
-    }();
-    return *pool;  // never destroyed: the workers sleep until the process ends
+      pool = new HostPool((int)std::min<unsigned>(16, hw ? hw : 1) - 1);  // never destroyed: the
+      owner = getpid();                                                   // workers sleep until exit
+    }
+    return *pool;
   }
   int threads() const { return (int)workers_.size() + 1; }
   void run(int n, const std::function<void(int)>& fn) {
