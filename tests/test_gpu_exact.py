@@ -32,9 +32,9 @@ def _set_fields(prob, fields):
         prob.set_physical_c(f, np.asarray(a, dtype=np.float32))
 
 
-@pytest.mark.parametrize("stepper", ["RK4", "LSRK4"])
-def test_abc_flow_decays_exactly(pkg, mo, stepper):
-    n, nu, dt, steps = 64, 0.02, 0.005, 200
+@pytest.mark.parametrize("n,stepper,steps", [(64, "RK4", 200), (64, "LSRK4", 200), (256, "RK4", 50)])
+def test_abc_flow_decays_exactly(pkg, mo, n, stepper, steps):
+    nu, dt = 0.02, 0.005
     g = mo.Grid(n)
     x, y, z = g.mesh()
     A, B, C = 1.0, 0.7, 0.4
@@ -53,7 +53,7 @@ def test_abc_flow_decays_exactly(pkg, mo, stepper):
     expect = s0 * math.exp(-nu * t)
     m = g.retained_mask()
     err_u = mo.rel_l2(got[:3], expect[:3], m)
-    print(f"ABC {stepper}: u rel L2 {err_u:.2e} after {steps} steps; B max {np.abs(got[3:]).max():.1e}")
+    print(f"ABC {n}^3 {stepper}: u rel L2 {err_u:.2e} after {steps} steps; B max {np.abs(got[3:]).max():.1e}")
     assert err_u < 1e-5
     assert np.abs(got[3:]).max() < 1e-6 * np.abs(got[:3]).max()
     assert e1 / e0 == pytest.approx(math.exp(-2 * nu * t), rel=1e-5)
