@@ -14,6 +14,10 @@ OpsBase* make_ops_512() {
   o->add_col<Plan<512, 32, 16, 8, 4>, 16, 1, 2, true>();
   o->add_col<Plan<512, 32, 16, 8, 4>, 8, 2, 2, true>();
   o->add_col_tma<Plan<512, 32, 16, 8, 4>, 1, 2, true>();
+  o->add_col<Plan<512, 16, 32, 16>, 16, 1, 2, true>();
+  o->add_col<Plan<512, 16, 32, 16>, 16, 1, 3, true>();
+  o->add_col_tma<Plan<512, 16, 32, 16>, 1, 2, true>();
+  o->add_col_tma<Plan<512, 16, 32, 16>, 1, 3, true>();
   o->add_x<Plan<512, 64, 8, 8, 8>, 2, 1, 1, 4>();
   o->add_x<Plan<512, 32, 16, 8, 4>, 4, 1, 1, 2>();
   o->add_x<Plan<512, 32, 8, 8, 8>, 4, 1, 1, 2>();
