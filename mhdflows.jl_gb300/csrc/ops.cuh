@@ -167,12 +167,17 @@ class Ops : public OpsBase {
   // transforms per exchange round, MINB CTAs per SM.
   template <class R, int GROUPS, int NTI, int NTF, int MINB>
   void add_x() {
+    add_x_form<R, GROUPS, NTI, NTF, MINB, false>();
+  }
+  // DIRECT: field rows loaded from global memory into registers, no staging copy ("/d")
+  template <class R, int GROUPS, int NTI, int NTF, int MINB, bool DIRECT>
+  void add_x_form() {
     constexpr int NTS = NTI > NTF ? NTI : NTF;
-    using XC = XCfg<R, NTS>;
+    using XC = XCfg<R, NTS, DIRECT>;
     XVariant v;
     v.name = "x:" + plan_name<R>() + "/nt" + std::to_string(NTI) + std::to_string(NTF) + "/c" +
-             std::to_string(GROUPS) + "/b" + std::to_string(MINB);
-    v.fn = x_fused_kernel<R, GROUPS, NTI, NTF, MINB>;
+             std::to_string(GROUPS) + "/b" + std::to_string(MINB) + (DIRECT ? "/d" : "");
+    v.fn = x_fused_kernel<R, GROUPS, NTI, NTF, MINB, 0, false, DIRECT>;
     v.threads = GROUPS * XC::TPG;
     v.rpg = XC::RPG;
     v.groups = GROUPS;

@@ -21,6 +21,7 @@ OpsBase* make_ops_512() {
   o->add_x<Plan<512, 64, 8, 8, 8>, 2, 1, 1, 4>();
   o->add_x<Plan<512, 32, 16, 8, 4>, 4, 1, 1, 2>();
   o->add_x<Plan<512, 32, 8, 8, 8>, 4, 1, 1, 2>();
+  o->add_x_form<Plan<512, 32, 8, 8, 8>, 4, 1, 1, 2, true>();
   o->add_x_vp<Plan<512, 64, 8, 8, 8>, 2, 1, 4>();
   o->add_x_hd<Plan<512, 64, 8, 8, 8>, 2, 4>();
   o->add_x_hdvp<Plan<512, 64, 8, 8, 8>, 2, 4>();

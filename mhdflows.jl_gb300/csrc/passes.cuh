@@ -569,13 +569,15 @@ struct RowCfg {
 // A row group is RPG = max(1, 32/G) consecutive rows handled by one warp (G <= 32) or one row
 // handled by G/32 warps.  Groups are persistent: while a group transforms its rows, cp.async
 // brings the six field rows of its next rows into the other half of a double buffer.
-template <class P, int NTS = 1>
+// DIRECT: the field rows are read from global memory straight into registers (coalesced across
+// the lanes of a row), with no staging copy in shared memory.
+template <class P, int NTS = 1, bool DIRECT = false>
 struct XCfg {
   static constexpr int G = P::G;
   static constexpr int RPG = G >= 32 ? 1 : 32 / G;        // rows per group
   static constexpr int TPG = G >= 32 ? G : 32;            // threads per group
   static constexpr int TS = RowCfg<P>::TS;                // exchange words per transform
-  static __host__ __device__ int stage_words(int kxp) { return RPG * 6 * kxp; }
+  static __host__ __device__ int stage_words(int kxp) { return DIRECT ? 0 : RPG * 6 * kxp; }
   // two staging buffers of the six field rows, then NTS exchange buffers per row
   static __host__ __device__ int group_words(int kxp) { return 2 * stage_words(kxp) + RPG * NTS * TS; }
 };
@@ -590,13 +592,13 @@ struct XCfg {
 // HDX (hydrodynamics, HDcalcN!): three fields in (ux uy | uz), B = 0 folded at compile time, two
 // inverse and three forward transforms; the products are the first five of the MHD set (the
 // sixth slot written is zero).
-template <class P, int GROUPS, int NTI, int NTF, int MINB, int VPM = 0, bool HDX = false>
+template <class P, int GROUPS, int NTI, int NTF, int MINB, int VPM = 0, bool HDX = false, bool DIRECT = false>
 __global__ void __launch_bounds__(GROUPS * XCfg<P>::TPG, MINB)
     x_fused_kernel(float2* pool, Geom geo, long long rowstride, long long slot, long long istride, BatchRef br,
                    const float2* __restrict__ tw, const float2* __restrict__ twr, unsigned int* vmax, VpRef vp) {
   using PR = typename Reverse<P>::type;
   constexpr int NTS = NTI > NTF ? NTI : NTF;
-  using XC = XCfg<P, NTS>;
+  using XC = XCfg<P, NTS, DIRECT>;
   static_assert(NTI == 1 || NTI == 3, "inverse transforms go one or three at a time");
   static_assert(NTF == 1 || NTF == 2 || NTF == 4, "forward transforms go one, two or four at a time");
   static_assert(NTF == 1 || P::G <= 32, "batched forward transforms need the row inside one warp");
@@ -642,15 +644,22 @@ __global__ void __launch_bounds__(GROUPS * XCfg<P>::TPG, MINB)
 
   long long q = (long long)blockIdx.x * GROUPS + grp;
   const long long qstep = (long long)gridDim.x * GROUPS;
-  if (q < ngroups) prefetch(q, gs);
+  if (!DIRECT && q < ngroups) prefetch(q, gs);
   cp_async_commit();
   for (int it = 0; q < ngroups; q += qstep, ++it) {
-    const float2* cur = gs + (it & 1) * sw;
-    if (q + qstep < ngroups) prefetch(q + qstep, gs + ((it + 1) & 1) * sw);
-    cp_async_commit();
-    cp_async_wait<1>();
-    sync();
-    const float2* rin = cur + rr * 6 * kxp;
+    const float2* rin;
+    if constexpr (DIRECT) {
+      // this row's own slots (slot stride == kxp); every lane loads its inputs before any lane
+      // stores an output over them (the stores follow the transforms)
+      rin = group_rows(q) + rr * rowstride;
+    } else {
+      const float2* cur = gs + (it & 1) * sw;
+      if (q + qstep < ngroups) prefetch(q + qstep, gs + ((it + 1) & 1) * sw);
+      cp_async_commit();
+      cp_async_wait<1>();
+      sync();
+      rin = cur + rr * 6 * kxp;
+    }
     float2 v[3][V];
 #pragma unroll
     for (int t = 0; t < NINV; ++t) {
