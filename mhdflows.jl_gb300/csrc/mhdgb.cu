@@ -101,7 +101,7 @@ Geom make_geom(int n, double L) {
 
 // Kernel classes for per-launch timing (KClass of ops.cuh).
 const char* kClassNames[KC_COUNT] = {"z_inverse", "y_inverse", "x_fused", "y_forward", "z_forward", "rk_epilogue",
-                                     "herm_kx0", "other"};
+                                     "other"};
 
 const double kLsA[5] = {0.0, -567301805773.0 / 1357537059087.0, -2404267990393.0 / 2016746695238.0,
                         -3550918686646.0 / 2091501179385.0, -1275806237668.0 / 842570457699.0};
@@ -495,19 +495,19 @@ struct mhd_problem {
     return launch(KC_YFWD, [&] { ops->col(KC_YFWD, a, g, g.n, nf, br, cap, stream, &tm_yfwd); });
   }
   // colbuf slots -> compact planes (nf fields/products) at dst + slot*dI, pruned output
-  int z_forward(float2* dst, long long dI, int nf, BatchRef br) {
+  // hx: the stage state whose kx = 0 Hermitian part the pass also writes into aux (the
+  // right-hand side's call), or nullptr
+  int z_forward(float2* dst, long long dI, int nf, BatchRef br, const float2* hx = nullptr) {
     ColArgs a{colbuf, dst, (long long)g.kxp, SLK(), AZ(), FS(), (long long)g.kxp, (long long)g.k2 * g.kxp, sz.colbuf, dI};
+    a.hx = hx;
+    a.hout = aux;
+    a.hfs = FS();
+    a.hsI = ST();
+    a.hoI = FS();
     return launch(KC_ZFWD, [&] { ops->col(KC_ZFWD, a, g, g.k2, nf, br, cap, stream, &tm_zfwd); });
   }
   // Stage epilogue: RHS from the 8 compact product planes (in rowbuf; 14 with the VP penalty
   // fields) and the stage state X.
-  int herm(const float2* X, BatchRef br) {
-    return launch(KC_HERM, [&] {
-      const int bxh = g.k2 <= 256 ? (g.k2 + 31) / 32 * 32 : 256;
-      const dim3 gh((g.k2 + bxh - 1) / bxh, g.k2, 6 * cap);
-      herm_kx0_kernel<<<gh, bxh, 0, stream>>>(X, aux, g, FS(), ST(), FS(), br);
-    });
-  }
   RkArgs rk_args(const float2* X, float2* xn, int op, float hf, float ca, float cb, int stage) const {
     RkArgs a{};
     a.prod = rowbuf;
@@ -537,10 +537,8 @@ struct mhd_problem {
   // starts by zeroing the velocity right-hand side: a hydrodynamic problem is unforced
   bool forced() const { return forcing && !p.hydro_only; }
   // xn: where the stage update writes (the next stage state, or sol; it may be X itself, so the
-  // Hermitian part of X's kx = 0 plane is copied out first by herm_kx0)
+  // Hermitian part of X's kx = 0 plane was copied out into aux by the z_forward before it)
   int epilogue(const float2* X, float2* xn, int op, float hf, float ca, float cb, BatchRef br, int stage) {
-    int rc = herm(X, br);
-    if (rc) return rc;
     const RkArgs a = rk_args(X, xn, op, hf, ca, cb, stage);
     const int bx = g.kx <= 256 ? (g.kx + 31) / 32 * 32 : 256;
     const dim3 grid((g.kx + bx - 1) / bx, g.k2, g.k2 * cap);
@@ -580,7 +578,7 @@ struct mhd_problem {
     if ((rc = y_inverse(nin, br))) return rc;
     if ((rc = x_fused(br, (record && cfl) ? dvmax : nullptr))) return rc;
     if ((rc = y_forward(nout, br))) return rc;
-    if ((rc = z_forward(rowbuf, sz.rowbuf, nout, br))) return rc;
+    if ((rc = z_forward(rowbuf, sz.rowbuf, nout, br, X))) return rc;
     return epilogue(X, xn, op, hf, ca, cb, br, stage);
   }
   // One step of every active slot (launches only; see run_steps for graphs and clocks).
@@ -1889,9 +1887,8 @@ int mhd_kernel_class_bytes(mhd_handle h, int cls, double* bytes) {
     case KC_YINV: b = nin * (n * k2 * kx * c + n * n * kx * c); break;
     case KC_XFUSED: b = (nin + xout) * n * n * kx * c + vpin; break;
     case KC_YFWD: b = ns * (n * n * kx * c + n * k2 * kx * c); break;
-    case KC_ZFWD: b = ns * (n * k2 * kx * c + state_field); break;
+    case KC_ZFWD: b = ns * (n * k2 * kx * c + state_field) + 2 * 6 * k2 * k2 * c; break;  // + the kx = 0 Hermitian part
     case KC_RKEPI: b = ns * state_field + arrays * nin * state_field + nin * k2 * k2 * c; break;
-    case KC_HERM: b = 2 * 6 * k2 * k2 * c; break;
     default: b = 0;
   }
   *bytes = b * inst;

@@ -20,7 +20,7 @@
 namespace mhdgb {
 
 // Kernel classes of one right-hand-side evaluation (also the per-launch profiling classes).
-enum KClass { KC_ZINV = 0, KC_YINV, KC_XFUSED, KC_YFWD, KC_ZFWD, KC_RKEPI, KC_HERM, KC_OTHER, KC_COUNT };
+enum KClass { KC_ZINV = 0, KC_YINV, KC_XFUSED, KC_YFWD, KC_ZFWD, KC_RKEPI, KC_OTHER, KC_COUNT };
 constexpr int kTunedClasses = 5;  // z_inverse .. z_forward
 
 // Error reporting of the library (defined with the C ABI): stores the message, returns code.

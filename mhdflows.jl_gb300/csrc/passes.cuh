@@ -95,7 +95,39 @@ struct ColArgs {
   long long sF, sO, sR;  // source strides (complex elements): field/slot, outer, row
   long long dF, dO, dR;  // destination strides
   long long sI, dI;      // source / destination slot strides (instances of a size class)
+  // the right-hand side's z_forward only (else hx == nullptr): once its tiles are done, the pass
+  // writes the Hermitian part of the stage state's kx = 0 plane (herm_kx0_items) from the state
+  // pool hx (field stride hfs, slot stride hsI) into hout (slot stride hoI)
+  const float2* hx;
+  float2* hout;
+  long long hfs, hsI, hoI;
 };
+
+// Hermitian part of the kx = 0 plane of the six fields of every active instance:
+// H(k) = (X(k) + conj X(-k)) / 2, with X(-k) = 0 when -k is in the alias band, stored as
+// H[f][kz'][ky'].  The reference's diffusion term is computed from the re-transformed physical
+// field, rfft(irfft(X)), which is exactly this on the kx = 0 plane.  Items (instance, field, kz',
+// ky') with ky' fastest, threads t0, t0 + stride, ... of a grid-stride walk.
+__device__ __forceinline__ void herm_kx0_items(const float2* __restrict__ Xpool, float2* __restrict__ Hpool,
+                                               const Geom& geo, long long fs, long long stI, long long hI,
+                                               BatchRef br, long long t0, long long stride) {
+  const long long pl = (long long)geo.k2 * geo.k2;
+  const long long total = (long long)(*br.count) * 6 * pl;
+  for (long long i = t0; i < total; i += stride) {
+    const int inst = (int)(i / (6 * pl));
+    const long long r = i - inst * 6 * pl;
+    const int c = (int)(r / pl);
+    const long long p = r - c * pl;
+    const int jz = (int)(p / geo.k2), jy = (int)(p - (long long)jz * geo.k2);
+    const int slot = br.list[inst];
+    const float2* X = Xpool + slot * stI + c * fs;
+    const int py = kept_of_signed(geo, -signed_of_kept(geo, jy));
+    const int pz = kept_of_signed(geo, -signed_of_kept(geo, jz));
+    const float2 xk = X[((long long)jz * geo.k2 + jy) * geo.kxp];
+    const float2 q = (py >= 0 && pz >= 0) ? X[((long long)pz * geo.k2 + py) * geo.kxp] : make_float2(0.f, 0.f);
+    Hpool[slot * hI + c * pl + p] = make_float2(0.5f * (xk.x + q.x), 0.5f * (xk.y - q.y));
+  }
+}
 
 // ------------------------------------------------------------------------------------------
 // Column pass: one length-n transform per (field, outer index, kx column); TX columns per tile.
@@ -268,6 +300,8 @@ __global__ void __launch_bounds__(TX * P0::G, MINB)
     __syncthreads();  // all exchange reads of cur done before it is refilled
   }
   cp_async_wait<0>();
+  if (a.hx) herm_kx0_items(a.hx, a.hout, geo, a.hfs, a.hsI, a.hoI, br, (long long)blockIdx.x * NT + threadIdx.x,
+                           (long long)gridDim.x * NT);
 }
 
 // ------------------------------------------------------------------------------------------
@@ -472,6 +506,8 @@ __global__ void __launch_bounds__(TX * P0::G, MINB)
   if (abort_flag && threadIdx.x == 0) {
     for (int k = it; k < issued; ++k) (void)mbar_wait(smem_u32(&bars[k % NBUF]), (unsigned int)((k / NBUF) & 1));
   }
+  if (a.hx) herm_kx0_items(a.hx, a.hout, geo, a.hfs, a.hsI, a.hoI, br, (long long)blockIdx.x * NT + threadIdx.x,
+                           (long long)gridDim.x * NT);
 }
 
 // ------------------------------------------------------------------------------------------

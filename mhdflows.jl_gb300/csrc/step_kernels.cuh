@@ -37,29 +37,6 @@ __global__ void __launch_bounds__(256) rk_epilogue_kernel(RkArgs a, Geom geo, Ba
   finish_mode<OP, FORCED, VPEN, HD>(a, geo, slot, jz, jy, x, i, kxv, kyv, kzv, m, prod);
 }
 
-// Hermitian part of the kx = 0 plane of the six fields: H(k) = (X(k) + conj X(-k)) / 2, with
-// X(-k) = 0 when -k is in the alias band.  The reference's diffusion term is computed from the
-// re-transformed physical field, rfft(irfft(X)), which is exactly this on the kx = 0 plane.
-__global__ void herm_kx0_kernel(const float2* __restrict__ Xpool, float2* __restrict__ Hpool, Geom geo, long long fs,
-                                long long stI, long long hI, BatchRef br) {
-  // grid (ceil(K2 / blockDim.x), K2, 6 cap): one thread per (field, ky', kz') of one instance.
-  // The kx = 0 elements sit one padded row apart, so every load is its own sector: many
-  // threads with two loads each keep enough of them in flight.
-  const int jy = blockIdx.x * blockDim.x + threadIdx.x;
-  const int jz = blockIdx.y;
-  const int inst = blockIdx.z / 6, c = blockIdx.z - 6 * inst;
-  if (jy >= geo.k2 || inst >= *br.count) return;
-  const int slot = br.list[inst];
-  const float2* X = Xpool + slot * stI + c * fs;
-  float2* H = Hpool + slot * hI + c * (long long)geo.k2 * geo.k2;
-  const int py = kept_of_signed(geo, -signed_of_kept(geo, jy));
-  const int pz = kept_of_signed(geo, -signed_of_kept(geo, jz));
-  const bool partner = py >= 0 && pz >= 0;
-  const float2 xk = X[((long long)jz * geo.k2 + jy) * geo.kxp];
-  const float2 q = partner ? X[((long long)pz * geo.k2 + py) * geo.kxp] : make_float2(0.f, 0.f);
-  H[(long long)jz * geo.k2 + jy] = make_float2(0.5f * (xk.x + q.x), 0.5f * (xk.y - q.y));
-}
-
 // On-device getCFL! (src/integrator.jl:158-198 of MHDFlows.jl) after a step of every active
 // slot: t += dt of the step just taken; next dt = min(coef * dx / max(|u|max, |B|max), tdiff)
 // from the maxima x_fused recorded on the step's last stage; the maxima are cleared for the next

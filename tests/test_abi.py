@@ -105,7 +105,7 @@ def test_null_handle_errors(pkg, lib):
     assert lib.mhd_step(None, 1) == pkg._lib.MHD_ERR_INVALID
     assert lib.mhd_destroy(None) == 0
     assert lib.mhd_get_clock(None, None, None, None) == pkg._lib.MHD_ERR_INVALID
-    assert lib.mhd_kernel_class_count() == 8
+    assert lib.mhd_kernel_class_count() == 7
     assert lib.mhd_kernel_class_name(2).decode() == "x_fused"
 
 
