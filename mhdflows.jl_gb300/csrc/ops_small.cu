@@ -54,6 +54,8 @@ OpsBase* make_ops_96() {
   auto* o = new Ops<96>();
   o->add_col<Plan<96, 8, 12, 4, 2>, 16, 2>();
   o->add_col<Plan<96, 8, 12, 4, 2>, 8, 4>();
+  o->add_col<Plan<96, 4, 8, 12>, 32, 4>();
+  o->add_col<Plan<96, 4, 8, 12>, 16, 8>();
   o->add_x<Plan<96, 8, 12, 4, 2>, 4, 1, 1, 2>();
   o->add_x_vp<Plan<96, 8, 12, 4, 2>, 4, 1, 2>();
   o->add_x_hd<Plan<96, 8, 12, 4, 2>, 4, 2>();
