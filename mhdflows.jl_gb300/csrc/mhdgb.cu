@@ -1103,9 +1103,14 @@ class HostPool {
     static pid_t owner = 0;
     std::lock_guard<std::mutex> lk(mk);
     if (!pool || owner != getpid()) {
+      // $MHDGB_HOST_THREADS threads in all (the caller included), else the hardware threads, at
+      // most 16 (on the 16-core Grace host, 8 threads left the zeros of get_state less hidden
+      // behind the step: 4.0-4.4 ms per e2e step against 4.0-4.15 ms, 4 threads 6 ms)
       const unsigned hw = std::thread::hardware_concurrency();
-      pool = new HostPool((int)std::min<unsigned>(16, hw ? hw : 1) - 1);  // never destroyed: the
-      owner = getpid();                                                   // workers sleep until exit
+      int nt = (int)std::min<unsigned>(16, hw ? hw : 1);
+      if (const char* e = std::getenv("MHDGB_HOST_THREADS")) nt = std::max(1, std::min(64, std::atoi(e)));
+      pool = new HostPool(nt - 1);  // never destroyed: the workers sleep until the process ends
+      owner = getpid();
     }
     return *pool;
   }
