@@ -84,8 +84,9 @@ def test_pinned_hydrodynamic_state_overwrites_every_element(pkg, mo, lib):
         lib.mhd_host_free(pin)
 
 
-def test_copy_engine_transfer_mode(pkg):
-    """The same round trip with MHDGB_HOST_TRANSFER=copy (read once per process: a child process)."""
+def _child_roundtrip(env_extra, tag):
+    """A mapped-buffer round trip at n = 96 (21.7 MB: the split zero path) in a child process with
+    extra environment variables (the library reads them once per process)."""
     root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
     code = textwrap.dedent("""
         import ctypes as C, sys
@@ -110,8 +111,20 @@ def test_copy_engine_transfer_mode(pkg):
         lib.mhd_host_free(pin)
         assert np.array_equal(got, ref)
         assert np.array_equal(np.where(g.retained_mask(), 0, got), np.zeros_like(got))
-        print("copy mode ok")
-    """) % root
-    env = dict(os.environ, MHDGB_HOST_TRANSFER="copy")
+        print("%s ok")
+    """) % (root, tag)
+    env = dict(os.environ, **env_extra)
     res = subprocess.run([sys.executable, "-c", code], env=env, capture_output=True, text=True, timeout=600)
-    assert res.returncode == 0 and "copy mode ok" in res.stdout, res.stdout + res.stderr
+    assert res.returncode == 0 and f"{tag} ok" in res.stdout, res.stdout + res.stderr
+
+
+def test_copy_engine_transfer_mode():
+    """The same round trip with MHDGB_HOST_TRANSFER=copy."""
+    _child_roundtrip({"MHDGB_HOST_TRANSFER": "copy"}, "copy mode")
+
+
+@pytest.mark.parametrize("zeros,threads", [("ce", "16"), ("host", "16"), ("split", "3")])
+def test_alias_zero_paths(zeros, threads):
+    """get_state's alias-band zeros from each path (MHDGB_HOST_ZEROS) and a small host pool
+    (MHDGB_HOST_THREADS): a garbage-filled mapped buffer comes back exact."""
+    _child_roundtrip({"MHDGB_HOST_ZEROS": zeros, "MHDGB_HOST_THREADS": threads}, f"zeros {zeros}")
